@@ -1,0 +1,351 @@
+"""Benchmark: frequent patterns per second of the GB300 gSpan miner.
+
+Workload (default): generator configuration 2 -- 100,000 graphs, Poisson(30)
+edges per graph, 5 vertex / 5 edge labels, 50 embedded seed patterns --
+mined at minsup 1% (1000 graphs).  One step = one complete mining pass at
+that support (every frequent pattern of the database enumerated, supports
+counted, canonicality checked, patterns emitted to the host).
+
+value      : patterns / second with the database already resident in HBM
+e2e        : same metric through the C ABI from host arrays: database built from
+             the reference's cudabin arrays, copied to the GPU, mined, patterns
+             emitted to a host callback -- all inside the timed step
+roofline   : the count kernel (k_wave_count, the dominant kernel): algorithmic
+             bytes per launch / kernel time, both measured inside the library on
+             its own stream with CUDA events, against the measured HBM peak
+cpu_baseline: the oracle (C restatement of the reference's sequential gSpan) on
+             one host core, time-bounded sample of the same workload
+
+--impl reference times the reference's CPU implementation (the oracle port,
+since the reference's own sources are not present on the GPU host) on all host
+cores, one process per core over disjoint root subtrees, time-bounded.
+
+Multi-GPU (torchrun, N > 1): every rank mines a disjoint set of root subtrees
+of the same database (no data exchange); the step time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+RANK = int(os.environ.get("RANK", "0"))
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+if WORLD > 1:
+    # one GPU per rank: the native library sees only this rank's device
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
+
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--config", type=int, default=2)
+    p.add_argument("--scale", type=float, default=1.0)
+    p.add_argument("--minsup-frac", type=float, default=0.01)
+    p.add_argument("--wave-nodes", type=int, default=None)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+        self.max_mhz = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        idx = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] if WORLD > 1 else "0"
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", idx, "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                mhz.append(float(s[0]))
+                mx = float(s[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, s[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        mhz.sort()
+        med = mhz[len(mhz) // 2] if mhz else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def cudabin_arrays(db, tmpdir):
+    """The reference's flat cudabin arrays of a database (host memory)."""
+    import numpy as np
+    p = os.path.join(tmpdir, "db.cudabin")
+    db.write(p, "cudabin")
+    raw = np.fromfile(p, dtype=np.int32)
+    os.remove(p)
+    n, esz, maxv, vc = (int(x) for x in raw[:4])
+    o = 4
+    arrs = {}
+    arrs["edges"] = raw[o:o + esz].copy(); o += esz
+    arrs["edges_labels"] = raw[o:o + esz].copy(); o += esz
+    arrs["vertex_labels"] = raw[o:o + n * maxv].copy(); o += n * maxv
+    arrs["vertex_offsets"] = raw[o:o + n * maxv + 1].copy()
+    return n, esz, maxv, vc, arrs
+
+
+def run_oracle_sample(db_txt, minsup, seconds, part=None):
+    oracle = os.path.join(REPO, "oracle", "_build", "gspan_oracle")
+    if not os.path.exists(oracle):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle")])
+    cmd = [oracle, "txt", db_txt, str(minsup), "-", "--time-limit", str(seconds)]
+    if part is not None:
+        cmd += ["--roots", "%d/%d" % part]
+    return subprocess.Popen(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+
+
+def parse_oracle(stderr):
+    d = {}
+    for tok in stderr.split():
+        if "=" in tok:
+            k, v = tok.split("=", 1)
+            d[k] = v
+    return float(d.get("total_time", "nan")), int(float(d.get("total_frequent_graphs", "0"))), "stopped" in d
+
+
+def cpu_oracle(db_txt, minsup, seconds, cores):
+    t0 = time.time()
+    procs = [run_oracle_sample(db_txt, minsup, seconds, (i, cores) if cores > 1 else None) for i in range(cores)]
+    res = [parse_oracle(p.communicate()[1]) for p in procs]
+    wall = time.time() - t0
+    elapsed = max(r[0] for r in res)
+    pats = sum(r[1] for r in res)
+    stopped = any(r[2] for r in res)
+    return pats, elapsed, stopped, wall
+
+
+def main():
+    a = parse()
+    import gpu_graph_mining_gb300 as g
+    if not os.path.exists(g.LIB_PATH):
+        from gpu_graph_mining_gb300 import build as b
+        b.build()
+
+    workload = "config%d: generator configuration %d x%.3g, minsup %.2f%%" % (a.config, a.config, a.scale,
+                                                                             100 * a.minsup_frac)
+    metric = "frequent patterns/sec"
+    unit = "patterns/s"
+    db = g.Database.generate(a.config, scale=a.scale)
+    minsup = max(1, int(round(a.minsup_frac * len(db))))
+    info = db.info()
+    config = {"workload": workload, "graphs": info["graphs"], "vertices": info["vertices"],
+              "adjacency_entries": info["adjacency_entries"], "minsup": minsup,
+              "l2": "flushed between steps (256 MiB write)"}
+
+    if a.impl == "reference":
+        if RANK != 0:
+            return
+        cores = os.cpu_count() or 1
+        with tempfile.TemporaryDirectory() as td:
+            p = os.path.join(td, "db.txt")
+            db.write(p, "txt")
+            for _ in range(a.warmup):  # short warm-up samples (page cache, CPU clocks)
+                cpu_oracle(p, minsup, 1.0, cores)
+            vals = []
+            t_all = 0.0
+            for _ in range(a.steps):
+                pats, el, stopped, wall = cpu_oracle(p, minsup, a.cpu_seconds, cores)
+                vals.append(pats / el if el > 0 else 0.0)
+                t_all += el
+        v = sum(vals) / len(vals)
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": 0, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": 1000 * t_all / a.steps, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port",
+                                 "sample": "oracle (C restatement of src/gspan) on the full database at the same "
+                                           "minsup, one process per core over disjoint root subtrees, each stopped "
+                                           "after %.0f s; patterns found / elapsed" % a.cpu_seconds},
+                "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    dist = None
+    if WORLD > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(0)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda:0")
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    part = dict(root_part=RANK, root_parts=WORLD) if WORLD > 1 else {}
+    db.upload()
+    # warm-up (also creates the engine's pool and scratch)
+    for _ in range(max(3, a.warmup)):
+        g.mine(db, minsup, wave_nodes=a.wave_nodes, collect=False, **part)
+
+    # ---- resident-database timing
+    clocks = Clocks()
+    clocks.start()
+    times, stats_all = [], []
+    n_patterns = None
+    for _ in range(a.steps):
+        flush_buf.fill_(1)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        counted = [0]
+        _, st = g.mine(db, minsup, wave_nodes=a.wave_nodes, collect=False,
+                       sink=lambda c, s: counted.__setitem__(0, counted[0] + 1), **part)
+        e1.record()
+        barrier()
+        times.append(e0.elapsed_time(e1))
+        stats_all.append(st)
+        n_patterns = counted[0]
+    clk = clocks.stop()
+    ms = sum(times) / len(times)
+    pats_local = n_patterns
+    if dist:
+        t = torch.tensor([ms, float(pats_local)], device=dev)
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        ms_job, pats_job = float(mx[0]), int(sm[1])
+    else:
+        ms_job, pats_job = ms, pats_local
+    value = pats_job / (ms_job / 1000.0)
+
+    # roofline of the count kernel (mean over timed steps)
+    cb = sum(s["count_bytes"] for s in stats_all) / len(stats_all)
+    cms = sum(s["count_ms"] for s in stats_all) / len(stats_all)
+    mb = sum(s["mat_bytes"] for s in stats_all) / len(stats_all)
+    mms = sum(s["mat_ms"] for s in stats_all) / len(stats_all)
+    peak, peak_kind = peaks()
+    waves = sum(s["waves"] for s in stats_all) / len(stats_all)
+    achieved = (cb / (cms / 1000.0)) / 1e9 if cms > 0 else 0.0
+    launches_per_step = sum(s["launches"] for s in stats_all) / len(stats_all)
+
+    # ---- end-to-end through the C ABI from host arrays
+    e2e_times, h2d, d2h = [], 0, 0
+    with tempfile.TemporaryDirectory() as td:
+        n, esz, maxv, vc, arrs = cudabin_arrays(db, td)
+        import ctypes
+        import numpy as np
+        P = ctypes.POINTER(ctypes.c_int32)
+
+        def ptr(x):
+            return x.ctypes.data_as(P)
+        for i in range(a.steps + 1):
+            flush_buf.fill_(1)
+            barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            st = ctypes.c_int32(0)
+            h = g.lib().gs_db_from_arrays(n, esz, maxv, vc, ptr(arrs["edges"]), ptr(arrs["edges_labels"]),
+                                          ptr(arrs["vertex_labels"]), ptr(arrs["vertex_offsets"]), ctypes.byref(st))
+            d = g.Database(h)
+            counted = [0]
+            _, s = g.mine(d, minsup, wave_nodes=a.wave_nodes, collect=False,
+                          sink=lambda c, s_: counted.__setitem__(0, counted[0] + 1), **part)
+            d.free()
+            e1.record()
+            barrier()
+            if i > 0:  # the first pass is a warm-up
+                e2e_times.append(e0.elapsed_time(e1))
+                h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+    e2e_ms = sum(e2e_times) / len(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t[0])
+    e2e = pats_job / (e2e_ms / 1000.0)
+
+    if RANK != 0:
+        dist.destroy_process_group() if dist else None
+        return
+
+    cpu = None
+    if not a.no_cpu_baseline and WORLD == 1:
+        with tempfile.TemporaryDirectory() as td:
+            p = os.path.join(td, "db.txt")
+            db.write(p, "txt")
+            pats, el, stopped, _ = cpu_oracle(p, minsup, a.cpu_seconds, 1)
+        cpu = {"value": pats / el if el > 0 else None, "unit": unit, "cores": 1, "kind": "port",
+               "sample": "oracle (C restatement of src/gspan, pinned to the reference) on the full database at "
+                         "minsup %d, %s after %.1f s: %d patterns" % (minsup, "stopped" if stopped else "finished",
+                                                                      el, pats)}
+
+    line = {
+        "metric": metric, "value": value, "unit": unit, "n_gpus": WORLD, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_job, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic", "config": config,
+        "patterns_per_step": pats_job,
+        "e2e": {"value": e2e, "unit": unit, "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "k_wave_count", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_step": cb, "kernel_ms_per_step": cms, "launches_per_step":
+                     waves, "materialize_GBps": (mb / (mms / 1000.0)) / 1e9 if mms > 0 else None},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": int(launches_per_step * a.steps),
+        "stats_last_step": stats_all[-1],
+    }
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

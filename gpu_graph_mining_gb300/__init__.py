@@ -1,0 +1,347 @@
+"""GB300 gSpan frequent-subgraph miner: Python bindings over the C ABI.
+
+The native library (``_lib/libgspan_gb300.so``, built by ``build.py``) does
+all the work; this module only marshals arguments through ctypes.  There is
+no Python or CPU fallback: if the library is missing, every call raises.
+
+The classes mirror the reference's mining interface
+(``gspan_cuda::gspan_cuda`` in src/gspan_cuda/gspan_cuda.hpp:53,284-292):
+``GSpanMiner.set_database / set_min_support / set_graph_output / run``, with
+the output sink receiving ``(DFS code, support)`` once per frequent pattern
+like ``graph_output::output_graph`` (src/globals/graph_output.hpp:12).
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgspan_gb300.so")
+CLI_PATH = os.path.join(_HERE, "_lib", "gspan_gb300")
+
+TXT, BIN, FSG, CUDABIN = 0, 1, 2, 3
+LABELS_FULL, LABELS_SEQ = 0, 1
+
+STATUS_NAMES = {
+    0: "GS_OK", 1: "GS_ERR_USAGE", 2: "GS_ERR_IO", 3: "GS_ERR_FORMAT", 4: "GS_ERR_CUDA",
+    5: "GS_ERR_NOMEM", 6: "GS_ERR_MINSUP_TOO_LARGE", 7: "GS_ERR_MINSUP_TOO_SMALL", 8: "GS_ERR_LIMIT",
+    9: "GS_ERR_TIMEOUT", 10: "GS_ERR_CANCELLED", 11: "GS_ERR_BUDGET", 12: "GS_ERR_STATE",
+}
+
+# every symbol include/gspan_gb300.h declares
+EXPORTS = [
+    "gs_last_error", "gs_filetype_from_name", "gs_db_load", "gs_db_from_arrays", "gs_db_generate",
+    "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
+    "gs_mine", "gs_mine_ex", "gs_mine_batch", "gs_support_count", "gs_dfs_code_is_min", "gs_engine_reset",
+    "gs_engine_set_pool_bytes",
+]
+
+
+class GSpanError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
+        self.status = status
+
+
+class MineOpts(ctypes.Structure):
+    _fields_ = [("max_edges", ctypes.c_int32), ("label_style", ctypes.c_int32),
+                ("wave_nodes", ctypes.c_int32), ("threads", ctypes.c_int32),
+                ("wave_rows", ctypes.c_int64), ("wave_words", ctypes.c_int64),
+                ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32)]
+
+
+class MineStats(ctypes.Structure):
+    _fields_ = [("patterns", ctypes.c_int64), ("waves", ctypes.c_int64), ("launches", ctypes.c_int64),
+                ("nodes", ctypes.c_int64), ("rows", ctypes.c_int64), ("extensions", ctypes.c_int64),
+                ("candidates", ctypes.c_int64), ("count_bytes", ctypes.c_int64), ("mat_bytes", ctypes.c_int64),
+                ("count_ms", ctypes.c_double), ("mat_ms", ctypes.c_double), ("support_ms", ctypes.c_double),
+                ("root_ms", ctypes.c_double), ("host_min_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
+                ("peak_pool_bytes", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class DbInfo(ctypes.Structure):
+    _fields_ = [("graphs", ctypes.c_int64), ("vertices", ctypes.c_int64),
+                ("adjacency_entries", ctypes.c_int64), ("vertex_labels", ctypes.c_int32),
+                ("edge_labels", ctypes.c_int32), ("device_bytes", ctypes.c_int64)]
+
+
+EMIT_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p)
+BATCH_EMIT_FN = ctypes.CFUNCTYPE(None, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                 ctypes.c_int64, ctypes.c_void_p)
+
+_lib = None
+
+
+def lib():
+    """Loads the native library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("native library missing: %s (run gpu_graph_mining_gb300/build.py)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    i32, i64, vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p
+    pi32 = ctypes.POINTER(ctypes.c_int32)
+    L.gs_last_error.restype = ctypes.c_char_p
+    L.gs_filetype_from_name.argtypes = [ctypes.c_char_p]
+    L.gs_filetype_from_name.restype = i32
+    L.gs_db_load.argtypes = [ctypes.c_char_p, i32, pi32]
+    L.gs_db_load.restype = vp
+    L.gs_db_from_arrays.argtypes = [i32, i32, i32, i32, pi32, pi32, pi32, pi32, pi32]
+    L.gs_db_from_arrays.restype = vp
+    L.gs_db_generate.argtypes = [i32, ctypes.c_uint64, ctypes.c_double, pi32]
+    L.gs_db_generate.restype = vp
+    L.gs_db_write.argtypes = [vp, ctypes.c_char_p, i32]
+    L.gs_db_write.restype = i32
+    L.gs_db_size.argtypes = [vp]
+    L.gs_db_size.restype = i32
+    L.gs_db_get_info.argtypes = [vp, ctypes.POINTER(DbInfo)]
+    L.gs_db_get_info.restype = i32
+    L.gs_db_upload.argtypes = [vp]
+    L.gs_db_upload.restype = i32
+    L.gs_db_free.argtypes = [vp]
+    L.gs_db_free.restype = None
+    L.gs_mine_opts_default.argtypes = [ctypes.POINTER(MineOpts)]
+    L.gs_mine_opts_default.restype = None
+    L.gs_mine.argtypes = [vp, i32, i32, EMIT_FN, vp]
+    L.gs_mine.restype = i32
+    L.gs_mine_ex.argtypes = [vp, i32, ctypes.POINTER(MineOpts), EMIT_FN, vp, ctypes.POINTER(MineStats)]
+    L.gs_mine_ex.restype = i32
+    L.gs_mine_batch.argtypes = [ctypes.POINTER(vp), i32, pi32, ctypes.POINTER(MineOpts), BATCH_EMIT_FN, vp,
+                                ctypes.POINTER(MineStats)]
+    L.gs_mine_batch.restype = i32
+    L.gs_support_count.argtypes = [pi32, pi32, i64, i32, i32, pi32]
+    L.gs_support_count.restype = i32
+    L.gs_dfs_code_is_min.argtypes = [pi32, i32]
+    L.gs_dfs_code_is_min.restype = i32
+    L.gs_engine_reset.argtypes = []
+    L.gs_engine_reset.restype = None
+    L.gs_engine_set_pool_bytes.argtypes = [i64]
+    L.gs_engine_set_pool_bytes.restype = None
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != 0:
+        raise GSpanError(status, lib().gs_last_error().decode(errors="replace"))
+
+
+def filetype(name):
+    if isinstance(name, int):
+        return name
+    ft = lib().gs_filetype_from_name(name.encode())
+    if ft < 0:
+        raise ValueError("unknown filetype %r" % name)
+    return ft
+
+
+class Database:
+    """A graph database (host copy plus, once mined or uploaded, its HBM copy)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def load(cls, path, ftype="txt"):
+        st = ctypes.c_int32(0)
+        h = lib().gs_db_load(os.fsencode(path), filetype(ftype), ctypes.byref(st))
+        if not h:
+            _check(st.value or 2)
+        return cls(h)
+
+    @classmethod
+    def generate(cls, config, seed=0, scale=1.0):
+        st = ctypes.c_int32(0)
+        h = lib().gs_db_generate(int(config), int(seed), float(scale), ctypes.byref(st))
+        if not h:
+            _check(st.value or 1)
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, db_size, max_graph_vertex_count, edges, edges_labels, vertex_labels, vertex_offsets,
+                    vertex_count=-1):
+        """The reference's cudabin arrays (graph_database_cuda); sequences of int32."""
+        def arr(x):
+            x = list(x)
+            return (ctypes.c_int32 * max(1, len(x)))(*x), len(x)
+        e, ne = arr(edges)
+        el, _ = arr(edges_labels)
+        vl, _ = arr(vertex_labels)
+        vo, _ = arr(vertex_offsets)
+        st = ctypes.c_int32(0)
+        P = ctypes.POINTER(ctypes.c_int32)
+        h = lib().gs_db_from_arrays(int(db_size), ne, int(max_graph_vertex_count), int(vertex_count),
+                                    ctypes.cast(e, P), ctypes.cast(el, P), ctypes.cast(vl, P), ctypes.cast(vo, P),
+                                    ctypes.byref(st))
+        if not h:
+            _check(st.value or 3)
+        return cls(h)
+
+    def write(self, path, ftype="txt"):
+        _check(lib().gs_db_write(self._h, os.fsencode(path), filetype(ftype)))
+
+    def __len__(self):
+        return lib().gs_db_size(self._h)
+
+    def info(self):
+        i = DbInfo()
+        _check(lib().gs_db_get_info(self._h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in DbInfo._fields_}
+
+    def upload(self):
+        _check(lib().gs_db_upload(self._h))
+
+    def free(self):
+        if self._h:
+            lib().gs_db_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise ValueError("database freed")
+        return self._h
+
+
+def code_to_string(code):
+    """'(f t fl el tl);...' as DFSCode::to_string(false) (src/globals/dfs_code.cpp:199-216)."""
+    return ";".join("(%d %d %d %d %d)" % tuple(d) for d in code)
+
+
+def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
+          root_part=0, root_parts=1):
+    o = MineOpts()
+    lib().gs_mine_opts_default(ctypes.byref(o))
+    o.max_edges = int(max_edges)
+    o.label_style = int(label_style)
+    if wave_nodes is not None:
+        o.wave_nodes = int(wave_nodes)
+    if threads:
+        o.threads = int(threads)
+    if wave_rows:
+        o.wave_rows = int(wave_rows)
+    if wave_words:
+        o.wave_words = int(wave_words)
+    o.root_part = int(root_part)
+    o.root_parts = int(root_parts)
+    return o
+
+
+def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
+         wave_rows=0, wave_words=0, root_part=0, root_parts=1):
+    """Mines db at absolute support minsup.
+
+    Returns (patterns, stats): patterns is a list of (code, support) with code a
+    tuple of 5-tuples, in the reference's traversal order (empty when
+    collect=False); sink(code, support) is called per pattern if given.
+    """
+    out = []
+
+    def cb(ptr, n, support, user):
+        code = tuple(tuple(ptr[5 * i + j] for j in range(5)) for i in range(n))
+        if collect:
+            out.append((code, support))
+        if sink is not None:
+            sink(code, support)
+
+    fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
+    o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts)
+    st = MineStats()
+    _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
+    return out, st.as_dict()
+
+
+def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True):
+    """Mines several databases in shared launches; returns ([patterns per db], stats)."""
+    out = [[] for _ in dbs]
+
+    def cb(idx, ptr, n, support, user):
+        code = tuple(tuple(ptr[5 * i + j] for j in range(5)) for i in range(n))
+        out[idx].append((code, support))
+
+    fn = BATCH_EMIT_FN(cb) if collect else ctypes.cast(None, BATCH_EMIT_FN)
+    hs = (ctypes.c_void_p * len(dbs))(*[d.handle for d in dbs])
+    ms = (ctypes.c_int32 * len(dbs))(*[int(m) for m in minsups])
+    o = _opts(max_edges, label_style, wave_nodes, threads)
+    st = MineStats()
+    _check(lib().gs_mine_batch(hs, len(dbs), ms, ctypes.byref(o), fn, None, ctypes.byref(st)))
+    return out, st.as_dict()
+
+
+def support_count(keys, graph_ids, n_keys, n_graphs):
+    """support[k] = distinct graph ids among records with key k (GPU)."""
+    n = len(keys)
+    k = (ctypes.c_int32 * max(1, n))(*[int(x) for x in keys])
+    g = (ctypes.c_int32 * max(1, n))(*[int(x) for x in graph_ids])
+    out = (ctypes.c_int32 * max(1, n_keys))()
+    _check(lib().gs_support_count(k, g, n, int(n_keys), int(n_graphs), out))
+    return list(out)[:n_keys]
+
+
+def dfs_code_is_min(code):
+    """Canonicality of a DFS code given as a sequence of 5-tuples (host only)."""
+    flat = [int(x) for d in code for x in d]
+    arr = (ctypes.c_int32 * max(1, len(flat)))(*flat)
+    r = lib().gs_dfs_code_is_min(arr, len(code))
+    if r < 0:
+        raise ValueError("invalid DFS code")
+    return bool(r)
+
+
+def parse_code(s):
+    """'(0 1 2 0 3);(1 2 -1 0 4)' -> tuple of 5-tuples (DFSCode::read_from_str)."""
+    out = []
+    for part in s.strip().split(";"):
+        part = part.strip()
+        if not part:
+            continue
+        out.append(tuple(int(x) for x in part.strip("()").split()))
+    return tuple(out)
+
+
+class GSpanMiner:
+    """The reference's miner interface (gspan_cuda::gspan_cuda) over the GB300 engine."""
+
+    def __init__(self, wave_nodes=None, label_style=LABELS_FULL, max_edges=0):
+        self._db = None
+        self._minsup = -1
+        self._out = None
+        self.wave_nodes = wave_nodes
+        self.label_style = label_style
+        self.max_edges = max_edges
+        self.stats = None
+
+    def set_database(self, db):
+        self._db = db
+
+    def set_min_support(self, minsup):
+        self._minsup = int(minsup)
+
+    def set_graph_output(self, sink):
+        """sink(code, support), called once per frequent pattern."""
+        self._out = sink
+
+    def run(self):
+        if self._db is None:
+            raise GSpanError(1, "no database set")
+        _, self.stats = mine(self._db, self._minsup, self.max_edges, self.label_style, self.wave_nodes,
+                             collect=False, sink=self._out)
+
+    def delete_database_from_device(self):
+        lib().gs_engine_reset()
+
+
+def engine_reset():
+    lib().gs_engine_reset()
+
+
+def set_pool_bytes(n):
+    lib().gs_engine_set_pool_bytes(int(n))

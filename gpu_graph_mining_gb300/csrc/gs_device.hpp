@@ -1,0 +1,77 @@
+// Device-side layouts shared by the kernels (gs_kernels.cu) and the host
+// engine that fills them (gs_engine.cpp).
+//
+// Graph database in HBM (one per resident database):
+//   adj[E2]      uint64: low 32 bits = neighbour (global vertex id),
+//                high 32 bits = (edge label << 16) | neighbour vertex label
+//   adj_off[V+1] int32 CSR offsets, vlabel[V] dense vertex labels,
+//   vgraph[V]    graph id of each vertex,
+//   pair_idx[VL*EL*VL]  dense index of (elabel, tolabel) among the pairs that
+//                occur next to a vertex of label fl, or -1.
+// Labels are compacted order-preservingly to 0..VL-1 / 0..EL-1 (< 2^16).
+//
+// Embedding store: one column per pattern vertex, element = int2
+// {graph vertex, row in the previous column}; an embedding is the chain
+// from a row of the last column back to column 0 (the reference's
+// embedding_list_columns, src/globals/embedding_lists.hpp:12-60).  A forward
+// child appends a column; a backward child replaces the last column with a
+// filtered copy.  Each DFS-tree node also carries gord[row]: the dense rank
+// of the row's graph among the graphs that contain the node's pattern
+// (0..support-1), the index into the node's support bitmaps.
+#pragma once
+#include <cstdint>
+
+namespace gsgb {
+
+struct DevDB {
+  const unsigned long long *adj;
+  const int32_t *adj_off;
+  const int32_t *vlabel;
+  const int32_t *vgraph;
+  const int32_t *pair_idx;
+  int32_t VL, EL;
+  int32_t n_graphs;
+  int32_t n_vertices;
+};
+
+// Per DFS-tree node of a wave (a batch of nodes extended together).
+struct NodeDesc {
+  long long row_begin;   // first row in the wave's concatenated row space
+  long long bm_base;     // first support-bitmap word of the node's key 0
+  const int32_t *gord;   // [nrows]
+  int32_t nrows;
+  int32_t k;             // columns = pattern vertices; the right-most vertex is k-1
+  int32_t col_off;       // first entry in the wave's column-pointer table
+  int32_t slot_off;      // first entry in the wave's slot table
+  int32_t vtab_off;      // first entry in the wave's vertex table (k entries)
+  int32_t nslot;         // right-most path vertices; slot nslot-1 is the right-most vertex
+  int32_t minlabel;      // label of pattern vertex 0: forward targets need label >= minlabel
+  int32_t words;         // bitmap words per key = ceil(support / 32)
+  int32_t key_base;      // first key of the node in the wave's key space
+  int32_t nkeys;
+  int32_t db;            // index into the resident-database table
+  int32_t pad;
+};
+
+// One right-most-path vertex of a node.
+struct SlotDesc {
+  int32_t vertex;    // pattern vertex id
+  int32_t vlab;      // its (dense) label
+  int32_t fkey_off;  // forward keys of this slot: fkey_off + pair_idx(vlab, el, tl)
+  int32_t fel, ftl;  // forward order rule from the right-most-path edge leaving this
+                     // vertex: allowed iff fel < el || (fel == el && ftl <= tl); fel = -1
+                     // for the right-most vertex (no rule)
+  int32_t bkey_off;  // backward keys to this vertex: bkey_off + el; -1 if not a target
+  int32_t bel, blab; // backward order rule: allowed iff bel < el || (bel == el && blab <= label(rightmost))
+};
+
+// Output slots of a child node selected for materialisation.
+struct ChildOut {
+  int2 *col;      // the child's new last column
+  int2 *col0;     // root children only: column 0
+  int32_t *gord;  // the child's graph ranks
+  int32_t kind;   // 0 forward, 1 backward, 2 root
+  int32_t pad;
+};
+
+}  // namespace gsgb

@@ -1,0 +1,1129 @@
+// Host side of the miner: resident databases, the device pool, and the wave
+// scheduler.
+//
+// The reference drives the DFS-code tree one node at a time from the host
+// (gspan_cuda_no_sort::mainloop, src/gspan_cuda/gspan_cuda_no_sort.cpp:
+// 275-489): every node costs ~15-30 kernel launches, each followed by a
+// device synchronise, plus per-node cudaMalloc/cudaFree.  Here a "wave" is a
+// batch of pending tree nodes (possibly of different mining jobs) extended
+// together: per wave there are three kernels (count, support, materialise),
+// one device->host copy of the candidate supports and one synchronise.  With
+// wave_nodes = 1 the same engine runs the plain one-pattern-at-a-time form.
+//
+// The pattern set, codes and supports follow the sequential miner
+// (src/gspan/gspan.cpp:172-351): roots (fl <= tl) in ascending label order,
+// candidates keyed like its Projected maps, canonicality by gSpan::is_min
+// (src/gspan/ismin.cpp), output in its pre-order traversal order.
+#include "gs_engine.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <thread>
+#include <unordered_map>
+
+#include "gs_kernels.hpp"
+
+namespace gsgb {
+
+void cuda_check(cudaError_t e, const char *what)
+{
+  if(e != cudaSuccess) throw Error(ST_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call) cuda_check((call), #call)
+
+// ------------------------------------------------------------------ database
+
+void Database::prepare()
+{
+  if(VL > 0 || host.n_graphs == 0) return;
+  compact_labels(host, vl_dense, el_dense, labels);
+  VL = (int32_t)labels.vlabel_of.size();
+  EL = (int32_t)labels.elabel_of.size();
+  if(VL == 0) VL = 1;
+  if(EL == 0) EL = 1;
+  if(VL > 65535 || EL > 65535) throw Error(ST_ERR_LIMIT, "more than 65535 distinct vertex or edge labels");
+  const int64_t tab = (int64_t)VL * EL * VL;
+  if(tab > (int64_t)1 << 28) throw Error(ST_ERR_LIMIT, "label alphabet too large for the dense pair table");
+  std::vector<uint8_t> seen((size_t)tab, 0);
+  for(int64_t v = 0; v < host.n_vertices(); v++) {
+    const int64_t a = vl_dense[v];
+    for(int64_t k = host.aoff[v]; k < host.aoff[v + 1]; k++)
+      seen[(size_t)((a * EL + el_dense[k]) * VL + vl_dense[host.adj_to[k]])] = 1;
+  }
+  pairs.assign(VL, {});
+  pair_cnt.assign(VL, 0);
+  root_off.assign(VL, 0);
+  int32_t acc = 0;
+  for(int32_t a = 0; a < VL; a++) {
+    for(int32_t e = 0; e < EL; e++)
+      for(int32_t t = 0; t < VL; t++)
+        if(seen[(size_t)(((int64_t)a * EL + e) * VL + t)]) pairs[a].push_back({ e, t });
+    pair_cnt[a] = (int32_t)pairs[a].size();
+    root_off[a] = acc;
+    acc += pair_cnt[a];
+  }
+  root_keys = acc;
+}
+
+void Database::upload()
+{
+  if(resident) return;
+  prepare();
+  const int64_t V = host.n_vertices(), E2 = host.n_adj();
+  const int64_t tab = (int64_t)VL * EL * VL;
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t o_adj = 0;
+  size_t o_off = o_adj + al(sizeof(unsigned long long) * (E2 + 1));
+  size_t o_vl = o_off + al(sizeof(int32_t) * (V + 1));
+  size_t o_vg = o_vl + al(sizeof(int32_t) * (V + 1));
+  size_t o_pi = o_vg + al(sizeof(int32_t) * (V + 1));
+  size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
+  size_t total = o_ro + al(sizeof(int32_t) * (VL + 1));
+  std::vector<unsigned long long> adj(E2 + 1, 0);
+  for(int64_t k = 0; k < E2; k++) {
+    const uint32_t w = (uint32_t)host.adj_to[k];
+    const uint32_t hi = ((uint32_t)el_dense[k] << 16) | (uint32_t)vl_dense[w];
+    adj[k] = ((unsigned long long)hi << 32) | w;
+  }
+  std::vector<int32_t> off(V + 1), vg(V + 1, 0), pidx(tab, -1);
+  for(int64_t v = 0; v <= V; v++) off[v] = (int32_t)host.aoff[v];
+  for(int32_t g = 0; g < host.n_graphs; g++)
+    for(int64_t v = host.vbase[g]; v < host.vbase[g + 1]; v++) vg[v] = g;
+  for(int32_t a = 0; a < VL; a++)
+    for(size_t i = 0; i < pairs[a].size(); i++)
+      pidx[((int64_t)a * EL + pairs[a][i].first) * VL + pairs[a][i].second] = (int32_t)i;
+  CK(cudaMalloc(&d_block, total));
+  d_bytes = total;
+  char *b = (char *)d_block;
+  CK(cudaMemcpy(b + o_adj, adj.data(), sizeof(unsigned long long) * (E2 + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_off, off.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
+  if(V) CK(cudaMemcpy(b + o_vl, vl_dense.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_vg, vg.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_pi, pidx.data(), sizeof(int32_t) * tab, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_ro, root_off.data(), sizeof(int32_t) * VL, cudaMemcpyHostToDevice));
+  dev.adj = (const unsigned long long *)(b + o_adj);
+  dev.adj_off = (const int32_t *)(b + o_off);
+  dev.vlabel = (const int32_t *)(b + o_vl);
+  dev.vgraph = (const int32_t *)(b + o_vg);
+  dev.pair_idx = (const int32_t *)(b + o_pi);
+  dev.VL = VL;
+  dev.EL = EL;
+  dev.n_graphs = host.n_graphs;
+  dev.n_vertices = (int32_t)V;
+  d_root_off = (int32_t *)(b + o_ro);
+  resident = true;
+}
+
+void Database::release()
+{
+  if(d_block) cudaFree(d_block);
+  d_block = nullptr;
+  resident = false;
+}
+
+Database::~Database() { release(); }
+
+namespace {
+
+// -------------------------------------------------------------- device pool
+
+// First-fit sub-allocator over a few large cudaMalloc chunks.  All work is
+// issued on one stream, so memory freed here may be handed out again
+// immediately: later kernels are ordered after the ones still reading it.
+class Pool {
+public:
+  void set_limit(int64_t b) { limit_ = b; }
+  void *alloc(size_t n)
+  {
+    n = (n + 255) & ~(size_t)255;
+    if(n == 0) n = 256;
+    for(size_t c = 0; c < chunks_.size(); c++) {
+      void *p = take(c, n);
+      if(p) return p;
+    }
+    grow(n);
+    void *p = take(chunks_.size() - 1, n);
+    if(!p) throw Error(ST_ERR_NOMEM, "device pool exhausted");
+    return p;
+  }
+  void release(void *p)
+  {
+    if(!p) return;
+    auto it = live_.find(p);
+    if(it == live_.end()) return;
+    int c = it->second.first;
+    size_t n = it->second.second;
+    live_.erase(it);
+    used_ -= n;
+    Chunk &ch = chunks_[c];
+    size_t off = (size_t)((char *)p - ch.base);
+    auto nx = ch.free.lower_bound(off);
+    if(nx != ch.free.end() && off + n == nx->first) { n += nx->second; nx = ch.free.erase(nx); }
+    if(nx != ch.free.begin()) {
+      auto pv = std::prev(nx);
+      if(pv->first + pv->second == off) { pv->second += n; return; }
+    }
+    ch.free.emplace(off, n);
+  }
+  size_t used() const { return used_; }
+  size_t peak() const { return peak_; }
+  void reset_peak() { peak_ = used_; }
+  void destroy()
+  {
+    for(auto &c : chunks_) cudaFree(c.base);
+    chunks_.clear();
+    live_.clear();
+    used_ = peak_ = total_ = 0;
+  }
+
+private:
+  struct Chunk {
+    char *base;
+    size_t size;
+    std::map<size_t, size_t> free;
+  };
+  void *take(size_t c, size_t n)
+  {
+    Chunk &ch = chunks_[c];
+    for(auto it = ch.free.begin(); it != ch.free.end(); ++it) {
+      if(it->second < n) continue;
+      size_t off = it->first, sz = it->second;
+      ch.free.erase(it);
+      if(sz > n) ch.free.emplace(off + n, sz - n);
+      void *p = ch.base + off;
+      live_[p] = { (int)c, n };
+      used_ += n;
+      peak_ = std::max(peak_, used_);
+      return p;
+    }
+    return nullptr;
+  }
+  void grow(size_t n)
+  {
+    size_t freeb = 0, totalb = 0;
+    CK(cudaMemGetInfo(&freeb, &totalb));
+    size_t lim = limit_ > 0 ? (size_t)limit_ : (size_t)(0.7 * (double)(freeb + total_));
+    size_t want = std::max(n, next_);
+    if(total_ + want > lim) want = std::max(n, lim > total_ ? lim - total_ : 0);
+    if(want < n || total_ + want > lim + n) throw Error(ST_ERR_NOMEM, "device pool limit reached");
+    char *p = nullptr;
+    if(cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(ST_ERR_NOMEM, "cudaMalloc for the device pool failed");
+    }
+    chunks_.push_back(Chunk{ p, want, {} });
+    chunks_.back().free.emplace(0, want);
+    total_ += want;
+    next_ = std::min<size_t>(next_ * 2, (size_t)16 << 30);
+  }
+  std::vector<Chunk> chunks_;
+  std::unordered_map<void *, std::pair<int, size_t>> live_;
+  size_t used_ = 0, peak_ = 0, total_ = 0;
+  size_t next_ = (size_t)1 << 30;
+  int64_t limit_ = 0;
+};
+
+// growable device / pinned buffers
+template <class T> struct DBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t n)
+  {
+    if(n <= cap) return;
+    if(p) cudaFree(p);
+    size_t c = std::max(n, cap * 2);
+    if(c < 64) c = 64;
+    p = nullptr;
+    CK(cudaMalloc(&p, c * sizeof(T)));
+    cap = c;
+  }
+  void free()
+  {
+    if(p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+template <class T> struct HBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t n)
+  {
+    if(n <= cap) return;
+    if(p) cudaFreeHost(p);
+    size_t c = std::max(n, cap * 2);
+    if(c < 64) c = 64;
+    p = nullptr;
+    CK(cudaHostAlloc(&p, c * sizeof(T), cudaHostAllocDefault));
+    cap = c;
+  }
+  void free()
+  {
+    if(p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// ------------------------------------------------------------- host workers
+
+class Workers {
+public:
+  explicit Workers(int n)
+  {
+    for(int i = 0; i < n; i++) th_.emplace_back([this, i] { loop(i + 1); });
+  }
+  ~Workers()
+  {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for(auto &t : th_) t.join();
+  }
+  int size() const { return (int)th_.size() + 1; }
+  // fn(index, worker_id); the caller is worker 0
+  void run(int64_t n, const std::function<void(int64_t, int)> &fn)
+  {
+    if(n <= 0) return;
+    if(th_.empty() || n < 8) {
+      for(int64_t i = 0; i < n; i++) fn(i, 0);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> g(m_);
+      fn_ = &fn;
+      n_ = n;
+      next_.store(0);
+      busy_ = (int)th_.size();
+      gen_++;
+    }
+    cv_.notify_all();
+    work(0);
+    std::unique_lock<std::mutex> l(m_);
+    done_.wait(l, [this] { return busy_ == 0; });
+    fn_ = nullptr;
+  }
+
+private:
+  void work(int id)
+  {
+    while(true) {
+      int64_t i = next_.fetch_add(1);
+      if(i >= n_) break;
+      (*fn_)(i, id);
+    }
+  }
+  void loop(int id)
+  {
+    uint64_t seen = 0;
+    while(true) {
+      {
+        std::unique_lock<std::mutex> l(m_);
+        cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+        if(stop_) return;
+        seen = gen_;
+      }
+      work(id);
+      {
+        std::lock_guard<std::mutex> g(m_);
+        if(--busy_ == 0) done_.notify_all();
+      }
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int64_t, int)> *fn_ = nullptr;
+  std::atomic<int64_t> next_{ 0 };
+  int64_t n_ = 0;
+  int busy_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// ------------------------------------------------------------------ engine
+
+struct Column {
+  int2 *ptr = nullptr;
+  int64_t n = 0;
+  int32_t refs = 0;
+};
+
+struct PatternRec {
+  int32_t parent;
+  DFS edge;
+  int64_t support;
+  std::vector<int32_t> children;
+};
+
+struct JobState {
+  MineJob *job;
+  int32_t db_slot;
+  std::vector<PatternRec> pats;
+  std::vector<int32_t> roots;
+};
+
+struct PNode {
+  int32_t job;
+  int32_t pattern;
+  Code code;
+  std::vector<int32_t> cols;
+  int32_t *gord;
+  int64_t nrows;
+  int64_t support;
+};
+
+struct Candidate {
+  int32_t node;
+  int32_t key;
+  DFS dfs;
+  int32_t support;
+  int32_t cnt;
+  bool ok;
+};
+
+struct NodeLayout {
+  int32_t nrm;
+  int32_t maxtoc;
+  int32_t nfwd;
+  std::vector<int32_t> vlab;   // per pattern vertex
+  std::vector<SlotDesc> slots;
+};
+
+struct Engine {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[8];
+  Pool pool;
+  std::unique_ptr<Workers> workers;
+  std::vector<MinChecker> checkers;
+  std::vector<Column> cols;
+  std::vector<int32_t> free_cols;
+  int64_t pool_limit = 0;
+  // device scratch
+  DBuf<char> d_desc;
+  DBuf<uint32_t> d_bm;
+  DBuf<int32_t> d_bmx, d_cnt, d_sup, d_childmap, d_cursor;
+  DBuf<ChildOut> d_outs;
+  DBuf<DevDB> d_dbs;
+  DBuf<unsigned long long> d_bytes;
+  // pinned host mirrors
+  HBuf<char> h_desc;
+  HBuf<int32_t> h_sup, h_cnt, h_childmap;
+  HBuf<ChildOut> h_outs;
+  bool ready = false;
+
+  void init(int threads)
+  {
+    if(!ready) {
+      CK(cudaSetDevice(0));
+      CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+      for(auto &e : ev) CK(cudaEventCreate(&e));
+      d_bytes.ensure(4);
+      ready = true;
+    }
+    pool.set_limit(pool_limit);
+    int want = threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    if(!workers || workers->size() != want) {
+      workers.reset(new Workers(want - 1));
+      checkers.assign(want, MinChecker());
+    }
+  }
+  void destroy()
+  {
+    if(!ready) return;
+    cudaStreamSynchronize(stream);
+    pool.destroy();
+    d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
+    d_outs.free(); d_dbs.free(); d_bytes.free();
+    h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free();
+    for(auto &e : ev) cudaEventDestroy(e);
+    cudaStreamDestroy(stream);
+    cols.clear();
+    free_cols.clear();
+    workers.reset();
+    ready = false;
+  }
+  int32_t new_col(int2 *p, int64_t n)
+  {
+    int32_t id;
+    if(!free_cols.empty()) { id = free_cols.back(); free_cols.pop_back(); }
+    else { id = (int32_t)cols.size(); cols.emplace_back(); }
+    cols[id].ptr = p;
+    cols[id].n = n;
+    cols[id].refs = 1;
+    return id;
+  }
+  void ref(int32_t id) { cols[id].refs++; }
+  void unref(int32_t id)
+  {
+    if(--cols[id].refs == 0) {
+      pool.release(cols[id].ptr);
+      cols[id].ptr = nullptr;
+      free_cols.push_back(id);
+    }
+  }
+};
+
+std::mutex g_mu;
+Engine g_engine;
+
+inline int32_t words_for(int64_t support) { return (int32_t)((support + 31) / 32); }
+
+// Right-most-path slots and key layout of one node (see NodeDesc/SlotDesc).
+void layout_node(const PNode &n, const Database &db, NodeLayout &L)
+{
+  const Code &c = n.code;
+  int rm[kMaxPatternEdges];
+  L.nrm = build_rmpath(c.data(), (int)c.size(), rm);
+  L.maxtoc = c[rm[0]].to;
+  const int k = L.maxtoc + 1;
+  L.vlab.assign(k, 0);
+  L.vlab[0] = c[0].fromlabel;
+  for(const DFS &d : c)
+    if(d.is_forward()) L.vlab[d.to] = d.tolabel;
+  L.slots.assign(L.nrm + 1, SlotDesc{});
+  int32_t fk = 0;
+  for(int s = 0; s <= L.nrm; s++) {
+    SlotDesc &sd = L.slots[s];
+    if(s < L.nrm) {
+      const DFS &e = c[rm[L.nrm - 1 - s]];
+      sd.vertex = e.from;
+      sd.fel = e.elabel;
+      sd.ftl = e.tolabel;
+    } else {
+      sd.vertex = L.maxtoc;
+      sd.fel = -1;
+      sd.ftl = 0;
+    }
+    sd.vlab = L.vlab[sd.vertex];
+    sd.fkey_off = fk;
+    fk += db.pair_cnt[sd.vlab];
+    sd.bkey_off = -1;
+    sd.bel = sd.blab = 0;
+  }
+  L.nfwd = fk;
+  // backward targets: from-vertices of rmpath edges other than the deepest
+  // (slots 0..nrm-2), unless the code already joins them to the right-most vertex
+  for(int s = 0; s + 1 < L.nrm; s++) {
+    SlotDesc &sd = L.slots[s];
+    const DFS &e = c[rm[L.nrm - 1 - s]];
+    bool joined = false;
+    for(const DFS &d : c)
+      if((d.from == L.maxtoc && d.to == sd.vertex) || (d.to == L.maxtoc && d.from == sd.vertex)) joined = true;
+    sd.bel = e.elabel;
+    sd.blab = e.tolabel;
+    sd.bkey_off = joined ? -1 : fk + s * db.EL;
+  }
+}
+
+int32_t layout_nkeys(const NodeLayout &L, const Database &db) { return L.nfwd + std::max(0, L.nrm - 1) * db.EL; }
+
+// key -> candidate DFS edge (full labels)
+bool decode_key(const NodeLayout &L, const Database &db, int32_t key, DFS &d)
+{
+  if(key < L.nfwd) {
+    for(int s = 0; s <= L.nrm; s++) {
+      const SlotDesc &sd = L.slots[s];
+      const int32_t cnt = db.pair_cnt[sd.vlab];
+      if(key >= sd.fkey_off && key < sd.fkey_off + cnt) {
+        const auto &p = db.pairs[sd.vlab][key - sd.fkey_off];
+        d = DFS{ sd.vertex, L.maxtoc + 1, sd.vlab, p.first, p.second };
+        return true;
+      }
+    }
+    return false;
+  }
+  const int32_t b = (key - L.nfwd) / db.EL, el = (key - L.nfwd) % db.EL;
+  if(b < 0 || b + 1 >= L.nrm) return false;
+  const SlotDesc &sd = L.slots[b];
+  if(sd.bkey_off < 0) return false;
+  d = DFS{ L.maxtoc, sd.vertex, L.vlab[L.maxtoc], el, sd.vlab };
+  return true;
+}
+
+// order of children in the sequential miner's traversal (gspan.cpp:250-271)
+bool seq_before(const DFS &a, const DFS &b)
+{
+  const bool fa = a.is_forward(), fb = b.is_forward();
+  if(fa != fb) return !fa;
+  if(!fa) {
+    if(a.to != b.to) return a.to < b.to;
+    return a.elabel < b.elabel;
+  }
+  if(a.from != b.from) return a.from > b.from;
+  if(a.elabel != b.elabel) return a.elabel < b.elabel;
+  return a.tolabel < b.tolabel;
+}
+
+template <class T> T *carve(char *base, size_t &off, size_t n)
+{
+  off = (off + 255) & ~(size_t)255;
+  T *p = (T *)(base + off);
+  off += sizeof(T) * n;
+  return p;
+}
+
+double ms_between(cudaEvent_t a, cudaEvent_t b)
+{
+  float ms = 0;
+  if(cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return ms;
+}
+
+class Runner {
+public:
+  Runner(Engine &e, std::vector<MineJob> &jobs, const MineOptions &wo, MineStats &st)
+      : E(e), jobs_(jobs), wo_(wo), st_(st) {}
+
+  void run()
+  {
+    auto t0 = std::chrono::steady_clock::now();
+    E.pool.reset_peak();
+    // resident databases
+    std::vector<Database *> dbs;
+    for(auto &j : jobs_) {
+      if(!j.db->resident) {
+        j.db->upload();
+        st_.h2d_bytes += (int64_t)j.db->d_bytes;
+      }
+      int32_t slot = -1;
+      for(size_t i = 0; i < dbs.size(); i++) if(dbs[i] == j.db) slot = (int32_t)i;
+      if(slot < 0) { slot = (int32_t)dbs.size(); dbs.push_back(j.db); }
+      js_.push_back(JobState{ &j, slot, {}, {} });
+    }
+    std::vector<DevDB> tab;
+    for(auto *d : dbs) tab.push_back(d->dev);
+    E.d_dbs.ensure(tab.size());
+    h2d(E.d_dbs.p, tab.data(), sizeof(DevDB) * tab.size());
+    CK(cudaMemsetAsync(E.d_bytes.p, 0, sizeof(unsigned long long) * 4, E.stream));
+    for(size_t j = 0; j < js_.size(); j++) root_phase((int32_t)j);
+    while(!stack_.empty()) wave();
+    flush_timing();
+    unsigned long long bytes[4] = { 0, 0, 0, 0 };
+    d2h(bytes, E.d_bytes.p, sizeof(bytes));
+    CK(cudaStreamSynchronize(E.stream));
+    st_.count_bytes += (int64_t)bytes[0];
+    st_.mat_bytes += (int64_t)bytes[1];
+    st_.peak_pool_bytes = std::max<int64_t>(st_.peak_pool_bytes, (int64_t)E.pool.peak());
+    for(auto &s : js_) emit(s);
+    st_.wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+private:
+  Engine &E;
+  std::vector<MineJob> &jobs_;
+  const MineOptions &wo_;
+  MineStats &st_;
+  std::vector<JobState> js_;
+  std::vector<PNode> stack_;
+  bool mat_pending_ = false;
+
+  void h2d(void *dst, const void *src, size_t n)
+  {
+    CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, E.stream));
+    st_.h2d_bytes += (int64_t)n;
+  }
+  void d2h(void *dst, const void *src, size_t n)
+  {
+    CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, E.stream));
+    st_.d2h_bytes += (int64_t)n;
+  }
+
+  void flush_timing()
+  {
+    if(mat_pending_) {
+      CK(cudaEventSynchronize(E.ev[5]));
+      st_.mat_ms += ms_between(E.ev[4], E.ev[5]);
+      mat_pending_ = false;
+    }
+  }
+
+  // ---- root level: all frequent 1-edge codes of one job
+  void root_phase(int32_t j)
+  {
+    JobState &S = js_[j];
+    Database &db = *S.job->db;
+    const int32_t words = words_for(db.host.n_graphs);
+    const int32_t R = db.root_keys;
+    if(R == 0) return;
+    const size_t nw = (size_t)R * words;
+    E.d_bm.ensure(nw);
+    E.d_bmx.ensure(nw);
+    E.d_cnt.ensure(R);
+    E.d_sup.ensure(R);
+    E.d_childmap.ensure(R);
+    // pseudo node spanning the root keys, for the support kernel
+    NodeDesc nd{};
+    nd.words = words;
+    nd.nkeys = R;
+    E.d_desc.ensure(sizeof(NodeDesc));
+    E.h_desc.ensure(sizeof(NodeDesc));
+    std::memcpy(E.h_desc.p, &nd, sizeof(nd));
+    h2d(E.d_desc.p, E.h_desc.p, sizeof(nd));
+    CK(cudaMemsetAsync(E.d_bm.p, 0, nw * 4, E.stream));
+    CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)R * 4, E.stream));
+    CK(cudaEventRecord(E.ev[0], E.stream));
+    launch_root_count(db.dev, db.d_root_off, E.d_bm.p, E.d_cnt.p, words, E.d_bytes.p + 2, E.stream);
+    launch_support((const NodeDesc *)E.d_desc.p, 1, R, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
+    CK(cudaEventRecord(E.ev[1], E.stream));
+    st_.launches += 2;
+    E.h_sup.ensure(R);
+    E.h_cnt.ensure(R);
+    d2h(E.h_sup.p, E.d_sup.p, (size_t)R * 4);
+    d2h(E.h_cnt.p, E.d_cnt.p, (size_t)R * 4);
+    CK(cudaStreamSynchronize(E.stream));
+    CK(cudaGetLastError());
+    st_.root_ms += ms_between(E.ev[0], E.ev[1]);
+
+    const bool extend = S.job->opt.max_edges != 1;
+    std::vector<ChildOut> outs;
+    std::vector<PNode> made;
+    E.h_childmap.ensure(R);
+    for(int32_t i = 0; i < R; i++) E.h_childmap.p[i] = -1;
+    int32_t root_index = 0;
+    for(int32_t fl = 0; fl < db.VL; fl++) {
+      for(size_t p = 0; p < db.pairs[fl].size(); p++) {
+        const int32_t el = db.pairs[fl][p].first, tl = db.pairs[fl][p].second;
+        if(tl < fl) continue;
+        const int32_t key = db.root_off[fl] + (int32_t)p;
+        const int32_t sup = E.h_sup.p[key];
+        if(sup < S.job->minsup) continue;
+        // root-subtree partition: independent subtrees, no exchange between parts
+        const int32_t ri = root_index++;
+        if(S.job->opt.root_parts > 1 && ri % S.job->opt.root_parts != S.job->opt.root_part) continue;
+        PatternRec pr{ -1, DFS{ 0, 1, fl, el, tl }, sup, {} };
+        S.pats.push_back(pr);
+        const int32_t pid = (int32_t)S.pats.size() - 1;
+        S.roots.push_back(pid);
+        if(!extend) continue;
+        const int64_t n = E.h_cnt.p[key];
+        char *blk = (char *)E.pool.alloc((size_t)n * 8);
+        char *blk0 = (char *)E.pool.alloc((size_t)n * 8);
+        int32_t *gord = (int32_t *)E.pool.alloc((size_t)n * 4);
+        ChildOut o{ (int2 *)blk, (int2 *)blk0, gord, 2, 0 };
+        E.h_childmap.p[key] = (int32_t)outs.size();
+        outs.push_back(o);
+        PNode nn;
+        nn.job = j;
+        nn.pattern = pid;
+        nn.code = { pr.edge };
+        nn.cols = { E.new_col((int2 *)blk0, n), E.new_col((int2 *)blk, n) };
+        nn.gord = gord;
+        nn.nrows = n;
+        nn.support = sup;
+        made.push_back(std::move(nn));
+      }
+    }
+    if(!outs.empty()) {
+      E.d_outs.ensure(outs.size());
+      E.d_cursor.ensure(outs.size());
+      E.h_outs.ensure(outs.size());
+      std::memcpy(E.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
+      h2d(E.d_outs.p, E.h_outs.p, sizeof(ChildOut) * outs.size());
+      h2d(E.d_childmap.p, E.h_childmap.p, (size_t)R * 4);
+      CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
+      launch_root_materialize(db.dev, db.d_root_off, E.d_bm.p, E.d_bmx.p, words, E.d_childmap.p, E.d_cursor.p,
+                              E.d_outs.p, E.stream);
+      st_.launches++;
+      // the pinned childmap/outs mirrors are rewritten by the next phase:
+      // wait for the copies (and the kernel) before reusing them
+      CK(cudaStreamSynchronize(E.stream));
+      CK(cudaGetLastError());
+    }
+    for(auto it = made.rbegin(); it != made.rend(); ++it) stack_.push_back(std::move(*it));
+  }
+
+  // ---- one wave of DFS-tree nodes
+  void wave()
+  {
+    std::vector<PNode> nodes;
+    std::vector<NodeLayout> lays;
+    int64_t rows = 0, words = 0;
+    int32_t keys = 0;
+    while(!stack_.empty() && (int32_t)nodes.size() < std::max(1, wo_.wave_nodes)) {
+      PNode &top = stack_.back();
+      NodeLayout L;
+      layout_node(top, *js_[top.job].job->db, L);
+      const int32_t nk = layout_nkeys(L, *js_[top.job].job->db);
+      const int64_t w = (int64_t)nk * words_for(top.support);
+      if(!nodes.empty() && (rows + top.nrows > wo_.wave_rows || words + w > wo_.wave_words)) break;
+      rows += top.nrows;
+      words += w;
+      keys += nk;
+      lays.push_back(std::move(L));
+      nodes.push_back(std::move(top));
+      stack_.pop_back();
+    }
+    const int32_t W = (int32_t)nodes.size();
+    st_.waves++;
+    st_.nodes += W;
+    st_.rows += rows;
+
+    // descriptors
+    int32_t tot_cols = 0, tot_slots = 0;
+    for(int32_t n = 0; n < W; n++) {
+      tot_cols += (int32_t)nodes[n].cols.size();
+      tot_slots += (int32_t)lays[n].slots.size();
+    }
+    size_t off = 0;
+    char *hb = nullptr;
+    size_t need = 256 * 5 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
+                  sizeof(int32_t) * tot_cols;
+    E.h_desc.ensure(need);
+    E.d_desc.ensure(need);
+    hb = E.h_desc.p;
+    NodeDesc *hn = carve<NodeDesc>(hb, off, W);
+    const int2 **hc = carve<const int2 *>(hb, off, tot_cols);
+    SlotDesc *hs = carve<SlotDesc>(hb, off, tot_slots);
+    int32_t *hv = carve<int32_t>(hb, off, tot_cols);
+    const size_t desc_bytes = off;
+    int32_t co = 0, so = 0;
+    int64_t rb = 0, bb = 0;
+    int32_t kb = 0;
+    for(int32_t n = 0; n < W; n++) {
+      const PNode &p = nodes[n];
+      const NodeLayout &L = lays[n];
+      const Database &db = *js_[p.job].job->db;
+      NodeDesc &d = hn[n];
+      d = NodeDesc{};
+      d.row_begin = rb;
+      d.bm_base = bb;
+      d.gord = p.gord;
+      d.nrows = (int32_t)p.nrows;
+      d.k = (int32_t)p.cols.size();
+      d.col_off = co;
+      d.slot_off = so;
+      d.vtab_off = co;
+      d.nslot = (int32_t)L.slots.size();
+      d.minlabel = p.code[0].fromlabel;
+      d.words = words_for(p.support);
+      d.key_base = kb;
+      d.nkeys = layout_nkeys(L, db);
+      d.db = js_[p.job].db_slot;
+      for(size_t c = 0; c < p.cols.size(); c++) {
+        hc[co + c] = E.cols[p.cols[c]].ptr;
+        hv[co + c] = -1;
+      }
+      for(size_t s = 0; s < L.slots.size(); s++) {
+        hs[so + s] = L.slots[s];
+        if(L.slots[s].bkey_off >= 0) hv[co + L.slots[s].vertex] = (int32_t)s;
+      }
+      co += d.k;
+      so += d.nslot;
+      rb += p.nrows;
+      bb += (int64_t)d.nkeys * d.words;
+      kb += d.nkeys;
+    }
+    char *db_ = E.d_desc.p;
+    const NodeDesc *dn = (const NodeDesc *)(db_ + ((char *)hn - hb));
+    const int2 *const *dc = (const int2 *const *)(db_ + ((char *)hc - hb));
+    const SlotDesc *ds = (const SlotDesc *)(db_ + ((char *)hs - hb));
+    const int32_t *dv = (const int32_t *)(db_ + ((char *)hv - hb));
+    E.d_bm.ensure(std::max<int64_t>(bb, 1));
+    E.d_bmx.ensure(std::max<int64_t>(bb, 1));
+    E.d_cnt.ensure(std::max(kb, 1));
+    E.d_sup.ensure(std::max(kb, 1));
+    E.d_childmap.ensure(std::max(kb, 1));
+    h2d(E.d_desc.p, hb, desc_bytes);
+    CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
+    CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
+    CK(cudaEventRecord(E.ev[0], E.stream));
+    launch_wave_count(dn, W, rows, dc, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, E.stream);
+    CK(cudaEventRecord(E.ev[1], E.stream));
+    launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
+    CK(cudaEventRecord(E.ev[2], E.stream));
+    st_.launches += 2;
+    E.h_sup.ensure(std::max(kb, 1));
+    E.h_cnt.ensure(std::max(kb, 1));
+    d2h(E.h_sup.p, E.d_sup.p, (size_t)kb * 4);
+    d2h(E.h_cnt.p, E.d_cnt.p, (size_t)kb * 4);
+    CK(cudaStreamSynchronize(E.stream));
+    CK(cudaGetLastError());
+    flush_timing();
+    st_.count_ms += ms_between(E.ev[0], E.ev[1]);
+    st_.support_ms += ms_between(E.ev[1], E.ev[2]);
+
+    // frequent candidates
+    std::vector<Candidate> cands;
+    for(int32_t n = 0; n < W; n++) {
+      const PNode &p = nodes[n];
+      const Database &db = *js_[p.job].job->db;
+      const int32_t base = hn[n].key_base;
+      for(int32_t k = 0; k < hn[n].nkeys; k++) {
+        st_.extensions += E.h_cnt.p[base + k];
+        if(E.h_sup.p[base + k] < js_[p.job].job->minsup) continue;
+        Candidate c;
+        c.node = n;
+        c.key = k;
+        c.support = E.h_sup.p[base + k];
+        c.cnt = E.h_cnt.p[base + k];
+        c.ok = false;
+        if(!decode_key(lays[n], db, k, c.dfs)) continue;
+        cands.push_back(c);
+      }
+    }
+    st_.candidates += (int64_t)cands.size();
+    // canonicality on the host, in parallel
+    {
+      auto t0 = std::chrono::steady_clock::now();
+      std::vector<Code> dummy;
+      E.workers->run((int64_t)cands.size(), [&](int64_t i, int w) {
+        Candidate &c = cands[i];
+        const Code &code = nodes[c.node].code;
+        DFS buf[kMaxPatternEdges + 1];
+        const size_t n = code.size();
+        if(n + 1 > (size_t)kMaxPatternEdges) { c.ok = false; return; }
+        std::copy(code.begin(), code.end(), buf);
+        buf[n] = c.dfs;
+        c.ok = E.checkers[w].is_min(buf, (int)n + 1);
+      });
+      st_.host_min_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    // accepted children: output tree, materialisation slots
+    for(int32_t i = 0; i < kb; i++) E.h_childmap.p[i] = -1;
+    std::vector<ChildOut> outs;
+    std::vector<std::vector<PNode>> made(W);
+    {
+      std::vector<std::vector<int32_t>> per(W);
+      for(int32_t i = 0; i < (int32_t)cands.size(); i++)
+        if(cands[i].ok) per[cands[i].node].push_back(i);
+      for(int32_t n = 0; n < W; n++) {
+        auto &v = per[n];
+        std::sort(v.begin(), v.end(), [&](int32_t a, int32_t b) { return seq_before(cands[a].dfs, cands[b].dfs); });
+        PNode &p = nodes[n];
+        JobState &S = js_[p.job];
+        const int32_t max_edges = S.job->opt.max_edges;
+        for(int32_t ci : v) {
+          const Candidate &c = cands[ci];
+          PatternRec pr{ p.pattern, c.dfs, c.support, {} };
+          S.pats.push_back(pr);
+          const int32_t pid = (int32_t)S.pats.size() - 1;
+          S.pats[p.pattern].children.push_back(pid);
+          const int32_t child_edges = (int32_t)p.code.size() + 1;
+          if(max_edges > 0 && child_edges >= max_edges) continue;
+          if(child_edges >= kMaxPatternEdges || (c.dfs.is_forward() && c.dfs.to + 1 > 64))
+            throw Error(ST_ERR_LIMIT, "pattern exceeds 64 vertices or 127 edges");
+          const int64_t rowsn = c.cnt;
+          int2 *col = (int2 *)E.pool.alloc((size_t)rowsn * 8);
+          int32_t *gord = (int32_t *)E.pool.alloc((size_t)rowsn * 4);
+          ChildOut o{ col, nullptr, gord, c.dfs.is_forward() ? 0 : 1, 0 };
+          E.h_childmap.p[hn[n].key_base + c.key] = (int32_t)outs.size();
+          outs.push_back(o);
+          PNode nn;
+          nn.job = p.job;
+          nn.pattern = pid;
+          nn.code = p.code;
+          nn.code.push_back(c.dfs);
+          if(c.dfs.is_forward()) {
+            nn.cols = p.cols;
+            for(int32_t id : p.cols) E.ref(id);
+            nn.cols.push_back(E.new_col(col, rowsn));
+          } else {
+            nn.cols.assign(p.cols.begin(), p.cols.end() - 1);
+            for(int32_t id : nn.cols) E.ref(id);
+            nn.cols.push_back(E.new_col(col, rowsn));
+          }
+          nn.gord = gord;
+          nn.nrows = rowsn;
+          nn.support = c.support;
+          made[n].push_back(std::move(nn));
+        }
+      }
+    }
+    if(!outs.empty()) {
+      E.d_outs.ensure(outs.size());
+      E.d_cursor.ensure(outs.size());
+      E.h_outs.ensure(outs.size());
+      std::memcpy(E.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
+      h2d(E.d_outs.p, E.h_outs.p, sizeof(ChildOut) * outs.size());
+      h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
+      CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
+      CK(cudaEventRecord(E.ev[4], E.stream));
+      launch_wave_materialize(dn, W, rows, dc, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p, E.d_cursor.p,
+                              E.d_outs.p, E.d_bytes.p + 1, E.stream);
+      CK(cudaEventRecord(E.ev[5], E.stream));
+      st_.launches++;
+      mat_pending_ = true;
+    }
+    // the parents are done: drop their column references and graph ranks
+    // (stream order keeps the materialise kernel ahead of any reuse)
+    for(auto &p : nodes) {
+      for(int32_t id : p.cols) E.unref(id);
+      E.pool.release(p.gord);
+    }
+    for(int32_t n = W - 1; n >= 0; n--)
+      for(auto it = made[n].rbegin(); it != made[n].rend(); ++it) stack_.push_back(std::move(*it));
+  }
+
+  // pre-order traversal of a job's pattern tree, codes in the caller's labels
+  void emit(JobState &S)
+  {
+    const MineJob &j = *S.job;
+    st_.patterns += (int64_t)S.pats.size();
+    if(!j.emit) return;
+    const LabelMap &lm = j.db->labels;
+    std::vector<DFS> path, styled;
+    std::vector<int32_t> flat;
+    struct Frame { int32_t pat; size_t next; };
+    std::vector<Frame> st;
+    auto out = [&](int32_t pid) {
+      const size_t n = path.size();
+      styled.resize(n);
+      std::vector<DFS> orig(n);
+      for(size_t i = 0; i < n; i++) {
+        orig[i] = path[i];
+        orig[i].fromlabel = lm.vlabel_of[path[i].fromlabel];
+        orig[i].tolabel = lm.vlabel_of[path[i].tolabel];
+        orig[i].elabel = lm.elabel_of[path[i].elabel];
+      }
+      to_style(orig.data(), (int)n, (LabelStyle)j.opt.label_style, styled.data());
+      flat.resize(n * 5);
+      for(size_t i = 0; i < n; i++) {
+        flat[i * 5 + 0] = styled[i].from;
+        flat[i * 5 + 1] = styled[i].to;
+        flat[i * 5 + 2] = styled[i].fromlabel;
+        flat[i * 5 + 3] = styled[i].elabel;
+        flat[i * 5 + 4] = styled[i].tolabel;
+      }
+      j.emit(flat.data(), (int32_t)n, S.pats[pid].support, j.user);
+    };
+    for(int32_t r : S.roots) {
+      path.assign(1, S.pats[r].edge);
+      out(r);
+      st.assign(1, Frame{ r, 0 });
+      while(!st.empty()) {
+        Frame &f = st.back();
+        const auto &ch = S.pats[f.pat].children;
+        if(f.next < ch.size()) {
+          const int32_t c = ch[f.next++];
+          path.push_back(S.pats[c].edge);
+          out(c);
+          st.push_back(Frame{ c, 0 });
+        } else {
+          st.pop_back();
+          path.pop_back();
+        }
+      }
+    }
+  }
+};
+
+}  // namespace
+
+int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats *stats, std::string &err)
+{
+  std::lock_guard<std::mutex> g(g_mu);
+  MineStats local;
+  MineStats &st = stats ? *stats : local;
+  try {
+    for(auto &j : jobs) {
+      if(!j.db) throw Error(ST_ERR_USAGE, "null database");
+      if(j.minsup < 1) throw Error(ST_ERR_MINSUP_TOO_SMALL, "error: absolute_min_support < 1");
+      if(j.minsup >= j.db->host.n_graphs)
+        throw Error(ST_ERR_MINSUP_TOO_LARGE, "error: user specified support " + std::to_string(j.minsup) +
+                                                 " is greater then the database size " +
+                                                 std::to_string(j.db->host.n_graphs));
+    }
+    g_engine.init(wave_opt.threads);
+    Runner r(g_engine, jobs, wave_opt, st);
+    r.run();
+  } catch(const Error &e) {
+    err = e.what();
+    // leave the engine usable: finish queued work, drop pooled memory
+    if(g_engine.ready) {
+      cudaStreamSynchronize(g_engine.stream);
+      cudaGetLastError();
+      g_engine.destroy();
+    }
+    return e.code;
+  } catch(const std::exception &e) {
+    err = e.what();
+    if(g_engine.ready) {
+      cudaStreamSynchronize(g_engine.stream);
+      cudaGetLastError();
+      g_engine.destroy();
+    }
+    return ST_ERR_STATE;
+  }
+  return ST_OK;
+}
+
+int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,
+                       int32_t *support, std::string &err)
+{
+  if(n < 0 || n_keys < 0 || n_graphs < 0 || (n > 0 && (!keys || !gids)) || (n_keys > 0 && !support)) {
+    err = "invalid arguments";
+    return ST_ERR_USAGE;
+  }
+  for(int64_t i = 0; i < n; i++)
+    if(keys[i] < 0 || keys[i] >= n_keys || gids[i] < 0 || gids[i] >= n_graphs) {
+      err = "record " + std::to_string(i) + " has a key or graph id out of range";
+      return ST_ERR_USAGE;
+    }
+  if(n_keys == 0) return ST_OK;
+  const int32_t words = std::max(1, (n_graphs + 31) / 32);
+  const size_t nw = (size_t)n_keys * words;
+  std::lock_guard<std::mutex> g(g_mu);
+  char *blk = nullptr;
+  cudaStream_t s = nullptr;
+  int rc = ST_OK;
+  try {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_k = 0, o_g = o_k + al(4 * (size_t)std::max<int64_t>(n, 1));
+    const size_t o_bm = o_g + al(4 * (size_t)std::max<int64_t>(n, 1));
+    const size_t o_bmx = o_bm + al(4 * nw), o_sup = o_bmx + al(4 * nw);
+    const size_t o_nd = o_sup + al(4 * (size_t)n_keys), total = o_nd + al(sizeof(NodeDesc));
+    CK(cudaSetDevice(0));
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaMalloc(&blk, total));
+    NodeDesc nd{};
+    nd.words = words;
+    nd.nkeys = n_keys;
+    if(n > 0) {
+      CK(cudaMemcpyAsync(blk + o_k, keys, 4 * (size_t)n, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(blk + o_g, gids, 4 * (size_t)n, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(blk + o_nd, &nd, sizeof(nd), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(blk + o_bm, 0, 4 * nw, s));
+    launch_records_bitmap((const int32_t *)(blk + o_k), (const int32_t *)(blk + o_g), n, words,
+                          (uint32_t *)(blk + o_bm), s);
+    launch_support((const NodeDesc *)(blk + o_nd), 1, n_keys, (const uint32_t *)(blk + o_bm),
+                   (int32_t *)(blk + o_bmx), (int32_t *)(blk + o_sup), s);
+    CK(cudaMemcpyAsync(support, blk + o_sup, 4 * (size_t)n_keys, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+  } catch(const Error &e) {
+    err = e.what();
+    rc = e.code;
+  }
+  if(s) cudaStreamSynchronize(s);
+  if(blk) cudaFree(blk);
+  if(s) cudaStreamDestroy(s);
+  return rc;
+}
+
+void engine_reset()
+{
+  std::lock_guard<std::mutex> g(g_mu);
+  g_engine.destroy();
+}
+
+void engine_set_pool_bytes(int64_t bytes)
+{
+  std::lock_guard<std::mutex> g(g_mu);
+  g_engine.pool_limit = bytes;
+}
+
+}  // namespace gsgb

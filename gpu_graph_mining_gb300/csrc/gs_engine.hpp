@@ -1,0 +1,125 @@
+// The mining engine: resident databases, the device memory pool, and the
+// wave scheduler that extends many DFS-tree nodes per kernel launch.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gs_db.hpp"
+#include "gs_device.hpp"
+#include "gs_dfs.hpp"
+
+namespace gsgb {
+
+// Status codes shared with the C ABI (include/gspan_gb300.h).
+enum Status {
+  ST_OK = 0,
+  ST_ERR_USAGE = 1,
+  ST_ERR_IO = 2,
+  ST_ERR_FORMAT = 3,
+  ST_ERR_CUDA = 4,
+  ST_ERR_NOMEM = 5,
+  ST_ERR_MINSUP_TOO_LARGE = 6,
+  ST_ERR_MINSUP_TOO_SMALL = 7,
+  ST_ERR_LIMIT = 8,
+  ST_ERR_TIMEOUT = 9,
+  ST_ERR_CANCELLED = 10,
+  ST_ERR_BUDGET = 11,
+  ST_ERR_STATE = 12,
+};
+
+struct Error : public std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char *what);
+
+// Host database plus, once uploaded, its device copy.
+struct Database {
+  HostDB host;
+  LabelMap labels;
+  std::vector<int32_t> vl_dense, el_dense;
+  int32_t VL = 0, EL = 0;
+  // pairs[a] = sorted (elabel, tolabel) pairs occurring next to label-a vertices
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> pairs;
+  std::vector<int32_t> pair_cnt, root_off;
+  int32_t root_keys = 0;
+  // device copy
+  void *d_block = nullptr;
+  size_t d_bytes = 0;
+  DevDB dev{};
+  int32_t *d_root_off = nullptr;
+  bool resident = false;
+
+  void prepare();   // label compaction and pair tables (host only)
+  void upload();    // device copy (idempotent)
+  void release();   // frees the device copy
+  ~Database();
+};
+
+using EmitFn = void (*)(const int32_t *dfs5xN, int32_t n_edges, int64_t support, void *user);
+
+struct MineOptions {
+  int32_t max_edges = 0;      // 0 = no cap
+  int32_t label_style = 0;    // LABELS_FULL / LABELS_SEQ
+  int32_t wave_nodes = 4096;  // 1 = plain one-pattern-at-a-time
+  int64_t wave_rows = 1 << 24;
+  int64_t wave_words = 1 << 24;  // support-bitmap words per wave
+  int32_t threads = 0;        // host threads for the canonicality check (0 = hardware)
+  int32_t root_part = 0;      // mine only the root subtrees with index % root_parts == root_part
+  int32_t root_parts = 1;
+};
+
+struct MineStats {
+  int64_t patterns = 0;
+  int64_t waves = 0;
+  int64_t launches = 0;
+  int64_t nodes = 0;
+  int64_t rows = 0;          // embedding rows extended
+  int64_t extensions = 0;    // (row, extension) pairs enumerated by the count pass
+  int64_t candidates = 0;    // frequent candidates checked for canonicality
+  int64_t count_bytes = 0;   // algorithmic bytes of the count kernels
+  int64_t mat_bytes = 0;     // algorithmic bytes of the materialise kernels
+  double count_ms = 0;       // summed kernel time of the count kernels
+  double mat_ms = 0;         // summed kernel time of the materialise kernels
+  double support_ms = 0;
+  double root_ms = 0;
+  double host_min_ms = 0;    // canonicality checks on the host
+  double wall_ms = 0;
+  int64_t peak_pool_bytes = 0;
+  int64_t h2d_bytes = 0;     // host->device bytes copied (database upload and per-wave tables)
+  int64_t d2h_bytes = 0;     // device->host bytes copied (candidate supports and counts)
+};
+
+struct MineJob {
+  Database *db = nullptr;
+  int32_t minsup = 1;
+  MineOptions opt;
+  EmitFn emit = nullptr;
+  void *user = nullptr;
+  int32_t tag = 0;   // caller's index (batch position / request id)
+};
+
+// Runs a set of mining jobs to completion in shared waves and emits each
+// job's patterns (in the reference's traversal order) after it finishes.
+// Jobs with emit == nullptr still count their patterns in stats.
+int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats *stats, std::string &err);
+
+// support[k] = number of distinct graph ids among the records with key k
+// (host arrays; records must satisfy 0 <= key < n_keys, 0 <= graph < n_graphs).
+int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,
+                       int32_t *support, std::string &err);
+
+// Releases the engine's device pool and scratch (the next call re-creates them).
+void engine_reset();
+
+// Bytes the engine's pool may use (0 = 70% of free device memory at first use).
+void engine_set_pool_bytes(int64_t bytes);
+
+}  // namespace gsgb

@@ -1,0 +1,41 @@
+// Launchers for the mining kernels (gs_kernels.cu).  All launches go to the
+// given stream; none synchronises.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gs_device.hpp"
+
+namespace gsgb {
+
+// Root level: one thread per vertex walks its adjacency; every directed
+// entry (v -> w) with label(v) <= label(w) is a 1-edge embedding
+// (get_forward_root, src/globals/graph_types.cpp:365-375).
+// Sets support-bitmap bit [key][graph] and counts embeddings per key.
+void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
+                       unsigned long long *bytes, cudaStream_t s);
+// Writes the two columns and graph ranks of every selected root key.
+void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
+                             int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
+                             cudaStream_t s);
+
+// Wave level: one thread per embedding row of every node of the wave.
+void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
+                       const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
+                       unsigned long long *bytes, cudaStream_t s);
+void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
+                             const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs, const uint32_t *bm,
+                             const int32_t *bmx, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
+                             unsigned long long *bytes, cudaStream_t s);
+
+// Extension records given as (key, graph id) pairs: sets bit [key][graph].
+// Keys and graph ids must be in range (checked by the caller).
+void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n, int32_t words, uint32_t *bm,
+                           cudaStream_t s);
+
+// One warp per key: support = popcount of the key's bitmap words; bmx gets
+// the exclusive prefix popcount of each word (for graph-rank lookups).
+void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,
+                    int32_t *support, cudaStream_t s);
+
+}  // namespace gsgb

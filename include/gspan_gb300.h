@@ -1,0 +1,197 @@
+/*
+ * gspan_gb300.h -- C ABI of the GB300 gSpan frequent-subgraph miner.
+ *
+ * Plain C types only (pointers, sizes, int32/int64).  All entry points
+ * report errors through a gs_status value (never abort()); the text of the
+ * last error on the calling thread is available from gs_last_error().
+ *
+ * Drop-in correspondence with the reference (zakimjz/GPU_graph_mining):
+ * the miner class gspan_cuda::gspan_cuda (src/gspan_cuda/gspan_cuda.hpp:
+ * 53,284-292) with set_database / set_min_support / set_graph_output / run,
+ * the database readers of src/globals/dbio.hpp:9-37 and the output sink
+ * graph_output::output_graph(const DFSCode&, size_t support)
+ * (src/globals/graph_output.hpp:12).
+ */
+#ifndef GSPAN_GB300_H
+#define GSPAN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GS_API __attribute__((visibility("default")))
+#else
+#define GS_API
+#endif
+
+typedef int32_t gs_status;
+
+/* Status codes.  GS_ERR_MINSUP_TOO_LARGE / _TOO_SMALL correspond to the
+ * reference mains' exit codes 2 and 3 (src/gspan_cuda/common_main.cpp:56-70). */
+enum {
+  GS_OK = 0,
+  GS_ERR_USAGE = 1,
+  GS_ERR_IO = 2,
+  GS_ERR_FORMAT = 3,
+  GS_ERR_CUDA = 4,
+  GS_ERR_NOMEM = 5,
+  GS_ERR_MINSUP_TOO_LARGE = 6,
+  GS_ERR_MINSUP_TOO_SMALL = 7,
+  GS_ERR_LIMIT = 8,
+  GS_ERR_TIMEOUT = 9,
+  GS_ERR_CANCELLED = 10,
+  GS_ERR_BUDGET = 11,
+  GS_ERR_STATE = 12
+};
+
+/* File types, numbered as dbio::FILE_TYPE (src/globals/dbio.hpp:9). */
+enum { GS_TXT = 0, GS_BIN = 1, GS_FSG = 2, GS_CUDABIN = 3 };
+
+/* Label conventions of emitted DFS codes.  GS_LABELS_FULL carries every
+ * vertex label, as the GPU reference's codes do; GS_LABELS_SEQ writes -1 for
+ * fromlabel after the first edge and for the tolabel of backward edges, as
+ * the sequential reference (src/gspan/gspan.cpp:254,267) does. */
+enum { GS_LABELS_FULL = 0, GS_LABELS_SEQ = 1 };
+
+typedef struct gs_db gs_db;
+
+/* Thread-local text of the last error ("" if none). */
+GS_API const char *gs_last_error(void);
+
+/* Parses "txt"/"-txt"/"bin"/"fsg"/"cudabin" like dbio::ftype2str
+ * (src/globals/dbio.cpp:33-41); -1 if unknown. */
+GS_API int32_t gs_filetype_from_name(const char *name);
+
+/* Loads a database file: replaces dbio::read_database / read_database_cudabin
+ * (src/globals/dbio.cpp:44-60, 381-404).  Graphs must be simple (no self
+ * loops, no parallel edges).  Returns NULL on error. */
+GS_API gs_db *gs_db_load(const char *path, int32_t filetype, gs_status *status);
+
+/* Builds a database from the reference's flat cudabin arrays
+ * (types::graph_database_cuda, src/globals/cuda_graph_types.hpp:16-50; the
+ * layout written by dbio::write_database_cudabin, dbio.cpp:354-370):
+ * edges/edges_labels[edges_sizes], vertex_labels[db_size*max_graph_vertex_count],
+ * vertex_offsets[db_size*max_graph_vertex_count+1], -1 marking padding.
+ * Replaces gspan_cuda::set_database(graph_database_cuda&) (gspan_cuda.cpp:73-104).
+ * The arrays are copied. */
+GS_API gs_db *gs_db_from_arrays(int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
+                                int32_t vertex_count, const int32_t *edges, const int32_t *edges_labels,
+                                const int32_t *vertex_labels, const int32_t *vertex_offsets, gs_status *status);
+
+/* Seeded synthetic database of benchmark configuration 1..5 with `scale`
+ * times its graph count.  No counterpart in the reference: it stands in for
+ * the PAFI graph generator the reference's experiments used
+ * (testdata/fsg/gen_graphs.sh). */
+GS_API gs_db *gs_db_generate(int32_t config, uint64_t seed, double scale, gs_status *status);
+
+/* Writes a database as txt, bin or cudabin (dbio::write_database_bin /
+ * write_database_cudabin, src/globals/dbio.cpp:209-260, 354-370). */
+GS_API gs_status gs_db_write(const gs_db *db, const char *path, int32_t filetype);
+
+/* Number of graphs (graph_database_cuda::size, cuda_graph_types.hpp:67). */
+GS_API int32_t gs_db_size(const gs_db *db);
+
+/* Vertex / adjacency-entry / label counts of a database. */
+typedef struct gs_db_info {
+  int64_t graphs;
+  int64_t vertices;
+  int64_t adjacency_entries; /* both directions of every edge */
+  int32_t vertex_labels;
+  int32_t edge_labels;
+  int64_t device_bytes;      /* bytes of the device copy, 0 if not resident */
+} gs_db_info;
+GS_API gs_status gs_db_get_info(const gs_db *db, gs_db_info *info);
+
+/* Copies the database to the GPU now (otherwise the first mining call does). */
+GS_API gs_status gs_db_upload(gs_db *db);
+
+/* Frees the host and device copies. */
+GS_API void gs_db_free(gs_db *db);
+
+/* Output sink, the C form of graph_output::output_graph(const DFSCode&, size_t)
+ * (src/globals/graph_output.hpp:12): called on the calling thread once per
+ * frequent pattern, in the sequential reference's traversal order (the GPU
+ * reference, gspan_cuda_no_sort.cpp:107,416, emits the same set).  dfs5xN
+ * holds n_edges tuples {from, to, fromlabel, elabel, tolabel}
+ * (types::DFS, src/globals/dfs_code.hpp:17-23); it is valid during the call. */
+typedef void (*gs_emit_fn)(const int32_t *dfs5xN, int32_t n_edges, int64_t support, void *user);
+
+typedef struct gs_mine_opts {
+  int32_t max_edges;   /* 0 = no cap on pattern edges */
+  int32_t label_style; /* GS_LABELS_FULL or GS_LABELS_SEQ */
+  int32_t wave_nodes;  /* DFS-tree nodes extended per launch; 1 = one pattern at a time */
+  int32_t threads;     /* host threads for the canonicality check; 0 = all cores */
+  int64_t wave_rows;   /* embedding rows per launch (soft cap; 0 = default) */
+  int64_t wave_words;  /* support-bitmap words per launch (soft cap; 0 = default) */
+  int32_t root_part;   /* mine only the root subtrees whose index (in the reference's root */
+  int32_t root_parts;  /* order) is root_part modulo root_parts; root_parts <= 1 = all */
+} gs_mine_opts;
+
+typedef struct gs_mine_stats {
+  int64_t patterns;
+  int64_t waves;
+  int64_t launches;        /* kernels launched by the miner */
+  int64_t nodes;           /* DFS-tree nodes extended */
+  int64_t rows;            /* embedding rows extended */
+  int64_t extensions;      /* one-edge extensions enumerated */
+  int64_t candidates;      /* frequent candidates checked for canonicality */
+  int64_t count_bytes;     /* algorithmic bytes of the count kernels */
+  int64_t mat_bytes;       /* algorithmic bytes of the materialise kernels */
+  double count_ms;         /* summed device time of the count kernels */
+  double mat_ms;           /* summed device time of the materialise kernels */
+  double support_ms;
+  double root_ms;
+  double host_min_ms;
+  double wall_ms;
+  int64_t peak_pool_bytes;
+  int64_t h2d_bytes;       /* host->device bytes copied (database upload, per-wave tables) */
+  int64_t d2h_bytes;       /* device->host bytes copied (candidate supports and counts) */
+} gs_mine_stats;
+
+GS_API void gs_mine_opts_default(gs_mine_opts *opts);
+
+/* Mines all frequent connected subgraphs with support >= abs_minsup:
+ * replaces set_min_support + set_graph_output + run of gspan_cuda::gspan_cuda
+ * (src/gspan_cuda/gspan_cuda.hpp:284-292).  Returns GS_ERR_MINSUP_TOO_LARGE
+ * when abs_minsup >= number of graphs and GS_ERR_MINSUP_TOO_SMALL when < 1. */
+GS_API gs_status gs_mine(gs_db *db, int32_t abs_minsup, int32_t max_edges, gs_emit_fn emit, void *user);
+GS_API gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,
+                            gs_mine_stats *stats);
+
+/* Batched form: n databases mined together, their DFS-tree nodes sharing
+ * launches.  emit receives the database index first.  No counterpart in the
+ * reference (it mines one database per process). */
+typedef void (*gs_batch_emit_fn)(int32_t db_index, const int32_t *dfs5xN, int32_t n_edges, int64_t support,
+                                 void *user);
+GS_API gs_status gs_mine_batch(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, const gs_mine_opts *opts,
+                               gs_batch_emit_fn emit, void *user, gs_mine_stats *stats);
+
+/* Support of candidate DFS edges from extension records: support[k] = the
+ * number of distinct graph ids among the records whose key is k, computed on
+ * the GPU with one support bitmap per key.  The GPU form of
+ * compute_support_remapped_db_multiple_dfs (src/gspan_cuda/compute_support.cpp:
+ * 885-960), which counts records x candidates flags.  Host arrays; keys in
+ * [0, n_keys), graph ids in [0, n_graphs), else GS_ERR_USAGE. */
+GS_API gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids, int64_t n_records, int32_t n_keys,
+                                  int32_t n_graphs, int32_t *support);
+
+/* Canonicality of a DFS code (n_edges tuples {from, to, fromlabel, elabel,
+ * tolabel}, either label convention): 1 if minimal, 0 if not, -1 on bad
+ * input.  Same semantics as the sequential reference's gSpan::is_min
+ * (src/gspan/ismin.cpp:36-143), which DFSCode::dfs_code_is_min
+ * (src/globals/dfs_ismin.cpp:23-160) mirrors; host-only, no GPU needed. */
+GS_API int32_t gs_dfs_code_is_min(const int32_t *dfs5xN, int32_t n_edges);
+
+/* Frees the miner's device pool and scratch buffers. */
+GS_API void gs_engine_reset(void);
+/* Caps the device pool (bytes; 0 = 70% of free device memory). */
+GS_API void gs_engine_set_pool_bytes(int64_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSPAN_GB300_H */

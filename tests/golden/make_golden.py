@@ -1,0 +1,166 @@
+"""Regenerates the golden fixtures in tests/golden/ from the reference.
+
+Run in a container that holds the reference tree (default /root/reference,
+or REF=...).  It
+  * builds the reference's own sequential gSpan (src/gspan) from its sources
+    through oracle/Makefile (`make -C oracle ref` -> oracle/_ref/gspan_ref),
+  * reads the reference's test sources as text to recover their vectors:
+      - src/globals/tests/dfs_ismin_tests.cpp:48-61   canonicality KATs
+      - src/globals/test_support.cpp:10-158            three 18-graph fixture databases
+      - src/gspan_cuda/tests/compute_support_remapped_test.cpp:23-71  support KAT
+      - src/gspan_cuda/tests/extract_extensions_test.cpp:30-157       candidate/support KAT
+  * copies the reference's BIN fixture databases (testdata/labeled.bin,
+    testdata/unlabeled.bin),
+  * writes the synthetic configuration-1 database (seed 1) with this
+    package's generator, and
+  * runs the reference miner on every fixture database at several supports,
+    writing "<code>\\t<support>" lines in the reference's traversal order.
+
+Nothing at test time reads the reference; the tests use only these files.
+"""
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
+REF = os.environ.get("REF", "/root/reference")
+REF_BIN = os.path.join(REPO, "oracle", "_ref", "gspan_ref")
+
+
+def build_ref():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + REF])
+
+
+def read(path):
+    with open(os.path.join(REF, path)) as f:
+        return f.read()
+
+
+def ismin_kats():
+    src = read("src/globals/tests/dfs_ismin_tests.cpp")
+    body = src[src.index("TEST(dfs_ismin, basic_test)"):]
+    body = body[:body.index("/*")]
+    out = []
+    for line in body.splitlines():
+        if line.strip().startswith("//"):
+            continue  # commented-out expectations
+        m = re.search(r'EXPECT_(TRUE|FALSE)\(static_ismin\("([^"]*)"\)\)', line)
+        if m:
+            out.append("%s\t%s" % (1 if m.group(1) == "TRUE" else 0, m.group(2)))
+    return out
+
+
+def fixture_dbs():
+    src = read("src/globals/test_support.cpp")
+    dbs = {}
+    for name in ("get_test_database", "get_labeled_test_database", "get_labeled_test_database2"):
+        start = src.index("types::graph_database_t %s()" % name)
+        arr = src[start:src.index("};", start)]
+        codes = [s for s in re.findall(r'"([^"]*)"', arr) if s]
+        dbs[name] = codes
+    return dbs
+
+
+def code_to_txt_graph(code_str, gid):
+    """DFSCode::toGraph (src/globals/dfs_code.cpp:245-266) written as a txt graph."""
+    code = [tuple(int(x) for x in p.strip("()").split()) for p in code_str.split(";")]
+    nv = max(max(f, t) for f, t, _, _, _ in code) + 1
+    lab = [0] * nv
+    for f, t, fl, el, tl in code:
+        if fl != -1:
+            lab[f] = fl
+        if tl != -1:
+            lab[t] = tl
+    lines = ["t # %d" % gid] + ["v %d %d" % (v, lab[v]) for v in range(nv)]
+    lines += ["e %d %d %d" % (f, t, el) for f, t, _, el, _ in code]
+    return lines
+
+
+def support_kat():
+    src = read("src/gspan_cuda/tests/compute_support_remapped_test.cpp")
+    recs = re.findall(r"extension_element_t\(\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+)\)", src)
+    mvc = int(re.search(r"int max_graph_vertex_count = (\d+);", src).group(1))
+    dfs = re.findall(r"DFS\((\d+), (\d+), (\d+), (\d+), (\d+)\)", src[src.index("types::DFS dfs_array[]"):])
+    exp = re.search(r"int expected_supports \[\] = \{([^}]*)\}", src).group(1)
+    return recs, mvc, dfs, [int(x) for x in exp.split(",")]
+
+
+def extract_kat():
+    src = read("src/gspan_cuda/tests/extract_extensions_test.cpp")
+    recs = re.findall(r"extension_element_t\(\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+)\)", src)
+    mvc = int(re.search(r"int max_graph_vertex_count = (\d+);", src).group(1))
+    res = src[src.index("types::DFS dfs_res[]"):]
+    dfs = re.findall(r"DFS\((\d+), (\d+), (\d+), (\d+), (\d+)\)", res)
+    supp = re.search(r"int supp_res\[\] = \{([^}]*)\}", src).group(1)
+    return recs, mvc, dfs, [int(x) for x in supp.split(",")]
+
+
+def run_ref(ftype, db, minsup, out):
+    r = subprocess.run([REF_BIN, ftype, db, str(minsup), out], stderr=subprocess.PIPE, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    return r.stderr.strip()
+
+
+def main():
+    build_ref()
+    with open(os.path.join(HERE, "ismin_kats.tsv"), "w") as f:
+        f.write("# expected(1=min)\tcode   from src/globals/tests/dfs_ismin_tests.cpp:48-61\n")
+        f.write("\n".join(ismin_kats()) + "\n")
+
+    for name, codes in fixture_dbs().items():
+        lines = []
+        for i, c in enumerate(codes):
+            lines += code_to_txt_graph(c, i)
+        with open(os.path.join(HERE, "fixture_%s.txt" % name), "w") as f:
+            f.write("\n".join(lines) + "\n")
+
+    recs, mvc, dfs, exp = support_kat()
+    with open(os.path.join(HERE, "support_kat.tsv"), "w") as f:
+        f.write("# compute_support_remapped_test.cpp:23-71: records (from to fl el tl from_grph to_grph row), "
+                "max_graph_vertex_count=%d\n" % mvc)
+        for r in recs:
+            f.write("rec\t%s\n" % " ".join(r))
+        for d, e in zip(dfs, exp):
+            f.write("dfs\t%s\t%d\n" % (" ".join(d), e))
+    recs, mvc, dfs, exp = extract_kat()
+    with open(os.path.join(HERE, "extract_kat.tsv"), "w") as f:
+        f.write("# extract_extensions_test.cpp:30-157: records, then the distinct DFS edges with supports, "
+                "max_graph_vertex_count=%d\n" % mvc)
+        for r in recs:
+            f.write("rec\t%s\n" % " ".join(r))
+        for d, e in zip(dfs, exp):
+            f.write("dfs\t%s\t%d\n" % (" ".join(d), e))
+
+    for b in ("labeled.bin", "unlabeled.bin"):
+        shutil.copyfile(os.path.join(REF, "testdata", b), os.path.join(HERE, "fixture_" + b))
+
+    sys.path.insert(0, REPO)
+    import gpu_graph_mining_gb300 as g
+    from gpu_graph_mining_gb300 import build as gb
+    gb.build()
+    g.Database.generate(1, seed=1).write(os.path.join(HERE, "cfg1_seed1.txt"), "txt")
+
+    runs = []
+    for name in ("get_test_database", "get_labeled_test_database", "get_labeled_test_database2"):
+        for s in (2, 3, 5, 9):
+            runs.append(("txt", "fixture_%s.txt" % name, s))
+    for b in ("labeled.bin", "unlabeled.bin"):
+        for s in (2, 4, 9):
+            runs.append(("bin", "fixture_" + b, s))
+    for s in (68, 34, 17, 10, 5):
+        runs.append(("txt", "cfg1_seed1.txt", s))
+    with open(os.path.join(HERE, "golden_runs.tsv"), "w") as idx:
+        idx.write("# filetype\tdatabase\tminsup\toutput\treference stderr\n")
+        for ft, db, s in runs:
+            out = "out_%s_s%d.txt" % (os.path.splitext(db)[0], s)
+            log = run_ref(ft, os.path.join(HERE, db), s, os.path.join(HERE, out))
+            idx.write("%s\t%s\t%d\t%s\t%s\n" % (ft, db, s, out, log))
+            print(ft, db, s, log)
+
+
+if __name__ == "__main__":
+    main()

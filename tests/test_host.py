@@ -1,0 +1,189 @@
+"""CPU tests: the oracle against the reference's golden vectors, the C ABI's
+exports, canonicality KATs, database I/O and the generators.  No GPU call."""
+import hashlib
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, REPO, golden_runs, read_lines, run_oracle
+
+REF_TREE = os.environ.get("REF", "/root/reference")
+
+
+def test_header_symbols_exported(gs):
+    with open(os.path.join(REPO, "include", "gspan_gb300.h")) as f:
+        hdr = f.read()
+    declared = set(re.findall(r"GS_API\s+[^;(]*?\b(gs_\w+)\s*\(", hdr))
+    assert declared, "no declarations parsed"
+    assert declared == set(gs.EXPORTS)
+    lib = gs.lib()
+    for name in declared:
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", gs.LIB_PATH], stdout=subprocess.PIPE, text=True).stdout
+    exported = set(re.findall(r"\b(gs_\w+)$", out, re.M))
+    assert declared <= exported
+
+
+def test_ismin_kats(gs):
+    n = 0
+    for line in read_lines(os.path.join(GOLDEN, "ismin_kats.tsv")):
+        if line.startswith("#"):
+            continue
+        exp, code = line.split("\t")
+        assert gs.dfs_code_is_min(gs.parse_code(code)) == (exp == "1"), code
+        n += 1
+    assert n == 12
+
+
+@pytest.mark.parametrize("run", golden_runs(), ids=lambda r: "%s-s%d" % (r[1], r[2]))
+def test_oracle_matches_reference_golden(oracle, run):
+    ft, db, s, out = run
+    got = run_oracle(oracle, ft, os.path.join(GOLDEN, db), s)
+    assert got == read_lines(os.path.join(GOLDEN, out))
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REF_TREE, "testdata", "Chemical_340")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("minsup", [68, 34])
+def test_oracle_matches_reference_binary_on_chemical340(oracle, minsup):
+    ref = os.path.join(REPO, "oracle", "_ref", "gspan_ref")
+    if not os.path.exists(ref):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref"])
+    path = os.path.join(REF_TREE, "testdata", "Chemical_340")
+    want = run_oracle(ref, "txt", path, minsup)
+    got = run_oracle(oracle, "txt", path, minsup)
+    assert got == want
+
+
+def test_oracle_time_limit_gives_prefix(oracle):
+    full = run_oracle(oracle, "txt", os.path.join(GOLDEN, "cfg1_seed1.txt"), 5)
+    part = run_oracle(oracle, "txt", os.path.join(GOLDEN, "cfg1_seed1.txt"), 5, ["--time-limit", "0.000001"])
+    assert full[:len(part)] == part
+
+
+def test_oracle_exit_codes(oracle):
+    db = os.path.join(GOLDEN, "fixture_get_test_database.txt")
+    assert subprocess.run([oracle, "txt", db, "18"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode == 2
+    assert subprocess.run([oracle, "txt", db, "0"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode == 3
+
+
+def _canon(db_path, ftype, gs):
+    """Order-free form of a database: per graph, vertex labels and sorted edge triples."""
+    tmp = db_path + ".canon.txt"
+    gs.Database.load(db_path, ftype).write(tmp, "txt")
+    graphs, cur = [], None
+    for line in read_lines(tmp):
+        p = line.split()
+        if p[0] == "t":
+            cur = ([], [])
+            graphs.append(cur)
+        elif p[0] == "v":
+            cur[0].append(int(p[2]))
+        elif p[0] == "e":
+            a, b, l = int(p[1]), int(p[2]), int(p[3])
+            cur[1].append((min(a, b), max(a, b), l))
+    os.remove(tmp)
+    return [(tuple(v), tuple(sorted(e))) for v, e in graphs]
+
+
+@pytest.mark.parametrize("ftype", ["txt", "bin", "cudabin"])
+def test_database_roundtrip(gs, tmp_path, ftype):
+    src = os.path.join(GOLDEN, "cfg1_seed1.txt")
+    d = gs.Database.load(src, "txt")
+    out = str(tmp_path / ("db." + ftype))
+    d.write(out, ftype)
+    assert _canon(src, "txt", gs) == _canon(out, ftype, gs)
+    assert len(gs.Database.load(out, ftype)) == len(d) == 340
+
+
+def test_bin_fixture_matches_txt_fixture(gs):
+    # testdata/labeled.bin serialises the labeled test database (test_support.cpp)
+    a = _canon(os.path.join(GOLDEN, "fixture_labeled.bin"), "bin", gs)
+    b = _canon(os.path.join(GOLDEN, "fixture_get_labeled_test_database.txt"), "txt", gs)
+    assert a == b
+
+
+def test_from_arrays_matches_cudabin_file(gs, tmp_path):
+    import numpy as np
+    d = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    p = str(tmp_path / "c.cudabin")
+    d.write(p, "cudabin")
+    raw = np.fromfile(p, dtype=np.int32)
+    n, esz, maxv, vc = raw[:4]
+    o = 4
+    edges = raw[o:o + esz]; o += esz
+    elab = raw[o:o + esz]; o += esz
+    vlab = raw[o:o + n * maxv]; o += n * maxv
+    voff = raw[o:o + n * maxv + 1]
+    d2 = gs.Database.from_arrays(n, maxv, edges, elab, vlab, voff, vc)
+    assert d2.info()["adjacency_entries"] == d.info()["adjacency_entries"]
+    assert d2.info()["vertices"] == d.info()["vertices"]
+
+
+def test_fsg_labels_renumbered_per_graph(gs, tmp_path):
+    # Graph::read_fsg numbers string labels per graph by first appearance
+    p = tmp_path / "x.fsg"
+    p.write_text("t # 0\nv 0 C\nv 1 O\nu 0 1 s\nt # 1\nv 0 O\nv 1 C\nu 0 1 d\n")
+    d = gs.Database.load(str(p), "fsg")
+    out = tmp_path / "x.txt"
+    d.write(str(out), "txt")
+    assert read_lines(str(out)) == ["t # 0", "v 0 0", "v 1 1", "e 0 1 0", "t # 1", "v 0 0", "v 1 1", "e 0 1 0"]
+
+
+def test_load_errors(gs, tmp_path):
+    with pytest.raises(gs.GSpanError) as e:
+        gs.Database.load(str(tmp_path / "missing.txt"), "txt")
+    assert e.value.status == 2
+    p = tmp_path / "loop.txt"
+    p.write_text("t # 0\nv 0 1\nv 1 1\ne 0 0 1\n")
+    with pytest.raises(gs.GSpanError) as e:
+        gs.Database.load(str(p), "txt")
+    assert e.value.status == 3
+    p = tmp_path / "par.txt"
+    p.write_text("t # 0\nv 0 1\nv 1 1\ne 0 1 1\ne 1 0 2\n")
+    with pytest.raises(gs.GSpanError) as e:
+        gs.Database.load(str(p), "txt")
+    assert e.value.status == 3
+    p = tmp_path / "order.txt"
+    p.write_text("t # 0\nv 0 1\ne 0 1 1\nv 1 1\n")
+    with pytest.raises(gs.GSpanError):
+        gs.Database.load(str(p), "txt")
+    with pytest.raises(ValueError):
+        gs.filetype("xml")
+
+
+def test_generator_deterministic(gs, tmp_path):
+    a, b = str(tmp_path / "a.txt"), str(tmp_path / "b.txt")
+    gs.Database.generate(2, seed=7, scale=0.01).write(a)
+    gs.Database.generate(2, seed=7, scale=0.01).write(b)
+    assert open(a).read() == open(b).read()
+    c = str(tmp_path / "c.txt")
+    gs.Database.generate(2, seed=8, scale=0.01).write(c)
+    assert open(a).read() != open(c).read()
+    # the committed configuration-1 fixture is what the generator makes
+    gs.Database.generate(1, seed=1).write(c)
+    assert hashlib.sha256(open(c, "rb").read()).hexdigest() == \
+        hashlib.sha256(open(os.path.join(GOLDEN, "cfg1_seed1.txt"), "rb").read()).hexdigest()
+
+
+def test_generator_shapes(gs):
+    i = gs.Database.generate(2, scale=0.02).info()
+    assert i["graphs"] == 2000 and i["vertex_labels"] == 5 and i["edge_labels"] == 5
+    mean_edges = i["adjacency_entries"] / 2 / i["graphs"]
+    assert 27 < mean_edges < 34
+    i = gs.Database.generate(5, scale=0.001).info()
+    assert i["graphs"] == 1000 and i["vertex_labels"] == 10 and i["edge_labels"] == 3
+    i = gs.Database.generate(1).info()
+    assert i["graphs"] == 340 and i["edge_labels"] == 4
+
+
+def test_cli_exit_codes(gs):
+    db = os.path.join(GOLDEN, "fixture_get_test_database.txt")
+    r = subprocess.run([gs.CLI_PATH], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    assert r.returncode == 1
+    r = subprocess.run([gs.CLI_PATH, "txt", db, "18"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    assert r.returncode == 2
+    r = subprocess.run([gs.CLI_PATH, "txt", db, "0"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    assert r.returncode == 3

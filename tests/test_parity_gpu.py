@@ -1,0 +1,186 @@
+"""GPU parity: the miner through the C ABI against the reference's golden
+outputs and against the oracle on the same seeded inputs.  Bit-exact: same
+patterns, same DFS codes, same supports, same order."""
+import hashlib
+import os
+
+import pytest
+
+from conftest import GOLDEN, golden_runs, read_lines, run_oracle, to_lines
+
+pytestmark = pytest.mark.gpu
+
+
+def _mine_lines(gs, db, minsup, **kw):
+    pats, stats = gs.mine(db, minsup, label_style=gs.LABELS_SEQ, **kw)
+    return to_lines(pats, gs), stats
+
+
+@pytest.mark.parametrize("run", golden_runs(), ids=lambda r: "%s-s%d" % (r[1], r[2]))
+def test_golden_parity(gs, run):
+    ft, dbf, s, out = run
+    db = gs.Database.load(os.path.join(GOLDEN, dbf), ft)
+    got, stats = _mine_lines(gs, db, s)
+    assert got == read_lines(os.path.join(GOLDEN, out))
+    assert stats["launches"] > 0
+
+
+@pytest.mark.parametrize("wave_nodes", [1, 3, 64])
+@pytest.mark.parametrize("minsup", [34, 5])
+def test_wave_sizes_agree(gs, wave_nodes, minsup):
+    db = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    got, stats = _mine_lines(gs, db, minsup, wave_nodes=wave_nodes)
+    assert got == read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s%d.txt" % minsup))
+    if wave_nodes == 1:
+        assert stats["waves"] == stats["nodes"]
+
+
+def test_small_waves_by_rows(gs):
+    # a tiny row budget splits waves by rows instead of node count
+    db = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    got, _ = _mine_lines(gs, db, 10, wave_rows=64, wave_words=64)
+    assert got == read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s10.txt"))
+
+
+def test_full_label_codes(gs):
+    db = gs.Database.load(os.path.join(GOLDEN, "fixture_get_labeled_test_database2.txt"), "txt")
+    pats, _ = gs.mine(db, 2, label_style=gs.LABELS_FULL)
+    seq = []
+    for code, sup in pats:
+        lab = {}
+        for i, (f, t, fl, el, tl) in enumerate(code):
+            assert fl != -1 and tl != -1
+            if i == 0:
+                lab[f] = fl
+            assert lab[f] == fl
+            if f < t:
+                lab[t] = tl
+            assert lab[t] == tl
+        s = [code[0]] + [(f, t, -1, el, tl if f < t else -1) for f, t, fl, el, tl in code[1:]]
+        seq.append("%s\t%d" % (gs.code_to_string(s), sup))
+    assert seq == read_lines(os.path.join(GOLDEN, "out_fixture_get_labeled_test_database2_s2.txt"))
+
+
+@pytest.mark.parametrize("config,scale,minsups", [(2, 0.02, (40, 20)), (5, 0.002, (10,)), (3, 0.05, (None,)),
+                                                   (4, 0.02, (None,))])
+def test_generated_vs_oracle(gs, oracle, tmp_path, config, scale, minsups):
+    db = gs.Database.generate(config, scale=scale)
+    p = str(tmp_path / "db.txt")
+    db.write(p, "txt")
+    for s in minsups:
+        s = s or max(2, int(0.05 * len(db)))
+        want = run_oracle(oracle, "txt", p, s)
+        got, _ = _mine_lines(gs, db, s)
+        assert got == want, (config, s)
+
+
+def test_cudabin_and_bin_inputs(gs, tmp_path):
+    src = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    want = read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s17.txt"))
+    for ft in ("cudabin", "bin"):
+        p = str(tmp_path / ("db." + ft))
+        src.write(p, ft)
+        got, _ = _mine_lines(gs, gs.Database.load(p, ft), 17)
+        assert got == want, ft
+
+
+@pytest.mark.parametrize("max_edges", [1, 2, 4])
+def test_max_edges(gs, oracle, max_edges):
+    p = os.path.join(GOLDEN, "cfg1_seed1.txt")
+    want = run_oracle(oracle, "txt", p, 10, ["--max-edges", str(max_edges)])
+    got, _ = _mine_lines(gs, gs.Database.load(p, "txt"), 10, max_edges=max_edges)
+    assert got == want
+
+
+def test_batch_equals_solo(gs):
+    dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.05) for i in range(4)]
+    sups = [max(2, int(0.05 * len(d))) for d in dbs]
+    batch, stats = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ)
+    for d, s, got in zip(dbs, sups, batch):
+        solo, _ = gs.mine(d, s, label_style=gs.LABELS_SEQ)
+        assert got == solo
+    assert stats["patterns"] == sum(len(b) for b in batch)
+
+
+def test_repeat_is_deterministic(gs):
+    db = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    a, _ = gs.mine(db, 10)
+    b, _ = gs.mine(db, 10)
+    assert a == b
+
+
+def test_minsup_bounds(gs):
+    db = gs.Database.load(os.path.join(GOLDEN, "fixture_get_test_database.txt"), "txt")
+    with pytest.raises(gs.GSpanError) as e:
+        gs.mine(db, len(db))
+    assert e.value.status == 6
+    with pytest.raises(gs.GSpanError) as e:
+        gs.mine(db, 0)
+    assert e.value.status == 7
+    # the engine stays usable after a rejected call
+    got, _ = _mine_lines(gs, db, 9)
+    assert got == read_lines(os.path.join(GOLDEN, "out_fixture_get_test_database_s9.txt"))
+
+
+def _kat(path):
+    recs, dfs = [], []
+    for line in read_lines(path):
+        if line.startswith("#"):
+            mvc = int(line.rsplit("=", 1)[1])
+            continue
+        kind, rest = line.split("\t", 1)
+        if kind == "rec":
+            recs.append(tuple(int(x) for x in rest.split()))
+        else:
+            d, s = rest.split("\t")
+            dfs.append((tuple(int(x) for x in d.split()), int(s)))
+    return recs, dfs, mvc
+
+
+@pytest.mark.parametrize("name", ["support_kat.tsv", "extract_kat.tsv"])
+def test_support_kats(gs, name):
+    # records (from, to, fl, el, tl, from_grph, to_grph, row); graph = vertex // max_graph_vertex_count
+    recs, dfs, mvc = _kat(os.path.join(GOLDEN, name))
+    keys = sorted({r[:5] for r in recs})
+    kid = {k: i for i, k in enumerate(keys)}
+    sup = gs.support_count([kid[r[:5]] for r in recs], [r[5] // mvc for r in recs], len(keys), 10)
+    got = {k: sup[kid[k]] for k in keys}
+    assert got == {d: s for d, s in dfs}
+
+
+def test_support_count_rejects_out_of_range(gs):
+    with pytest.raises(gs.GSpanError):
+        gs.support_count([0, 5], [0, 0], 2, 4)
+
+
+def _fullsize():
+    rows = []
+    for line in read_lines(os.path.join(GOLDEN, "fullsize.tsv")):
+        if line.startswith("#"):
+            continue
+        c, seed, scale, dbsha, s, n, sha = line.split("\t")
+        rows.append((int(c), int(seed), float(scale), dbsha, int(s), int(n), sha))
+    return rows
+
+
+@pytest.mark.parametrize("row", _fullsize(), ids=lambda r: "cfg%d-s%d" % (r[0], r[4]))
+def test_full_size_checksums(gs, tmp_path, row):
+    config, seed, scale, dbsha, s, n, sha = row
+    db = gs.Database.generate(config, seed=seed, scale=scale)
+    p = str(tmp_path / "db.txt")
+    db.write(p, "txt")
+    assert hashlib.sha256(open(p, "rb").read()).hexdigest() == dbsha
+    lines, stats = _mine_lines(gs, db, s)
+    assert len(lines) == n
+    assert hashlib.sha256(("\n".join(lines) + "\n").encode()).hexdigest() == sha
+    # size-independent properties
+    sup = {}
+    for line in lines:
+        code, v = line.split("\t")
+        assert int(v) >= s
+        sup[code] = int(v)
+    for code, v in sup.items():
+        parts = code.split(";")
+        if len(parts) > 1:
+            parent = ";".join(parts[:-1])
+            assert parent in sup and sup[parent] >= v
