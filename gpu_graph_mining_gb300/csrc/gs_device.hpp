@@ -71,7 +71,7 @@ struct ChildOut {
   int2 *col0;     // root children only: column 0
   int32_t *gord;  // the child's graph ranks
   int32_t kind;   // 0 forward, 1 backward, 2 root
-  int32_t pad;
+  int32_t cap;    // rows allocated (the count pass's embedding count for the key)
 };
 
 }  // namespace gsgb

@@ -613,6 +613,8 @@ public:
     unsigned long long bytes[4] = { 0, 0, 0, 0 };
     d2h(bytes, E.d_bytes.p, sizeof(bytes));
     CK(cudaStreamSynchronize(E.stream));
+    CK(cudaGetLastError());
+    if(bytes[3]) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(bytes[3]) + ")");
     st_.count_bytes += (int64_t)bytes[0];
     st_.mat_bytes += (int64_t)bytes[1];
     st_.peak_pool_bytes = std::max<int64_t>(st_.peak_pool_bytes, (int64_t)E.pool.peak());
@@ -638,6 +640,16 @@ private:
   {
     CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, E.stream));
     st_.d2h_bytes += (int64_t)n;
+  }
+
+  // device error flag of the kernels' consistency checks (slot 3 of the counters)
+  unsigned int *err_flag() { return reinterpret_cast<unsigned int *>(E.d_bytes.p + 3); }
+  void check_err()
+  {
+    unsigned long long v = 0;
+    CK(cudaMemcpyAsync(&v, E.d_bytes.p + 3, sizeof(v), cudaMemcpyDeviceToHost, E.stream));
+    CK(cudaStreamSynchronize(E.stream));
+    if(v) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(v) + ")");
   }
 
   void flush_timing()
@@ -711,7 +723,7 @@ private:
         char *blk = (char *)E.pool.alloc((size_t)n * 8);
         char *blk0 = (char *)E.pool.alloc((size_t)n * 8);
         int32_t *gord = (int32_t *)E.pool.alloc((size_t)n * 4);
-        ChildOut o{ (int2 *)blk, (int2 *)blk0, gord, 2, 0 };
+        ChildOut o{ (int2 *)blk, (int2 *)blk0, gord, 2, (int32_t)n };
         E.h_childmap.p[key] = (int32_t)outs.size();
         outs.push_back(o);
         PNode nn;
@@ -734,12 +746,13 @@ private:
       h2d(E.d_childmap.p, E.h_childmap.p, (size_t)R * 4);
       CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
       launch_root_materialize(db.dev, db.d_root_off, E.d_bm.p, E.d_bmx.p, words, E.d_childmap.p, E.d_cursor.p,
-                              E.d_outs.p, E.stream);
+                              E.d_outs.p, err_flag(), E.stream);
       st_.launches++;
       // the pinned childmap/outs mirrors are rewritten by the next phase:
       // wait for the copies (and the kernel) before reusing them
       CK(cudaStreamSynchronize(E.stream));
       CK(cudaGetLastError());
+      check_err();
     }
     for(auto it = made.rbegin(); it != made.rend(); ++it) stack_.push_back(std::move(*it));
   }
@@ -778,8 +791,8 @@ private:
     }
     size_t off = 0;
     char *hb = nullptr;
-    size_t need = 256 * 5 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
-                  sizeof(int32_t) * tot_cols;
+    size_t need = 256 * 6 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
+                  2 * sizeof(int32_t) * tot_cols;
     E.h_desc.ensure(need);
     E.d_desc.ensure(need);
     hb = E.h_desc.p;
@@ -787,6 +800,7 @@ private:
     const int2 **hc = carve<const int2 *>(hb, off, tot_cols);
     SlotDesc *hs = carve<SlotDesc>(hb, off, tot_slots);
     int32_t *hv = carve<int32_t>(hb, off, tot_cols);
+    int32_t *hl = carve<int32_t>(hb, off, tot_cols);
     const size_t desc_bytes = off;
     int32_t co = 0, so = 0;
     int64_t rb = 0, bb = 0;
@@ -813,6 +827,7 @@ private:
       d.db = js_[p.job].db_slot;
       for(size_t c = 0; c < p.cols.size(); c++) {
         hc[co + c] = E.cols[p.cols[c]].ptr;
+        hl[co + c] = (int32_t)E.cols[p.cols[c]].n;
         hv[co + c] = -1;
       }
       for(size_t s = 0; s < L.slots.size(); s++) {
@@ -830,6 +845,7 @@ private:
     const int2 *const *dc = (const int2 *const *)(db_ + ((char *)hc - hb));
     const SlotDesc *ds = (const SlotDesc *)(db_ + ((char *)hs - hb));
     const int32_t *dv = (const int32_t *)(db_ + ((char *)hv - hb));
+    const int32_t *dl = (const int32_t *)(db_ + ((char *)hl - hb));
     E.d_bm.ensure(std::max<int64_t>(bb, 1));
     E.d_bmx.ensure(std::max<int64_t>(bb, 1));
     E.d_cnt.ensure(std::max(kb, 1));
@@ -839,7 +855,8 @@ private:
     CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
     CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
     CK(cudaEventRecord(E.ev[0], E.stream));
-    launch_wave_count(dn, W, rows, dc, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, E.stream);
+    launch_wave_count(dn, W, rows, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
+                      E.stream);
     CK(cudaEventRecord(E.ev[1], E.stream));
     launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
     CK(cudaEventRecord(E.ev[2], E.stream));
@@ -850,6 +867,7 @@ private:
     d2h(E.h_cnt.p, E.d_cnt.p, (size_t)kb * 4);
     CK(cudaStreamSynchronize(E.stream));
     CK(cudaGetLastError());
+    check_err();
     flush_timing();
     st_.count_ms += ms_between(E.ev[0], E.ev[1]);
     st_.support_ms += ms_between(E.ev[1], E.ev[2]);
@@ -918,7 +936,7 @@ private:
           const int64_t rowsn = c.cnt;
           int2 *col = (int2 *)E.pool.alloc((size_t)rowsn * 8);
           int32_t *gord = (int32_t *)E.pool.alloc((size_t)rowsn * 4);
-          ChildOut o{ col, nullptr, gord, c.dfs.is_forward() ? 0 : 1, 0 };
+          ChildOut o{ col, nullptr, gord, c.dfs.is_forward() ? 0 : 1, (int32_t)rowsn };
           E.h_childmap.p[hn[n].key_base + c.key] = (int32_t)outs.size();
           outs.push_back(o);
           PNode nn;
@@ -951,8 +969,8 @@ private:
       h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
       CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(E.ev[4], E.stream));
-      launch_wave_materialize(dn, W, rows, dc, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p, E.d_cursor.p,
-                              E.d_outs.p, E.d_bytes.p + 1, E.stream);
+      launch_wave_materialize(dn, W, rows, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
+                              E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
       CK(cudaEventRecord(E.ev[5], E.stream));
       st_.launches++;
       mat_pending_ = true;

@@ -46,16 +46,20 @@ __device__ __forceinline__ int find_node_by_key(const NodeDesc *nodes, int n, in
 
 // Enumerates the valid one-edge extensions of embedding row i of a node and
 // calls visit(key, neighbour, is_backward) for each.  phi receives the graph
-// vertex of every pattern vertex.  Returns the algorithmic bytes read.
+// vertex of every pattern vertex.  Adds the algorithmic bytes read to bytes.
+// Every data-dependent index is checked (back-link rows against column
+// lengths, vertices against the database, pair indices against -1); a failed
+// check skips the row and returns false so the caller can raise the error flag.
 template <class Visit>
-__device__ __forceinline__ unsigned enumerate_row(const NodeDesc &nd, const DevDB &db, const int2 *const *cols,
-                                                  const SlotDesc *slots, const int32_t *vtab, int i, int *phi,
-                                                  int &last_prev, Visit &visit)
+__device__ __forceinline__ bool enumerate_row(const NodeDesc &nd, const DevDB &db, const int2 *const *cols,
+                                              const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
+                                              int i, int *phi, int &last_prev, unsigned &bytes, Visit &visit)
 {
-  unsigned bytes = 0;
   int idx = i;
   for(int c = nd.k - 1; c >= 0; --c) {
+    if((unsigned)idx >= (unsigned)collen[c]) return false;
     const int2 e = __ldg(&cols[c][idx]);
+    if((unsigned)e.x >= (unsigned)db.n_vertices) return false;
     phi[c] = e.x;
     if(c == nd.k - 1) last_prev = e.y;
     idx = e.y;
@@ -80,7 +84,9 @@ __device__ __forceinline__ unsigned enumerate_row(const NodeDesc &nd, const DevD
         bool in_emb = false;
         for(int t = 0; t < nd.k; ++t) in_emb |= (phi[t] == w);
         if(in_emb) continue;
-        visit(sd.fkey_off + __ldg(&db.pair_idx[((long long)sd.vlab * db.EL + el) * db.VL + wl]), w, false);
+        const int pk = __ldg(&db.pair_idx[((long long)sd.vlab * db.EL + el) * db.VL + wl]);
+        if(pk < 0) return false;
+        visit(sd.fkey_off + pk, w, false);
       } else {
         int j = -1;
         for(int t = 0; t < nd.k; ++t) if(phi[t] == w) j = t;
@@ -94,11 +100,13 @@ __device__ __forceinline__ unsigned enumerate_row(const NodeDesc &nd, const DevD
           continue;
         }
         if(wl < nd.minlabel) continue;
-        visit(sd.fkey_off + __ldg(&db.pair_idx[((long long)sd.vlab * db.EL + el) * db.VL + wl]), w, false);
+        const int pk = __ldg(&db.pair_idx[((long long)sd.vlab * db.EL + el) * db.VL + wl]);
+        if(pk < 0) return false;
+        visit(sd.fkey_off + pk, w, false);
       }
     }
   }
-  return bytes;
+  return true;
 }
 
 struct CountVisit {
@@ -126,6 +134,7 @@ struct MatVisit {
   long long base;
   int words, g, key_base, row, k;
   unsigned n, nsel;
+  bool overflow;
   __device__ __forceinline__ void operator()(int key, int w, bool bwd)
   {
     n++;
@@ -136,6 +145,10 @@ struct MatVisit {
     const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (g & 31)) - 1u));
     const int pos = atomicAdd(&cursor[c], 1);
     const ChildOut o = outs[c];
+    if(pos >= o.cap) {  // more rows than the count pass saw: never write past the slot
+      overflow = true;
+      return;
+    }
     o.col[pos] = bwd ? make_int2(phi[k - 1], *last_prev) : make_int2(w, row);
     o.gord[pos] = rank;
   }
@@ -151,10 +164,11 @@ __device__ __forceinline__ void add_bytes(unsigned long long *bytes, unsigned lo
 
 __global__ void __launch_bounds__(kBlock) k_wave_count(const NodeDesc *__restrict__ nodes, int nnodes,
                                                         long long total_rows, const int2 *const *__restrict__ coltab,
+                                                        const int32_t *__restrict__ collen,
                                                         const SlotDesc *__restrict__ slottab,
                                                         const int32_t *__restrict__ vtab,
                                                         const DevDB *__restrict__ dbs, uint32_t *bm, int32_t *cnt,
-                                                        unsigned long long *bytes)
+                                                        unsigned long long *bytes, unsigned int *err)
 {
   int phi[kMaxV];
   unsigned long long mine = 0;
@@ -165,10 +179,16 @@ __global__ void __launch_bounds__(kBlock) k_wave_count(const NodeDesc *__restric
     const DevDB db = dbs[nd.db];
     const int i = (int)(r - nd.row_begin);
     const int g = nd.gord[i];
+    if((unsigned)g >= (unsigned)nd.words * 32u) {
+      atomicOr(err, 1u);
+      continue;
+    }
     CountVisit v{ bm, cnt, nd.bm_base, nd.words, g, nd.key_base, 0u };
     int last_prev = 0;
-    unsigned b = enumerate_row(nd, db, coltab + nd.col_off, slottab + nd.slot_off, vtab + nd.vtab_off, i, phi,
-                               last_prev, v);
+    unsigned b = 0;
+    if(!enumerate_row(nd, db, coltab + nd.col_off, collen + nd.col_off, slottab + nd.slot_off, vtab + nd.vtab_off,
+                      i, phi, last_prev, b, v))
+      atomicOr(err, 2u);
     mine += b + 4u + 8ull * v.n;  // gord read; one bitmap word and one counter update per extension
   }
   add_bytes(bytes, mine);
@@ -176,9 +196,10 @@ __global__ void __launch_bounds__(kBlock) k_wave_count(const NodeDesc *__restric
 
 __global__ void __launch_bounds__(kBlock) k_wave_materialize(
     const NodeDesc *__restrict__ nodes, int nnodes, long long total_rows, const int2 *const *__restrict__ coltab,
-    const SlotDesc *__restrict__ slottab, const int32_t *__restrict__ vtab, const DevDB *__restrict__ dbs,
-    const uint32_t *__restrict__ bm, const int32_t *__restrict__ bmx, const int32_t *__restrict__ childmap,
-    int32_t *cursor, const ChildOut *__restrict__ outs, unsigned long long *bytes)
+    const int32_t *__restrict__ collen, const SlotDesc *__restrict__ slottab, const int32_t *__restrict__ vtab,
+    const DevDB *__restrict__ dbs, const uint32_t *__restrict__ bm, const int32_t *__restrict__ bmx,
+    const int32_t *__restrict__ childmap, int32_t *cursor, const ChildOut *__restrict__ outs,
+    unsigned long long *bytes, unsigned int *err)
 {
   int phi[kMaxV];
   unsigned long long mine = 0;
@@ -189,10 +210,18 @@ __global__ void __launch_bounds__(kBlock) k_wave_materialize(
     const DevDB db = dbs[nd.db];
     const int i = (int)(r - nd.row_begin);
     const int g = nd.gord[i];
+    if((unsigned)g >= (unsigned)nd.words * 32u) {
+      atomicOr(err, 1u);
+      continue;
+    }
     int last_prev = 0;
-    MatVisit v{ bm, bmx, childmap, cursor, outs, phi, &last_prev, nd.bm_base, nd.words, g, nd.key_base, i, nd.k, 0u, 0u };
-    unsigned b = enumerate_row(nd, db, coltab + nd.col_off, slottab + nd.slot_off, vtab + nd.vtab_off, i, phi,
-                               last_prev, v);
+    MatVisit v{ bm, bmx, childmap, cursor, outs, phi, &last_prev, nd.bm_base, nd.words, g, nd.key_base, i, nd.k,
+                0u, 0u, false };
+    unsigned b = 0;
+    if(!enumerate_row(nd, db, coltab + nd.col_off, collen + nd.col_off, slottab + nd.slot_off, vtab + nd.vtab_off,
+                      i, phi, last_prev, b, v))
+      atomicOr(err, 2u);
+    if(v.overflow) atomicOr(err, 4u);
     mine += b + 4u + 4ull * v.n + 20ull * v.nsel;  // childmap per extension; bitmap, prefix, column, rank per selected
   }
   add_bytes(bytes, mine);
@@ -226,7 +255,7 @@ __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int
                                                               const uint32_t *__restrict__ bm,
                                                               const int32_t *__restrict__ bmx, int32_t words,
                                                               const int32_t *__restrict__ childmap, int32_t *cursor,
-                                                              const ChildOut *__restrict__ outs)
+                                                              const ChildOut *__restrict__ outs, unsigned int *err)
 {
   const int stride = gridDim.x * blockDim.x;
   for(int v = blockIdx.x * blockDim.x + threadIdx.x; v < db.n_vertices; v += stride) {
@@ -246,6 +275,10 @@ __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int
       const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (g & 31)) - 1u));
       const int pos = atomicAdd(&cursor[c], 1);
       const ChildOut o = outs[c];
+      if(pos >= o.cap) {
+        atomicOr(err, 4u);
+        continue;
+      }
       o.col0[pos] = make_int2(v, -1);
       o.col[pos] = make_int2(w, pos);
       o.gord[pos] = rank;
@@ -307,28 +340,29 @@ void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, i
 
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
                              int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             cudaStream_t s)
+                             unsigned int *err, cudaStream_t s)
 {
-  k_root_materialize<<<grid_for(db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, bmx, words, childmap, cursor, outs);
+  k_root_materialize<<<grid_for(db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, bmx, words, childmap, cursor, outs,
+                                                                 err);
 }
 
 void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
-                       const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
-                       unsigned long long *bytes, cudaStream_t s)
+                       const int32_t *collen, const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs,
+                       uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err, cudaStream_t s)
 {
   if(total_rows <= 0) return;
-  k_wave_count<<<grid_for(total_rows), kBlock, 0, s>>>(nodes, nnodes, total_rows, coltab, slots, vtab, dbs, bm, cnt,
-                                                        bytes);
+  k_wave_count<<<grid_for(total_rows), kBlock, 0, s>>>(nodes, nnodes, total_rows, coltab, collen, slots, vtab, dbs,
+                                                        bm, cnt, bytes, err);
 }
 
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
-                             const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs, const uint32_t *bm,
-                             const int32_t *bmx, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned long long *bytes, cudaStream_t s)
+                             const int32_t *collen, const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs,
+                             const uint32_t *bm, const int32_t *bmx, const int32_t *childmap, int32_t *cursor,
+                             const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s)
 {
   if(total_rows <= 0) return;
-  k_wave_materialize<<<grid_for(total_rows), kBlock, 0, s>>>(nodes, nnodes, total_rows, coltab, slots, vtab, dbs, bm,
-                                                              bmx, childmap, cursor, outs, bytes);
+  k_wave_materialize<<<grid_for(total_rows), kBlock, 0, s>>>(nodes, nnodes, total_rows, coltab, collen, slots, vtab,
+                                                              dbs, bm, bmx, childmap, cursor, outs, bytes, err);
 }
 
 void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n, int32_t words, uint32_t *bm,

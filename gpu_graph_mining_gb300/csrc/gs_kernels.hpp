@@ -1,5 +1,8 @@
 // Launchers for the mining kernels (gs_kernels.cu).  All launches go to the
-// given stream; none synchronises.
+// given stream; none synchronises.  `err` receives bit flags when a kernel's
+// consistency checks fail (1: graph rank out of range, 2: back-link, vertex or
+// label-pair index out of range, 4: more child rows than counted); the
+// offending access is skipped, never performed.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -17,16 +20,17 @@ void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, i
 // Writes the two columns and graph ranks of every selected root key.
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
                              int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             cudaStream_t s);
+                             unsigned int *err, cudaStream_t s);
 
 // Wave level: one thread per embedding row of every node of the wave.
+// collen[] parallels coltab[]: the length of every column.
 void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
-                       const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
-                       unsigned long long *bytes, cudaStream_t s);
+                       const int32_t *collen, const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs,
+                       uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err, cudaStream_t s);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
-                             const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs, const uint32_t *bm,
-                             const int32_t *bmx, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned long long *bytes, cudaStream_t s);
+                             const int32_t *collen, const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs,
+                             const uint32_t *bm, const int32_t *bmx, const int32_t *childmap, int32_t *cursor,
+                             const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s);
 
 // Extension records given as (key, graph id) pairs: sets bit [key][graph].
 // Keys and graph ids must be in range (checked by the caller).
