@@ -910,6 +910,7 @@ private:
     }
 
     // accepted children: output tree, materialisation slots
+    E.h_childmap.ensure(std::max(kb, 1));
     for(int32_t i = 0; i < kb; i++) E.h_childmap.p[i] = -1;
     std::vector<ChildOut> outs;
     std::vector<std::vector<PNode>> made(W);
