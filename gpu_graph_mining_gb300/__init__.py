@@ -30,8 +30,8 @@ STATUS_NAMES = {
 EXPORTS = [
     "gs_last_error", "gs_filetype_from_name", "gs_db_load", "gs_db_from_arrays", "gs_db_generate",
     "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
-    "gs_mine", "gs_mine_ex", "gs_mine_batch", "gs_support_count", "gs_dfs_code_is_min", "gs_engine_reset",
-    "gs_engine_set_pool_bytes",
+    "gs_mine", "gs_mine_ex", "gs_mine_batch", "gs_support_count", "gs_support_count_noalloc",
+    "gs_dfs_code_is_min", "gs_engine_reset", "gs_engine_set_pool_bytes",
 ]
 
 
@@ -113,6 +113,8 @@ def lib():
     L.gs_mine_batch.restype = i32
     L.gs_support_count.argtypes = [pi32, pi32, i64, i32, i32, pi32]
     L.gs_support_count.restype = i32
+    L.gs_support_count_noalloc.argtypes = [vp, vp, i64, i32, i32, vp, vp]
+    L.gs_support_count_noalloc.restype = i32
     L.gs_dfs_code_is_min.argtypes = [pi32, i32]
     L.gs_dfs_code_is_min.restype = i32
     L.gs_engine_reset.argtypes = []

@@ -93,6 +93,10 @@ void batch_trampoline(const int32_t *dfs, int32_t n, int64_t sup, void *u)
 
 }  // namespace
 
+namespace gsgb {
+void capi_set_error(const char *msg) { t_err = msg ? msg : ""; }
+}  // namespace gsgb
+
 extern "C" {
 
 const char *gs_last_error(void) { return t_err.c_str(); }

@@ -178,6 +178,34 @@ GS_API gs_status gs_mine_batch(gs_db *const *dbs, int32_t n, const int32_t *abs_
 GS_API gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids, int64_t n_records, int32_t n_keys,
                                   int32_t n_graphs, int32_t *support);
 
+/* gs_support_count for callers that cannot allocate device memory: code that
+ * runs inside another framework's memory arena or allocator (which must own
+ * and account for every device allocation), processes given a fixed device
+ * memory budget up front, and code paths that must not incur the implicit
+ * device synchronisation cudaMalloc/cudaFree can cause.  No counterpart in
+ * the reference.
+ *
+ * It allocates nothing.  The caller passes DEVICE pointers it owns: keys and
+ * graph ids (n_records each) and support (n_keys int32, written by the call).
+ * The only scratch, the support bitmaps, is a fixed 4 MiB device array inside
+ * this library that every GPU which loads the library holds until the process
+ * exits; it must hold n_keys * ceil(n_graphs / 32) 32-bit words, at most
+ * GS_NOALLOC_MAX_BITMAP_WORDS (1,048,576), else the call returns
+ * GS_ERR_LIMIT and launches nothing.  Records whose key or graph id is out of
+ * range are ignored.  Work is queued on `stream` (a cudaStream_t; NULL = the
+ * default stream) and the call returns without synchronising; support is
+ * ready when the stream reaches that point.
+ *
+ * The first call on each device looks up the scratch's device address
+ * (cudaGetSymbolAddress, which may load the module): make that first call
+ * before any stream capture.  Every call shares the one scratch array and
+ * clears the part it uses before use, so calls that may overlap on the GPU
+ * (different streams, or threads without ordering) race and give wrong
+ * results: serialise them. */
+#define GS_NOALLOC_MAX_BITMAP_WORDS (1u << 20)
+GS_API gs_status gs_support_count_noalloc(const int32_t *d_keys, const int32_t *d_graph_ids, int64_t n_records,
+                                          int32_t n_keys, int32_t n_graphs, int32_t *d_support, void *stream);
+
 /* Canonicality of a DFS code (n_edges tuples {from, to, fromlabel, elabel,
  * tolabel}, either label convention): 1 if minimal, 0 if not, -1 on bad
  * input.  Same semantics as the sequential reference's gSpan::is_min
