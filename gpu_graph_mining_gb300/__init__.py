@@ -30,7 +30,8 @@ STATUS_NAMES = {
 EXPORTS = [
     "gs_last_error", "gs_filetype_from_name", "gs_db_load", "gs_db_from_arrays", "gs_db_generate",
     "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
-    "gs_mine", "gs_mine_ex", "gs_mine_batch", "gs_support_count", "gs_support_count_noalloc",
+    "gs_mine", "gs_mine_ex", "gs_mine_collect", "gs_patterns_free", "gs_mine_batch", "gs_support_count",
+    "gs_support_count_noalloc",
     "gs_dfs_code_is_min", "gs_engine_reset", "gs_engine_set_pool_bytes",
 ]
 
@@ -64,6 +65,12 @@ class DbInfo(ctypes.Structure):
     _fields_ = [("graphs", ctypes.c_int64), ("vertices", ctypes.c_int64),
                 ("adjacency_entries", ctypes.c_int64), ("vertex_labels", ctypes.c_int32),
                 ("edge_labels", ctypes.c_int32), ("device_bytes", ctypes.c_int64)]
+
+
+class Patterns(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int64), ("n_tuples", ctypes.c_int64),
+                ("offset", ctypes.POINTER(ctypes.c_int64)), ("dfs", ctypes.POINTER(ctypes.c_int32)),
+                ("support", ctypes.POINTER(ctypes.c_int64))]
 
 
 EMIT_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p)
@@ -108,6 +115,11 @@ def lib():
     L.gs_mine.restype = i32
     L.gs_mine_ex.argtypes = [vp, i32, ctypes.POINTER(MineOpts), EMIT_FN, vp, ctypes.POINTER(MineStats)]
     L.gs_mine_ex.restype = i32
+    L.gs_mine_collect.argtypes = [vp, i32, ctypes.POINTER(MineOpts), ctypes.POINTER(ctypes.POINTER(Patterns)),
+                                  ctypes.POINTER(MineStats)]
+    L.gs_mine_collect.restype = i32
+    L.gs_patterns_free.argtypes = [ctypes.POINTER(Patterns)]
+    L.gs_patterns_free.restype = None
     L.gs_mine_batch.argtypes = [ctypes.POINTER(vp), i32, pi32, ctypes.POINTER(MineOpts), BATCH_EMIT_FN, vp,
                                 ctypes.POINTER(MineStats)]
     L.gs_mine_batch.restype = i32
@@ -259,6 +271,32 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()
+
+
+def mine_collect(db, minsup, decode=True, **kw):
+    """Bulk form (gs_mine_collect): all patterns land in one native host buffer.
+
+    Returns (patterns, stats); with decode=False the buffer is freed without
+    converting it to Python objects and patterns is its pattern count.
+    """
+    o = _opts(**kw)
+    st = MineStats()
+    p = ctypes.POINTER(Patterns)()
+    _check(lib().gs_mine_collect(db.handle, int(minsup), ctypes.byref(o), ctypes.byref(p), ctypes.byref(st)))
+    try:
+        P = p.contents
+        if not decode:
+            return P.count, st.as_dict()
+        import numpy as np
+        off = np.ctypeslib.as_array(P.offset, shape=(P.count + 1,)).copy() if P.count else np.zeros(1, np.int64)
+        dfs = (np.ctypeslib.as_array(P.dfs, shape=(5 * P.n_tuples,)).reshape(-1, 5).copy()
+               if P.n_tuples else np.zeros((0, 5), np.int32))
+        sup = np.ctypeslib.as_array(P.support, shape=(P.count,)).copy() if P.count else np.zeros(0, np.int64)
+        out = [(tuple(tuple(int(x) for x in row) for row in dfs[off[i]:off[i + 1]]), int(sup[i]))
+               for i in range(P.count)]
+        return out, st.as_dict()
+    finally:
+        lib().gs_patterns_free(p)
 
 
 def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True):

@@ -802,7 +802,7 @@ private:
     int32_t *hv = carve<int32_t>(hb, off, tot_cols);
     int32_t *hl = carve<int32_t>(hb, off, tot_cols);
     const size_t desc_bytes = off;
-    int32_t co = 0, so = 0;
+    int32_t co = 0, so = 0, kmax = 1;
     int64_t rb = 0, bb = 0;
     int32_t kb = 0;
     for(int32_t n = 0; n < W; n++) {
@@ -836,6 +836,7 @@ private:
       }
       co += d.k;
       so += d.nslot;
+      kmax = std::max(kmax, d.k);
       rb += p.nrows;
       bb += (int64_t)d.nkeys * d.words;
       kb += d.nkeys;
@@ -855,7 +856,7 @@ private:
     CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
     CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
     CK(cudaEventRecord(E.ev[0], E.stream));
-    launch_wave_count(dn, W, rows, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
+    launch_wave_count(dn, W, rows, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
                       E.stream);
     CK(cudaEventRecord(E.ev[1], E.stream));
     launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
@@ -970,7 +971,7 @@ private:
       h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
       CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(E.ev[4], E.stream));
-      launch_wave_materialize(dn, W, rows, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
+      launch_wave_materialize(dn, W, rows, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
                               E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
       CK(cudaEventRecord(E.ev[5], E.stream));
       st_.launches++;

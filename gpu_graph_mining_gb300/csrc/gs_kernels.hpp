@@ -22,15 +22,19 @@ void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uin
                              int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
                              unsigned int *err, cudaStream_t s);
 
-// Wave level: one thread per embedding row of every node of the wave.
-// collen[] parallels coltab[]: the length of every column.
-void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
-                       const int32_t *collen, const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs,
-                       uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err, cudaStream_t s);
-void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_rows, const int2 *const *coltab,
-                             const int32_t *collen, const SlotDesc *slots, const int32_t *vtab, const DevDB *dbs,
-                             const uint32_t *bm, const int32_t *bmx, const int32_t *childmap, int32_t *cursor,
-                             const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s);
+// Wave level (gs_wave.cu): a warp per 32 embedding rows of the wave's nodes.
+// kmax = the largest column count of the wave's nodes (selects the instance
+// sized for 8/16/32/64 pattern vertices); collen[] parallels coltab[]: the
+// length of every column.
+void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_rows, int32_t kmax,
+                       const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
+                       const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
+                       cudaStream_t s);
+void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_rows, int32_t kmax,
+                             const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
+                             const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
+                             const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
+                             unsigned long long *bytes, unsigned int *err, cudaStream_t s);
 
 // Extension records given as (key, graph id) pairs: sets bit [key][graph].
 // Keys and graph ids must be in range (checked by the caller).

@@ -161,6 +161,22 @@ GS_API gs_status gs_mine(gs_db *db, int32_t abs_minsup, int32_t max_edges, gs_em
 GS_API gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,
                             gs_mine_stats *stats);
 
+/* Bulk output: all frequent patterns in one host buffer instead of one
+ * output_graph call per pattern (the reference's sink is a virtual call per
+ * pattern, graph_output.cpp:91-96).  Pattern i is the tuples
+ * dfs[5*offset[i] .. 5*offset[i+1]) with support[i], in traversal order.
+ * Free with gs_patterns_free. */
+typedef struct gs_patterns {
+  int64_t count;
+  int64_t n_tuples;
+  const int64_t *offset;  /* [count + 1] */
+  const int32_t *dfs;     /* [5 * n_tuples] {from, to, fromlabel, elabel, tolabel} */
+  const int64_t *support; /* [count] */
+} gs_patterns;
+GS_API gs_status gs_mine_collect(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_patterns **out,
+                                 gs_mine_stats *stats);
+GS_API void gs_patterns_free(gs_patterns *p);
+
 /* Batched form: n databases mined together, their DFS-tree nodes sharing
  * launches.  emit receives the database index first.  No counterpart in the
  * reference (it mines one database per process). */

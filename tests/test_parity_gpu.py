@@ -102,6 +102,15 @@ def test_batch_equals_solo(gs):
     assert stats["patterns"] == sum(len(b) for b in batch)
 
 
+def test_bulk_output_equals_callbacks(gs):
+    db = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    cb, _ = gs.mine(db, 10, label_style=gs.LABELS_SEQ)
+    bulk, stats = gs.mine_collect(db, 10, label_style=gs.LABELS_SEQ)
+    assert bulk == cb
+    n, _ = gs.mine_collect(db, 10, decode=False)
+    assert n == len(cb) == stats["patterns"]
+
+
 def test_repeat_is_deterministic(gs):
     db = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
     a, _ = gs.mine(db, 10)
