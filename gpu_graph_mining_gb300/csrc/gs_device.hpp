@@ -37,6 +37,7 @@ struct DevDB {
 // Per DFS-tree node of a wave (a batch of nodes extended together).
 struct NodeDesc {
   long long row_begin;   // first row in the wave's concatenated row space
+  long long tile_begin;  // first 32-row warp tile of the node (tiles never span two nodes)
   long long bm_base;     // first support-bitmap word of the node's key 0
   const int32_t *gord;   // [nrows]
   int32_t nrows;

@@ -803,7 +803,7 @@ private:
     int32_t *hl = carve<int32_t>(hb, off, tot_cols);
     const size_t desc_bytes = off;
     int32_t co = 0, so = 0, kmax = 1;
-    int64_t rb = 0, bb = 0;
+    int64_t rb = 0, bb = 0, tb = 0;
     int32_t kb = 0;
     for(int32_t n = 0; n < W; n++) {
       const PNode &p = nodes[n];
@@ -812,6 +812,7 @@ private:
       NodeDesc &d = hn[n];
       d = NodeDesc{};
       d.row_begin = rb;
+      d.tile_begin = tb;
       d.bm_base = bb;
       d.gord = p.gord;
       d.nrows = (int32_t)p.nrows;
@@ -838,6 +839,7 @@ private:
       so += d.nslot;
       kmax = std::max(kmax, d.k);
       rb += p.nrows;
+      tb += (p.nrows + 31) / 32;
       bb += (int64_t)d.nkeys * d.words;
       kb += d.nkeys;
     }
@@ -856,7 +858,7 @@ private:
     CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
     CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
     CK(cudaEventRecord(E.ev[0], E.stream));
-    launch_wave_count(dn, W, rows, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
+    launch_wave_count(dn, W, tb, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
                       E.stream);
     CK(cudaEventRecord(E.ev[1], E.stream));
     launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
@@ -971,7 +973,7 @@ private:
       h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
       CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(E.ev[4], E.stream));
-      launch_wave_materialize(dn, W, rows, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
+      launch_wave_materialize(dn, W, tb, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
                               E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
       CK(cudaEventRecord(E.ev[5], E.stream));
       st_.launches++;

@@ -6,9 +6,10 @@
 //   forward   get_forward_pure   src/globals/graph_types.cpp:337-357
 //             get_forward_rmpath src/globals/graph_types.cpp:305-322
 //
-// Work layout.  A warp owns a tile of 32 consecutive embedding rows (lane l =
-// row tile+l, rows of any node of the wave).  Phase 1, per lane: find the
-// row's node, walk the back-links column by column (one 8-byte load per
+// Work layout.  A warp owns a tile of 32 consecutive embedding rows of one
+// node (tiles never span nodes, so the node's descriptor, database and
+// right-most-path slots are loaded once per tile).  Phase 1, per lane: walk
+// the back-links column by column (one 8-byte load per
 // column, into shared memory laid out [vertex][lane] so that a warp reads a
 // column without bank conflicts), and record for every right-most-path vertex
 // the start of its adjacency and the running degree sum.  Phase 2, per warp:
@@ -37,7 +38,7 @@ constexpr unsigned kFull = 0xffffffffu;
 struct WaveArgs {
   const NodeDesc *nodes;
   int nnodes;
-  long long total_rows;
+  long long total_tiles;  // sum over nodes of ceil(rows / 32)
   const int2 *const *coltab;
   const int32_t *collen;
   const SlotDesc *slots;
@@ -57,6 +58,8 @@ template <int KMAX> struct Smem {
   int phi[KMAX][32];        // graph vertex of pattern vertex t for lane l
   int start[KMAX][32];      // adjacency start of right-most-path slot s
   int pre[KMAX + 1][32];    // degree prefix over slots
+  SlotDesc slot[KMAX];      // the tile's node: right-most-path slots
+  int vtab[KMAX];           // the tile's node: pattern vertex -> backward slot
 };
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -72,66 +75,75 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Smem<KMAX> &S = reinterpret_cast<Smem<KMAX> *>(smem_raw)[warp];
-  const long long tiles = (a.total_rows + 31) >> 5;
   const long long gwarp = (long long)blockIdx.x * kWarps + warp;
   const long long nwarps = (long long)gridDim.x * kWarps;
   unsigned long long mine = 0;
 
-  for(long long tile = gwarp; tile < tiles; tile += nwarps) {
-    const long long r = tile * 32 + lane;
-    // ---- phase 1: this lane's row
+  for(long long tile = gwarp; tile < a.total_tiles; tile += nwarps) {
+    // ---- the tile's node (warp-uniform: tiles never span nodes)
     int n = 0;
     if(lane == 0) {
       int lo = 0, hi = a.nnodes - 1;
       while(lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if(a.nodes[mid].row_begin <= tile * 32) lo = mid; else hi = mid - 1;
+        if(a.nodes[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
       }
       n = lo;
     }
     n = __shfl_sync(kFull, n, 0);
-    bool valid = r < a.total_rows;
-    if(valid)
-      while(n + 1 < a.nnodes && a.nodes[n + 1].row_begin <= r) n++;
-    int W = 0, g = 0, i = 0, last_prev = 0;
+    const NodeDesc &nd = a.nodes[n];
+    const int k = nd.k, nslot = nd.nslot, minlabel = nd.minlabel, words = nd.words, key_base = nd.key_base;
+    const long long bm_base = nd.bm_base;
+    const DevDB &dbr = a.dbs[nd.db];
+    const unsigned long long *__restrict__ adj = dbr.adj;
+    const int32_t *__restrict__ adj_off = dbr.adj_off;
+    const int32_t *__restrict__ pair_idx = dbr.pair_idx;
+    const int EL = dbr.EL, VL = dbr.VL, nv = dbr.n_vertices;
+    if(k > KMAX || nslot > KMAX || k < 1 || nslot < 1) {
+      if(lane == 0) atomicOr(a.err, 2u);
+      continue;
+    }
+    if(lane < nslot) S.slot[lane] = a.slots[nd.slot_off + lane];
+    if(lane < k) S.vtab[lane] = a.vtab[nd.vtab_off + lane];
+    // ---- phase 1: this lane's row
+    const int i = (int)((tile - nd.tile_begin) * 32) + lane;
+    bool valid = i < nd.nrows;
+    int W = 0, g = 0, last_prev = 0;
+    __syncwarp();
     if(valid) {
-      const NodeDesc &nd = a.nodes[n];
-      i = (int)(r - nd.row_begin);
       g = nd.gord[i];
-      if((unsigned)g >= (unsigned)nd.words * 32u || nd.k > KMAX || nd.nslot > KMAX) {
+      if((unsigned)g >= (unsigned)words * 32u) {
         atomicOr(a.err, 1u);
         valid = false;
       }
-      if(valid) {
-        const int2 *const *cols = a.coltab + nd.col_off;
-        const int32_t *clen = a.collen + nd.col_off;
-        const DevDB &db = a.dbs[nd.db];
-        int idx = i;
-        for(int c = nd.k - 1; c >= 0; --c) {
-          if((unsigned)idx >= (unsigned)clen[c]) { valid = false; break; }
-          const int2 e = __ldg(&cols[c][idx]);
-          if((unsigned)e.x >= (unsigned)db.n_vertices) { valid = false; break; }
-          S.phi[c][lane] = e.x;
-          if(c == nd.k - 1) last_prev = e.y;
-          idx = e.y;
-        }
-        if(!valid) atomicOr(a.err, 2u);
-        if(valid) {
-          const SlotDesc *sl = a.slots + nd.slot_off;
-          for(int s = 0; s < nd.nslot; ++s) {
-            const int v = S.phi[sl[s].vertex][lane];
-            const int a0 = __ldg(&db.adj_off[v]), a1 = __ldg(&db.adj_off[v + 1]);
-            S.start[s][lane] = a0;
-            S.pre[s][lane] = W;
-            W += a1 - a0;
-          }
-          S.pre[nd.nslot][lane] = W;
-          mine += 8ull * nd.k + 4 + 8ull * nd.nslot;
-        }
+    }
+    if(valid) {
+      const int2 *const *cols = a.coltab + nd.col_off;
+      const int32_t *clen = a.collen + nd.col_off;
+      int idx = i;
+      for(int c = k - 1; c >= 0; --c) {
+        if((unsigned)idx >= (unsigned)clen[c]) { valid = false; break; }
+        const int2 e = __ldg(&cols[c][idx]);
+        if((unsigned)e.x >= (unsigned)nv) { valid = false; break; }
+        S.phi[c][lane] = e.x;
+        if(c == k - 1) last_prev = e.y;
+        idx = e.y;
       }
+      if(!valid) atomicOr(a.err, 2u);
+    }
+    if(valid) {
+      for(int s = 0; s < nslot; ++s) {
+        const int v = S.phi[S.slot[s].vertex][lane];
+        const int a0 = __ldg(&adj_off[v]), a1 = __ldg(&adj_off[v + 1]);
+        S.start[s][lane] = a0;
+        S.pre[s][lane] = W;
+        W += a1 - a0;
+      }
+      S.pre[nslot][lane] = W;
+      mine += 8ull * k + 4 + 8ull * nslot;
     }
     __syncwarp();
-    // ---- phase 2: the tile's items, 32 at a time
+    // ---- phase 2: the tile's (row, slot, neighbour) items, 32 at a time
     int incl = W;
     for(int o = 1; o < 32; o <<= 1) {
       const int t = __shfl_up_sync(kFull, incl, o);
@@ -139,6 +151,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
     }
     const int off = incl - W;
     const int T = __shfl_sync(kFull, incl, 31);
+    const int rlab = S.slot[nslot - 1].vlab;
     for(int base = 0; base < T; base += 32) {
       const int j = base + lane;
       const bool has = j < T;
@@ -151,67 +164,57 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         if(oc <= j) o = c;
       }
       const int q = j - __shfl_sync(kFull, off, o);
-      const int n_o = __shfl_sync(kFull, n, o);
       const int g_o = __shfl_sync(kFull, g, o);
-      const int i_o = __shfl_sync(kFull, i, o);
       const int lp_o = __shfl_sync(kFull, last_prev, o);
       int key = -1, w = 0;
       bool bwd = false;
-      const NodeDesc *ndp = a.nodes + n_o;
       if(has) {
-        const NodeDesc &nd = *ndp;
-        const DevDB &db = a.dbs[nd.db];
         int s = 0;
         while(S.pre[s + 1][o] <= q) s++;
         const int e = S.start[s][o] + (q - S.pre[s][o]);
-        const unsigned long long ent = __ldg(&db.adj[e]);
+        const unsigned long long ent = __ldg(&adj[e]);
         w = (int)(unsigned)(ent & 0xffffffffull);
         const unsigned hi = (unsigned)(ent >> 32);
         const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
-        const SlotDesc *sl = a.slots + nd.slot_off;
-        const SlotDesc &sd = sl[s];
-        const bool is_r = (s == nd.nslot - 1);
+        const SlotDesc &sd = S.slot[s];
         mine += 8;
-        if(!is_r) {
+        if(s != nslot - 1) {
           // forward from a right-most-path vertex: label and order rules first
-          if(wl >= nd.minlabel && (sd.fel < el || (sd.fel == el && sd.ftl <= wl))) {
+          if(wl >= minlabel && (sd.fel < el || (sd.fel == el && sd.ftl <= wl))) {
             bool in_emb = false;
-            for(int t = 0; t < nd.k; ++t) in_emb |= (S.phi[t][o] == w);
+            for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
             if(!in_emb) {
-              const int pk = __ldg(&db.pair_idx[((long long)sd.vlab * db.EL + el) * db.VL + wl]);
+              const int pk = __ldg(&pair_idx[((long long)sd.vlab * EL + el) * VL + wl]);
               if(pk < 0) atomicOr(a.err, 2u); else key = sd.fkey_off + pk;
             }
           }
         } else {
           int jv = -1;
-          for(int t = 0; t < nd.k; ++t) if(S.phi[t][o] == w) jv = t;
+          for(int t = 0; t < k; ++t) if(S.phi[t][o] == w) jv = t;
           if(jv >= 0) {
             // backward edge from the right-most vertex to a right-most-path vertex
-            const int bs = a.vtab[nd.vtab_off + jv];
+            const int bs = S.vtab[jv];
             if(bs >= 0) {
-              const SlotDesc &bd = sl[bs];
-              if(bd.bel < el || (bd.bel == el && bd.blab <= sd.vlab)) {
+              const SlotDesc &bd = S.slot[bs];
+              if(bd.bel < el || (bd.bel == el && bd.blab <= rlab)) {
                 key = bd.bkey_off + el;
                 bwd = true;
               }
             }
-          } else if(wl >= nd.minlabel) {
-            const int pk = __ldg(&db.pair_idx[((long long)sd.vlab * db.EL + el) * db.VL + wl]);
+          } else if(wl >= minlabel) {
+            const int pk = __ldg(&pair_idx[((long long)sd.vlab * EL + el) * VL + wl]);
             if(pk < 0) atomicOr(a.err, 2u); else key = sd.fkey_off + pk;
           }
         }
       }
       // ---- emission, warp converged
-      const int key_base = has ? ndp->key_base : 0;
       if(!MAT) {
         if(key >= 0) {
-          const NodeDesc &nd = *ndp;
-          atomicOr(&a.bm[nd.bm_base + (long long)key * nd.words + (g_o >> 5)], 1u << (g_o & 31));
+          atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
           mine += 8;
         }
-        const int gk = key >= 0 ? key_base + key : -1;
-        const unsigned peers = __match_any_sync(kFull, gk);
-        if(gk >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[gk], __popc(peers));
+        const unsigned peers = __match_any_sync(kFull, key);
+        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[key_base + key], __popc(peers));
       } else {
         const int c = key >= 0 ? a.childmap[key_base + key] : -1;
         if(key >= 0) mine += 4;
@@ -221,12 +224,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         if(c >= 0 && lane == leader) pos = atomicAdd(&a.cursor[c], __popc(peers));
         pos = __shfl_sync(kFull, pos, leader) + __popc(peers & lanemask_lt());
         if(c >= 0) {
-          const NodeDesc &nd = *ndp;
-          const long long wi = nd.bm_base + (long long)key * nd.words + (g_o >> 5);
+          const long long wi = bm_base + (long long)key * words + (g_o >> 5);
           const int rank = a.bmx[wi] + __popc(a.bm[wi] & ((1u << (g_o & 31)) - 1u));
           const ChildOut out = a.outs[c];
           if(pos < out.cap) {
-            out.col[pos] = bwd ? make_int2(S.phi[nd.k - 1][o], lp_o) : make_int2(w, i_o);
+            const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
+            out.col[pos] = bwd ? make_int2(S.phi[k - 1][o], lp_o) : make_int2(w, i_o);
             out.gord[pos] = rank;
           } else {
             atomicOr(a.err, 4u);
@@ -251,8 +254,7 @@ template <int KMAX, bool MAT> void launch_k(const WaveArgs &a, cudaStream_t s)
     cudaFuncSetAttribute(k_wave<KMAX, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
-  const long long tiles = (a.total_rows + 31) / 32;
-  long long blocks = (tiles + kWarps - 1) / kWarps;
+  long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
   const long long cap = 152LL * 32;
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
@@ -269,25 +271,25 @@ template <bool MAT> void dispatch(int kmax, const WaveArgs &a, cudaStream_t s)
 
 }  // namespace
 
-void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_rows, int32_t kmax,
+void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                        const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
                        const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
                        cudaStream_t s)
 {
-  if(total_rows <= 0) return;
-  WaveArgs a{ nodes, nnodes, total_rows, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
+  if(total_tiles <= 0) return;
+  WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
               nullptr, nullptr, nullptr, bytes, err };
   dispatch<false>(kmax, a, s);
 }
 
-void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_rows, int32_t kmax,
+void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
                              unsigned long long *bytes, unsigned int *err, cudaStream_t s)
 {
-  if(total_rows <= 0) return;
-  WaveArgs a{ nodes, nnodes, total_rows, coltab, collen, slots, vtab, dbs, const_cast<uint32_t *>(bm), bmx,
+  if(total_tiles <= 0) return;
+  WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, const_cast<uint32_t *>(bm), bmx,
               nullptr, childmap, cursor, outs, bytes, err };
   dispatch<true>(kmax, a, s);
 }
