@@ -55,7 +55,9 @@ class MineStats(ctypes.Structure):
                 ("candidates", ctypes.c_int64), ("count_bytes", ctypes.c_int64), ("mat_bytes", ctypes.c_int64),
                 ("count_ms", ctypes.c_double), ("mat_ms", ctypes.c_double), ("support_ms", ctypes.c_double),
                 ("root_ms", ctypes.c_double), ("host_min_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
-                ("peak_pool_bytes", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+                ("peak_pool_bytes", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
+                ("host_build_ms", ctypes.c_double), ("host_wait_ms", ctypes.c_double),
+                ("host_select_ms", ctypes.c_double), ("host_emit_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -77,6 +77,10 @@ void fill_stats(const gsgb::MineStats &s, gs_mine_stats *o)
   o->peak_pool_bytes = s.peak_pool_bytes;
   o->h2d_bytes = s.h2d_bytes;
   o->d2h_bytes = s.d2h_bytes;
+  o->host_build_ms = s.host_build_ms;
+  o->host_wait_ms = s.host_wait_ms;
+  o->host_select_ms = s.host_select_ms;
+  o->host_emit_ms = s.host_emit_ms;
 }
 
 struct BatchCtx {

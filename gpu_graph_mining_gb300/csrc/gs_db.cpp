@@ -4,15 +4,35 @@
 #include "gs_db.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <unordered_map>
 
 namespace gsgb {
+
+void parallel_ranges(int64_t n, const std::function<void(int64_t, int64_t, int)> &fn, int64_t min_chunk)
+{
+  int T = (int)std::min<unsigned>(32u, std::max(1u, std::thread::hardware_concurrency()));
+  if(n < 2 * min_chunk) T = 1;
+  else T = (int)std::min<int64_t>(T, n / min_chunk);
+  if(T <= 1) {
+    fn(0, n, 0);
+    return;
+  }
+  std::vector<std::thread> th;
+  for(int t = 0; t < T; t++) {
+    const int64_t b = n * t / T, e = n * (t + 1) / T;
+    th.emplace_back([&fn, b, e, t] { fn(b, e, t); });
+  }
+  for(auto &x : th) x.join();
+}
 
 int parse_filetype(const char *name)
 {
@@ -255,31 +275,74 @@ LoadResult db_from_cudabin_arrays(int32_t db_size, int32_t edges_sizes, int32_t 
 {
   if(db_size < 0 || edges_sizes < 0 || maxv < 0) return fail(ST_ERR_FORMAT, "cudabin: negative sizes");
   db = HostDB();
-  db.vbase.push_back(0);
-  db.aoff.push_back(0);
   const int64_t slots = (int64_t)db_size * maxv;
-  for(int64_t g = 0; g < db_size; g++) {
-    int64_t base = g * maxv;
-    int32_t nv = 0;
-    while(nv < maxv && voff[base + nv] != -1) nv++;
-    int64_t gbase = db.vbase.back();
-    for(int32_t v = 0; v < nv; v++) {
-      int64_t nxt = (v + 1 < nv) ? base + v + 1 : (g + 1) * maxv;
-      if(nxt > slots) nxt = slots;
-      int64_t b0 = voff[base + v], b1 = voff[nxt];
-      if(b0 < 0 || b1 < b0 || b1 > edges_sizes) return fail(ST_ERR_FORMAT, "cudabin: bad vertex offsets");
-      db.vlabel.push_back(vlab[base + v]);
-      for(int64_t k = b0; k < b1; k++) {
-        int64_t t = (int64_t)edges[k] - base;
-        if(t < 0 || t >= nv) return fail(ST_ERR_FORMAT, "cudabin: edge leaves its graph");
-        db.adj_to.push_back((int32_t)(gbase + t));
-        db.adj_el.push_back(elab[k]);
+  // pass 1 (parallel over graphs): vertices per graph (valid slots are a
+  // prefix of the graph's slots) and adjacency entries per graph, which end
+  // where the next graph's first slot (or the trailing sentinel) begins
+  std::vector<int64_t> gnv((size_t)db_size + 1, 0), gadj((size_t)db_size + 1, 0);
+  std::atomic<int> bad{ 0 };
+  parallel_ranges(db_size, [&](int64_t g0, int64_t g1, int) {
+    for(int64_t g = g0; g < g1; g++) {
+      const int64_t base = g * maxv;
+      int32_t nv = 0;
+      while(nv < maxv && voff[base + nv] != -1) nv++;
+      gnv[g] = nv;
+      if(nv > 0) {
+        const int64_t nxt = (g + 1) * maxv <= slots ? (g + 1) * maxv : slots;
+        const int64_t b0 = voff[base], e1 = voff[nxt];
+        if(b0 < 0 || e1 < b0 || e1 > edges_sizes) bad = 1;
+        else gadj[g] = e1 - b0;
       }
-      db.aoff.push_back((int64_t)db.adj_to.size());
     }
-    db.vbase.push_back(gbase + nv);
-    db.n_graphs++;
+  });
+  if(bad) return fail(ST_ERR_FORMAT, "cudabin: bad vertex offsets");
+  db.vbase.resize((size_t)db_size + 1);
+  std::vector<int64_t> gpos((size_t)db_size + 1);
+  db.vbase[0] = 0;
+  gpos[0] = 0;
+  for(int64_t g = 0; g < db_size; g++) {
+    db.vbase[g + 1] = db.vbase[g] + gnv[g];
+    gpos[g + 1] = gpos[g] + gadj[g];
   }
+  const int64_t V = db.vbase[db_size], nadj = gpos[db_size];
+  db.vlabel.resize((size_t)V);
+  db.aoff.resize((size_t)V + 1);
+  db.adj_to.resize((size_t)nadj);
+  db.adj_el.resize((size_t)nadj);
+  db.aoff[0] = 0;
+  // pass 2 (parallel over graphs): a vertex's neighbourhood ends at the next
+  // valid slot's offset (graph_database_cuda::get_next_valid_vertex_idx)
+  parallel_ranges(db_size, [&](int64_t g0, int64_t g1, int) {
+    for(int64_t g = g0; g < g1; g++) {
+      const int64_t base = g * maxv, gbase = db.vbase[g];
+      const int32_t nv = (int32_t)(db.vbase[g + 1] - gbase);
+      int64_t pos = gpos[g];
+      for(int32_t v = 0; v < nv; v++) {
+        int64_t nxt = (v + 1 < nv) ? base + v + 1 : (g + 1) * maxv;
+        if(nxt > slots) nxt = slots;
+        const int64_t b0 = voff[base + v], b1 = voff[nxt];
+        if(b0 < 0 || b1 < b0 || b1 > edges_sizes || pos + (b1 - b0) > gpos[g + 1]) {
+          bad = 1;
+          return;
+        }
+        db.vlabel[gbase + v] = vlab[base + v];
+        for(int64_t k = b0; k < b1; k++) {
+          const int64_t t = (int64_t)edges[k] - base;
+          if(t < 0 || t >= nv) {
+            bad = 2;
+            return;
+          }
+          db.adj_to[pos] = (int32_t)(gbase + t);
+          db.adj_el[pos++] = elab[k];
+        }
+        db.aoff[gbase + v + 1] = pos;
+      }
+      if(pos != gpos[g + 1]) bad = 1;
+    }
+  });
+  if(bad == 2) return fail(ST_ERR_FORMAT, "cudabin: edge leaves its graph");
+  if(bad) return fail(ST_ERR_FORMAT, "cudabin: vertex offsets do not tile the edge array");
+  db.n_graphs = db_size;
   return LoadResult();
 }
 
@@ -329,36 +392,95 @@ LoadResult load_database(const char *path, int filetype, HostDB &db)
 
 LoadResult validate_simple(const HostDB &db)
 {
-  std::vector<int32_t> nb;
-  for(int64_t v = 0; v < db.n_vertices(); v++) {
-    nb.assign(db.adj_to.begin() + db.aoff[v], db.adj_to.begin() + db.aoff[v + 1]);
-    for(int32_t w : nb)
-      if(w == v) return fail(ST_ERR_FORMAT, "self loop at global vertex " + std::to_string(v) + " (only simple graphs are supported)");
-    std::sort(nb.begin(), nb.end());
-    for(size_t i = 1; i < nb.size(); i++)
-      if(nb[i] == nb[i - 1]) return fail(ST_ERR_FORMAT, "parallel edges at global vertex " + std::to_string(v) + " (only simple graphs are supported)");
+  // one pass: stamp[w] = the last vertex that listed w as a neighbour, so a
+  // repeat within one vertex's list is a parallel edge (no per-vertex sort)
+  // (parallel over graphs: neighbours never leave their graph, so the stamp
+  // entries a part touches belong to its own graphs)
+  std::vector<int32_t> stamp((size_t)db.n_vertices(), -1);
+  std::atomic<int64_t> first_bad{ INT64_MAX };
+  std::atomic<int> kind{ 0 };
+  parallel_ranges(db.n_graphs, [&](int64_t g0, int64_t g1, int) {
+    for(int64_t v = db.vbase[g0]; v < db.vbase[g1]; v++) {
+      for(int64_t k = db.aoff[v]; k < db.aoff[v + 1]; k++) {
+        const int32_t w = db.adj_to[k];
+        int why = 0;
+        if(w == v) why = 1;
+        else if(w < db.vbase[g0] || w >= db.vbase[g1]) why = 3;
+        else if(stamp[w] == (int32_t)v) why = 2;
+        if(why) {
+          int64_t cur = first_bad.load();
+          while(v < cur && !first_bad.compare_exchange_weak(cur, v)) {}
+          if(first_bad.load() == v) kind = why;
+          return;
+        }
+        stamp[w] = (int32_t)v;
+      }
+    }
+  });
+  if(kind) {
+    const std::string v = std::to_string(first_bad.load());
+    if(kind == 1) return fail(ST_ERR_FORMAT, "self loop at global vertex " + v + " (only simple graphs are supported)");
+    if(kind == 2) return fail(ST_ERR_FORMAT, "parallel edges at global vertex " + v + " (only simple graphs are supported)");
+    return fail(ST_ERR_FORMAT, "neighbour outside its graph at global vertex " + v);
   }
   return LoadResult();
 }
 
+namespace {
+
+// Dense, order-preserving relabelling of one label array: a lookup table
+// over [min, max] when that range is small, else sort + binary search.
+void dense_labels(const std::vector<int32_t> &in, std::vector<int32_t> &out, std::vector<int32_t> &of)
+{
+  out.resize(in.size());
+  of.clear();
+  if(in.empty()) return;
+  std::vector<int32_t> plo(32, INT32_MAX), phi_(32, INT32_MIN);
+  parallel_ranges((int64_t)in.size(), [&](int64_t b, int64_t e, int t) {
+    int32_t l = INT32_MAX, h = INT32_MIN;
+    for(int64_t i = b; i < e; i++) { l = std::min(l, in[i]); h = std::max(h, in[i]); }
+    plo[t] = l;
+    phi_[t] = h;
+  }, 1 << 16);
+  const int32_t lo = *std::min_element(plo.begin(), plo.end()), hi = *std::max_element(phi_.begin(), phi_.end());
+  const int64_t range = (int64_t)hi - lo + 1;
+  if(range <= ((int64_t)1 << 24)) {
+    std::vector<int32_t> map((size_t)range, -1);
+    if(range <= 4096) {
+      // small alphabets: per-part presence, merged
+      std::vector<std::vector<uint8_t>> seen(32);
+      parallel_ranges((int64_t)in.size(), [&](int64_t b, int64_t e, int t) {
+        std::vector<uint8_t> s((size_t)range, 0);
+        for(int64_t i = b; i < e; i++) s[(size_t)((int64_t)in[i] - lo)] = 1;
+        seen[t].swap(s);
+      }, 1 << 16);
+      for(auto &s : seen)
+        for(size_t r = 0; r < s.size(); r++)
+          if(s[r]) map[r] = 0;
+    } else {
+      for(int32_t x : in) map[(size_t)((int64_t)x - lo)] = 0;
+    }
+    int32_t next = 0;
+    for(int64_t r = 0; r < range; r++)
+      if(map[r] == 0) { map[r] = next++; of.push_back((int32_t)(lo + r)); }
+    parallel_ranges((int64_t)in.size(), [&](int64_t b, int64_t e, int) {
+      for(int64_t i = b; i < e; i++) out[i] = map[(size_t)((int64_t)in[i] - lo)];
+    }, 1 << 16);
+  } else {
+    of = in;
+    std::sort(of.begin(), of.end());
+    of.erase(std::unique(of.begin(), of.end()), of.end());
+    for(size_t i = 0; i < in.size(); i++)
+      out[i] = (int32_t)(std::lower_bound(of.begin(), of.end(), in[i]) - of.begin());
+  }
+}
+
+}  // namespace
+
 void compact_labels(const HostDB &db, std::vector<int32_t> &vl, std::vector<int32_t> &el, LabelMap &map)
 {
-  std::vector<int32_t> u(db.vlabel);
-  std::sort(u.begin(), u.end());
-  u.erase(std::unique(u.begin(), u.end()), u.end());
-  map.vlabel_of = u;
-  std::unordered_map<int32_t, int32_t> vm;
-  for(size_t i = 0; i < u.size(); i++) vm[u[i]] = (int32_t)i;
-  vl.resize(db.vlabel.size());
-  for(size_t i = 0; i < db.vlabel.size(); i++) vl[i] = vm[db.vlabel[i]];
-  std::vector<int32_t> e(db.adj_el);
-  std::sort(e.begin(), e.end());
-  e.erase(std::unique(e.begin(), e.end()), e.end());
-  map.elabel_of = e;
-  std::unordered_map<int32_t, int32_t> em;
-  for(size_t i = 0; i < e.size(); i++) em[e[i]] = (int32_t)i;
-  el.resize(db.adj_el.size());
-  for(size_t i = 0; i < db.adj_el.size(); i++) el[i] = em[db.adj_el[i]];
+  dense_labels(db.vlabel, vl, map.vlabel_of);
+  dense_labels(db.adj_el, el, map.elabel_of);
 }
 
 // -------------------------------------------------------------- writers

@@ -2,10 +2,15 @@
 // layer, label compaction, and the CSR arrays the device copy is built from.
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
 namespace gsgb {
+
+// Runs fn(begin, end, part) over [0, n) split into contiguous parts on the
+// host's cores (one part when n < 2 * min_chunk).
+void parallel_ranges(int64_t n, const std::function<void(int64_t, int64_t, int)> &fn, int64_t min_chunk = 4096);
 
 // File types, numbered like dbio::FILE_TYPE (src/globals/dbio.hpp:9).
 enum FileType { FT_TXT = 0, FT_BIN = 1, FT_FSG = 2, FT_CUDABIN = 3 };

@@ -51,10 +51,20 @@ void Database::prepare()
   const int64_t tab = (int64_t)VL * EL * VL;
   if(tab > (int64_t)1 << 28) throw Error(ST_ERR_LIMIT, "label alphabet too large for the dense pair table");
   std::vector<uint8_t> seen((size_t)tab, 0);
-  for(int64_t v = 0; v < host.n_vertices(); v++) {
-    const int64_t a = vl_dense[v];
-    for(int64_t k = host.aoff[v]; k < host.aoff[v + 1]; k++)
-      seen[(size_t)((a * EL + el_dense[k]) * VL + vl_dense[host.adj_to[k]])] = 1;
+  {
+    // per-part presence tables over the vertices, merged
+    std::vector<std::vector<uint8_t>> part(32);
+    parallel_ranges(host.n_vertices(), [&](int64_t v0, int64_t v1, int t) {
+      std::vector<uint8_t> s((size_t)tab, 0);
+      for(int64_t v = v0; v < v1; v++) {
+        const int64_t a = vl_dense[v];
+        for(int64_t k = host.aoff[v]; k < host.aoff[v + 1]; k++)
+          s[(size_t)((a * EL + el_dense[k]) * VL + vl_dense[host.adj_to[k]])] = 1;
+      }
+      part[t].swap(s);
+    }, tab > (1 << 20) ? INT64_MAX / 4 : 1 << 15);
+    for(auto &s : part)
+      for(size_t i = 0; i < s.size(); i++) seen[i] |= s[i];
   }
   pairs.assign(VL, {});
   pair_cnt.assign(VL, 0);
@@ -86,15 +96,21 @@ void Database::upload()
   size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
   size_t total = o_ro + al(sizeof(int32_t) * (VL + 1));
   std::vector<unsigned long long> adj(E2 + 1, 0);
-  for(int64_t k = 0; k < E2; k++) {
-    const uint32_t w = (uint32_t)host.adj_to[k];
-    const uint32_t hi = ((uint32_t)el_dense[k] << 16) | (uint32_t)vl_dense[w];
-    adj[k] = ((unsigned long long)hi << 32) | w;
-  }
+  parallel_ranges(E2, [&](int64_t b, int64_t e, int) {
+    for(int64_t k = b; k < e; k++) {
+      const uint32_t w = (uint32_t)host.adj_to[k];
+      const uint32_t hi = ((uint32_t)el_dense[k] << 16) | (uint32_t)vl_dense[w];
+      adj[k] = ((unsigned long long)hi << 32) | w;
+    }
+  }, 1 << 16);
   std::vector<int32_t> off(V + 1), vg(V + 1, 0), pidx(tab, -1);
-  for(int64_t v = 0; v <= V; v++) off[v] = (int32_t)host.aoff[v];
-  for(int32_t g = 0; g < host.n_graphs; g++)
-    for(int64_t v = host.vbase[g]; v < host.vbase[g + 1]; v++) vg[v] = g;
+  parallel_ranges(V + 1, [&](int64_t b, int64_t e, int) {
+    for(int64_t v = b; v < e; v++) off[v] = (int32_t)host.aoff[v];
+  }, 1 << 16);
+  parallel_ranges(host.n_graphs, [&](int64_t g0, int64_t g1, int) {
+    for(int64_t g = g0; g < g1; g++)
+      for(int64_t v = host.vbase[g]; v < host.vbase[g + 1]; v++) vg[v] = (int32_t)g;
+  });
   for(int32_t a = 0; a < VL; a++)
     for(size_t i = 0; i < pairs[a].size(); i++)
       pidx[((int64_t)a * EL + pairs[a][i].first) * VL + pairs[a][i].second] = (int32_t)i;
@@ -581,6 +597,14 @@ double ms_between(cudaEvent_t a, cudaEvent_t b)
   return ms;
 }
 
+// adds the wall time of a scope to a millisecond counter
+struct ScopeMs {
+  double &acc;
+  std::chrono::steady_clock::time_point t0;
+  explicit ScopeMs(double &a) : acc(a), t0(std::chrono::steady_clock::now()) {}
+  ~ScopeMs() { acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
 class Runner {
 public:
   Runner(Engine &e, std::vector<MineJob> &jobs, const MineOptions &wo, MineStats &st)
@@ -618,7 +642,10 @@ public:
     st_.count_bytes += (int64_t)bytes[0];
     st_.mat_bytes += (int64_t)bytes[1];
     st_.peak_pool_bytes = std::max<int64_t>(st_.peak_pool_bytes, (int64_t)E.pool.peak());
-    for(auto &s : js_) emit(s);
+    {
+      ScopeMs t(st_.host_emit_ms);
+      for(auto &s : js_) emit(s);
+    }
     st_.wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
 
@@ -760,6 +787,8 @@ private:
   // ---- one wave of DFS-tree nodes
   void wave()
   {
+    using clk = std::chrono::steady_clock;
+    const clk::time_point t_begin = clk::now();
     std::vector<PNode> nodes;
     std::vector<NodeLayout> lays;
     int64_t rows = 0, words = 0;
@@ -868,10 +897,15 @@ private:
     E.h_cnt.ensure(std::max(kb, 1));
     d2h(E.h_sup.p, E.d_sup.p, (size_t)kb * 4);
     d2h(E.h_cnt.p, E.d_cnt.p, (size_t)kb * 4);
+    const clk::time_point t_sync = clk::now();
+    st_.host_build_ms += std::chrono::duration<double, std::milli>(t_sync - t_begin).count();
     CK(cudaStreamSynchronize(E.stream));
     CK(cudaGetLastError());
     check_err();
     flush_timing();
+    const clk::time_point t_ready = clk::now();
+    st_.host_wait_ms += std::chrono::duration<double, std::milli>(t_ready - t_sync).count();
+    const double min_before = st_.host_min_ms;
     st_.count_ms += ms_between(E.ev[0], E.ev[1]);
     st_.support_ms += ms_between(E.ev[1], E.ev[2]);
 
@@ -987,6 +1021,8 @@ private:
     }
     for(int32_t n = W - 1; n >= 0; n--)
       for(auto it = made[n].rbegin(); it != made[n].rend(); ++it) stack_.push_back(std::move(*it));
+    st_.host_select_ms += std::chrono::duration<double, std::milli>(clk::now() - t_ready).count() -
+                          (st_.host_min_ms - min_before);
   }
 
   // pre-order traversal of a job's pattern tree, codes in the caller's labels

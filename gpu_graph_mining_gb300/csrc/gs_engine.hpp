@@ -95,6 +95,10 @@ struct MineStats {
   int64_t peak_pool_bytes = 0;
   int64_t h2d_bytes = 0;     // host->device bytes copied (database upload and per-wave tables)
   int64_t d2h_bytes = 0;     // device->host bytes copied (candidate supports and counts)
+  double host_build_ms = 0;  // wave layout and descriptor tables
+  double host_wait_ms = 0;   // blocked on the device (stream synchronisations)
+  double host_select_ms = 0; // candidate decoding, child allocation, child tables
+  double host_emit_ms = 0;   // pattern-tree traversal and output
 };
 
 struct MineJob {

@@ -149,6 +149,10 @@ typedef struct gs_mine_stats {
   int64_t peak_pool_bytes;
   int64_t h2d_bytes;       /* host->device bytes copied (database upload, per-wave tables) */
   int64_t d2h_bytes;       /* device->host bytes copied (candidate supports and counts) */
+  double host_build_ms;    /* host: wave layout and descriptor tables */
+  double host_wait_ms;     /* host: blocked on the device */
+  double host_select_ms;   /* host: candidate decoding and child allocation */
+  double host_emit_ms;     /* host: output */
 } gs_mine_stats;
 
 GS_API void gs_mine_opts_default(gs_mine_opts *opts);
