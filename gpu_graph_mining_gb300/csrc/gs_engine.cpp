@@ -367,10 +367,19 @@ private:
 
 // ------------------------------------------------------------------ engine
 
+// One pool allocation holding the new columns and graph ranks of every child
+// made by one wave (or one root phase); returned to the pool when the last
+// column or rank array carved from it is released.
+struct Block {
+  void *base = nullptr;
+  int32_t refs = 0;
+};
+
 struct Column {
   int2 *ptr = nullptr;
   int64_t n = 0;
   int32_t refs = 0;
+  int32_t blk = -1;
 };
 
 struct PatternRec {
@@ -393,6 +402,7 @@ struct PNode {
   Code code;
   std::vector<int32_t> cols;
   int32_t *gord;
+  int32_t gord_blk;
   int64_t nrows;
   int64_t support;
 };
@@ -422,6 +432,8 @@ struct Engine {
   std::vector<MinChecker> checkers;
   std::vector<Column> cols;
   std::vector<int32_t> free_cols;
+  std::vector<Block> blocks;
+  std::vector<int32_t> free_blocks;
   int64_t pool_limit = 0;
   // device scratch
   DBuf<char> d_desc;
@@ -464,10 +476,31 @@ struct Engine {
     cudaStreamDestroy(stream);
     cols.clear();
     free_cols.clear();
+    blocks.clear();
+    free_blocks.clear();
     workers.reset();
     ready = false;
   }
-  int32_t new_col(int2 *p, int64_t n)
+  // a pool block of `bytes`; starts with no references
+  int32_t new_block(size_t bytes)
+  {
+    int32_t id;
+    if(!free_blocks.empty()) { id = free_blocks.back(); free_blocks.pop_back(); }
+    else { id = (int32_t)blocks.size(); blocks.emplace_back(); }
+    blocks[id].base = pool.alloc(bytes);
+    blocks[id].refs = 0;
+    return id;
+  }
+  void block_ref(int32_t b) { blocks[b].refs++; }
+  void block_unref(int32_t b)
+  {
+    if(--blocks[b].refs == 0) {
+      pool.release(blocks[b].base);
+      blocks[b].base = nullptr;
+      free_blocks.push_back(b);
+    }
+  }
+  int32_t new_col(int2 *p, int64_t n, int32_t blk)
   {
     int32_t id;
     if(!free_cols.empty()) { id = free_cols.back(); free_cols.pop_back(); }
@@ -475,16 +508,31 @@ struct Engine {
     cols[id].ptr = p;
     cols[id].n = n;
     cols[id].refs = 1;
+    cols[id].blk = blk;
+    block_ref(blk);
     return id;
   }
   void ref(int32_t id) { cols[id].refs++; }
   void unref(int32_t id)
   {
     if(--cols[id].refs == 0) {
-      pool.release(cols[id].ptr);
+      block_unref(cols[id].blk);
       cols[id].ptr = nullptr;
       free_cols.push_back(id);
     }
+  }
+};
+
+// Carves consecutive 256-byte-aligned pieces out of one block.
+struct Carver {
+  char *base;
+  size_t off = 0;
+  static size_t round(size_t x) { return (x + 255) & ~(size_t)255; }
+  template <class T> T *take(size_t n)
+  {
+    T *p = (T *)(base + off);
+    off += round(sizeof(T) * n);
+    return p;
   }
 };
 
@@ -730,7 +778,11 @@ private:
     std::vector<PNode> made;
     E.h_childmap.ensure(R);
     for(int32_t i = 0; i < R; i++) E.h_childmap.p[i] = -1;
+    // frequent roots of this job (and partition), in the reference's order
+    struct Sel { int32_t key, pid; DFS d; int32_t sup; int64_t n; };
+    std::vector<Sel> sel;
     int32_t root_index = 0;
+    size_t bytes = 0;
     for(int32_t fl = 0; fl < db.VL; fl++) {
       for(size_t p = 0; p < db.pairs[fl].size(); p++) {
         const int32_t el = db.pairs[fl][p].first, tl = db.pairs[fl][p].second;
@@ -747,20 +799,31 @@ private:
         S.roots.push_back(pid);
         if(!extend) continue;
         const int64_t n = E.h_cnt.p[key];
-        char *blk = (char *)E.pool.alloc((size_t)n * 8);
-        char *blk0 = (char *)E.pool.alloc((size_t)n * 8);
-        int32_t *gord = (int32_t *)E.pool.alloc((size_t)n * 4);
-        ChildOut o{ (int2 *)blk, (int2 *)blk0, gord, 2, (int32_t)n };
-        E.h_childmap.p[key] = (int32_t)outs.size();
+        sel.push_back(Sel{ key, pid, pr.edge, sup, n });
+        bytes += 2 * Carver::round((size_t)n * 8) + Carver::round((size_t)n * 4);
+      }
+    }
+    if(!sel.empty()) {
+      // all root columns and ranks in one pool block
+      const int32_t blk = E.new_block(bytes);
+      Carver cv{ (char *)E.blocks[blk].base };
+      for(const Sel &s : sel) {
+        int2 *c1 = cv.take<int2>(s.n);
+        int2 *c0 = cv.take<int2>(s.n);
+        int32_t *gord = cv.take<int32_t>(s.n);
+        ChildOut o{ c1, c0, gord, 2, (int32_t)s.n };
+        E.h_childmap.p[s.key] = (int32_t)outs.size();
         outs.push_back(o);
         PNode nn;
         nn.job = j;
-        nn.pattern = pid;
-        nn.code = { pr.edge };
-        nn.cols = { E.new_col((int2 *)blk0, n), E.new_col((int2 *)blk, n) };
+        nn.pattern = s.pid;
+        nn.code = { s.d };
+        nn.cols = { E.new_col(c0, s.n, blk), E.new_col(c1, s.n, blk) };
         nn.gord = gord;
-        nn.nrows = n;
-        nn.support = sup;
+        nn.gord_blk = blk;
+        E.block_ref(blk);
+        nn.nrows = s.n;
+        nn.support = s.sup;
         made.push_back(std::move(nn));
       }
     }
@@ -932,7 +995,6 @@ private:
     // canonicality on the host, in parallel
     {
       auto t0 = std::chrono::steady_clock::now();
-      std::vector<Code> dummy;
       E.workers->run((int64_t)cands.size(), [&](int64_t i, int w) {
         Candidate &c = cands[i];
         const Code &code = nodes[c.node].code;
@@ -955,6 +1017,10 @@ private:
       std::vector<std::vector<int32_t>> per(W);
       for(int32_t i = 0; i < (int32_t)cands.size(); i++)
         if(cands[i].ok) per[cands[i].node].push_back(i);
+      // pass 1: output tree (reference order) and which children to materialise
+      struct Mat { int32_t node, cand, pid; };
+      std::vector<Mat> mats;
+      size_t bytes = 0;
       for(int32_t n = 0; n < W; n++) {
         auto &v = per[n];
         std::sort(v.begin(), v.end(), [&](int32_t a, int32_t b) { return seq_before(cands[a].dfs, cands[b].dfs); });
@@ -971,30 +1037,41 @@ private:
           if(max_edges > 0 && child_edges >= max_edges) continue;
           if(child_edges >= kMaxPatternEdges || (c.dfs.is_forward() && c.dfs.to + 1 > 64))
             throw Error(ST_ERR_LIMIT, "pattern exceeds 64 vertices or 127 edges");
+          mats.push_back(Mat{ n, ci, pid });
+          bytes += Carver::round((size_t)c.cnt * 8) + Carver::round((size_t)c.cnt * 4);
+        }
+      }
+      // pass 2: every child's new column and graph ranks carved from one block
+      if(!mats.empty()) {
+        const int32_t blk = E.new_block(bytes);
+        Carver cv{ (char *)E.blocks[blk].base };
+        for(const Mat &m : mats) {
+          const Candidate &c = cands[m.cand];
+          PNode &p = nodes[m.node];
           const int64_t rowsn = c.cnt;
-          int2 *col = (int2 *)E.pool.alloc((size_t)rowsn * 8);
-          int32_t *gord = (int32_t *)E.pool.alloc((size_t)rowsn * 4);
+          int2 *col = cv.take<int2>(rowsn);
+          int32_t *gord = cv.take<int32_t>(rowsn);
           ChildOut o{ col, nullptr, gord, c.dfs.is_forward() ? 0 : 1, (int32_t)rowsn };
-          E.h_childmap.p[hn[n].key_base + c.key] = (int32_t)outs.size();
+          E.h_childmap.p[hn[m.node].key_base + c.key] = (int32_t)outs.size();
           outs.push_back(o);
           PNode nn;
           nn.job = p.job;
-          nn.pattern = pid;
+          nn.pattern = m.pid;
+          nn.code.reserve(p.code.size() + 1);
           nn.code = p.code;
           nn.code.push_back(c.dfs);
-          if(c.dfs.is_forward()) {
-            nn.cols = p.cols;
-            for(int32_t id : p.cols) E.ref(id);
-            nn.cols.push_back(E.new_col(col, rowsn));
-          } else {
-            nn.cols.assign(p.cols.begin(), p.cols.end() - 1);
-            for(int32_t id : nn.cols) E.ref(id);
-            nn.cols.push_back(E.new_col(col, rowsn));
-          }
+          // forward children append a column, backward children replace the last
+          const size_t keep = c.dfs.is_forward() ? p.cols.size() : p.cols.size() - 1;
+          nn.cols.reserve(keep + 1);
+          nn.cols.assign(p.cols.begin(), p.cols.begin() + keep);
+          for(int32_t id : nn.cols) E.ref(id);
+          nn.cols.push_back(E.new_col(col, rowsn, blk));
           nn.gord = gord;
+          nn.gord_blk = blk;
+          E.block_ref(blk);
           nn.nrows = rowsn;
           nn.support = c.support;
-          made[n].push_back(std::move(nn));
+          made[m.node].push_back(std::move(nn));
         }
       }
     }
@@ -1017,7 +1094,7 @@ private:
     // (stream order keeps the materialise kernel ahead of any reuse)
     for(auto &p : nodes) {
       for(int32_t id : p.cols) E.unref(id);
-      E.pool.release(p.gord);
+      E.block_unref(p.gord_blk);
     }
     for(int32_t n = W - 1; n >= 0; n--)
       for(auto it = made[n].rbegin(); it != made[n].rend(); ++it) stack_.push_back(std::move(*it));

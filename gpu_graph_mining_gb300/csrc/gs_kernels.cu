@@ -32,28 +32,103 @@ __device__ __forceinline__ void add_bytes(unsigned long long *bytes, unsigned lo
   if((threadIdx.x & 31) == 0 && mine) atomicAdd(bytes, mine);
 }
 
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Root level, warp-cooperative: a warp owns 32 consecutive vertices, whose
+// adjacency entries form one contiguous range; lanes take consecutive entries
+// (coalesced 8-byte loads) and find their source vertex by a 5-step shuffle
+// search over the lanes' adjacency starts.  The warp stays converged, so the
+// embedding counters and child cursors take one atomic per distinct key.
+template <bool MAT>
+__device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__restrict__ root_off, uint32_t *bm,
+                                           const int32_t *__restrict__ bmx, int32_t *cnt, int32_t words,
+                                           const int32_t *__restrict__ childmap, int32_t *cursor,
+                                           const ChildOut *__restrict__ outs, unsigned long long *bytes,
+                                           unsigned int *err)
+{
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long tiles = ((long long)db.n_vertices + 31) / 32;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  unsigned long long mine = 0;
+  for(long long tile = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < tiles; tile += nwarps) {
+    const long long v = tile * 32 + lane;
+    const bool valid = v < db.n_vertices;
+    const int a0 = valid ? __ldg(&db.adj_off[v]) : 0;
+    const int a1 = valid ? __ldg(&db.adj_off[v + 1]) : 0;
+    const int fl = valid ? __ldg(&db.vlabel[v]) : 0;
+    const int g = valid ? __ldg(&db.vgraph[v]) : 0;
+    const int W = a1 - a0;
+    int incl = W;
+    for(int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(full, incl, o);
+      if(lane >= o) incl += t;
+    }
+    const int off = incl - W;
+    const int T = __shfl_sync(full, incl, 31);
+    if(valid) mine += 16;
+    for(int base = 0; base < T; base += 32) {
+      const int j = base + lane;
+      const bool has = j < T;
+      int o = 0;
+#pragma unroll
+      for(int step = 16; step >= 1; step >>= 1) {
+        const int c = o + step;
+        if(__shfl_sync(full, off, c) <= j) o = c;
+      }
+      const int e = __shfl_sync(full, a0, o) + (j - __shfl_sync(full, off, o));
+      const int fl_o = __shfl_sync(full, fl, o);
+      const int g_o = __shfl_sync(full, g, o);
+      int key = -1, w = 0;
+      if(has) {
+        const unsigned long long ent = __ldg(&db.adj[e]);
+        w = (int)(unsigned)(ent & 0xffffffffull);
+        const unsigned hi = (unsigned)(ent >> 32);
+        const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
+        mine += 8;
+        if(fl_o <= wl) key = root_off[fl_o] + __ldg(&db.pair_idx[((long long)fl_o * db.EL + el) * db.VL + wl]);
+      }
+      if(!MAT) {
+        if(key >= 0) {
+          atomicOr(&bm[(long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
+          mine += 8;
+        }
+        const unsigned peers = __match_any_sync(full, key);
+        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[key], __popc(peers));
+      } else {
+        const int c = key >= 0 ? childmap[key] : -1;
+        const unsigned peers = __match_any_sync(full, c);
+        const int leader = __ffs(peers) - 1;
+        int pos = 0;
+        if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[c], __popc(peers));
+        pos = __shfl_sync(full, pos, leader) + __popc(peers & lanemask_lt());
+        if(c >= 0) {
+          const long long wi = (long long)key * words + (g_o >> 5);
+          const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (g_o & 31)) - 1u));
+          const ChildOut out = outs[c];
+          if(pos < out.cap) {
+            out.col0[pos] = make_int2((int)(tile * 32 + o), -1);
+            out.col[pos] = make_int2(w, pos);
+            out.gord[pos] = rank;
+          } else {
+            atomicOr(err, 4u);
+          }
+        }
+      }
+    }
+  }
+  if(!MAT) add_bytes(bytes, mine);
+}
+
 __global__ void __launch_bounds__(kBlock) k_root_count(DevDB db, const int32_t *__restrict__ root_off, uint32_t *bm,
                                                         int32_t *cnt, int32_t words, unsigned long long *bytes)
 {
-  unsigned long long mine = 0;
-  const int stride = gridDim.x * blockDim.x;
-  for(int v = blockIdx.x * blockDim.x + threadIdx.x; v < db.n_vertices; v += stride) {
-    const int fl = db.vlabel[v];
-    const int g = db.vgraph[v];
-    const int a0 = db.adj_off[v], a1 = db.adj_off[v + 1];
-    mine += 16u + 8u * (unsigned)(a1 - a0);
-    for(int e = a0; e < a1; ++e) {
-      const unsigned long long a = __ldg(&db.adj[e]);
-      const unsigned hi = (unsigned)(a >> 32);
-      const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
-      if(fl > wl) continue;
-      const int key = root_off[fl] + __ldg(&db.pair_idx[((long long)fl * db.EL + el) * db.VL + wl]);
-      atomicOr(&bm[(long long)key * words + (g >> 5)], 1u << (g & 31));
-      atomicAdd(&cnt[key], 1);
-      mine += 8u;
-    }
-  }
-  add_bytes(bytes, mine);
+  root_tiles<false>(db, root_off, bm, nullptr, cnt, words, nullptr, nullptr, nullptr, bytes, nullptr);
 }
 
 __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int32_t *__restrict__ root_off,
@@ -62,33 +137,8 @@ __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int
                                                               const int32_t *__restrict__ childmap, int32_t *cursor,
                                                               const ChildOut *__restrict__ outs, unsigned int *err)
 {
-  const int stride = gridDim.x * blockDim.x;
-  for(int v = blockIdx.x * blockDim.x + threadIdx.x; v < db.n_vertices; v += stride) {
-    const int fl = db.vlabel[v];
-    const int g = db.vgraph[v];
-    const int a0 = db.adj_off[v], a1 = db.adj_off[v + 1];
-    for(int e = a0; e < a1; ++e) {
-      const unsigned long long a = __ldg(&db.adj[e]);
-      const int w = (int)(unsigned)(a & 0xffffffffull);
-      const unsigned hi = (unsigned)(a >> 32);
-      const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
-      if(fl > wl) continue;
-      const int key = root_off[fl] + __ldg(&db.pair_idx[((long long)fl * db.EL + el) * db.VL + wl]);
-      const int c = childmap[key];
-      if(c < 0) continue;
-      const long long wi = (long long)key * words + (g >> 5);
-      const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (g & 31)) - 1u));
-      const int pos = atomicAdd(&cursor[c], 1);
-      const ChildOut o = outs[c];
-      if(pos >= o.cap) {
-        atomicOr(err, 4u);
-        continue;
-      }
-      o.col0[pos] = make_int2(v, -1);
-      o.col[pos] = make_int2(w, pos);
-      o.gord[pos] = rank;
-    }
-  }
+  root_tiles<true>(db, root_off, const_cast<uint32_t *>(bm), bmx, nullptr, words, childmap, cursor, outs, nullptr,
+                   err);
 }
 
 __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__ nodes, int nnodes, int total_keys,
@@ -140,7 +190,7 @@ inline int grid_for(long long n)
 void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
                        unsigned long long *bytes, cudaStream_t s)
 {
-  k_root_count<<<grid_for(db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, cnt, words, bytes);
+  k_root_count<<<grid_for((long long)db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, cnt, words, bytes);
 }
 
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
