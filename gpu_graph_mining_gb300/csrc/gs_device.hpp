@@ -28,10 +28,13 @@ struct DevDB {
   const int32_t *adj_off;
   const int32_t *vlabel;
   const int32_t *vgraph;
+  const int32_t *vbase;     // [G+1] first global vertex of each graph
   const int32_t *pair_idx;
   int32_t VL, EL;
   int32_t n_graphs;
   int32_t n_vertices;
+  int32_t max_graph_vertices;
+  int32_t pad;
 };
 
 // Per DFS-tree node of a wave (a batch of nodes extended together).

@@ -94,7 +94,8 @@ void Database::upload()
   size_t o_vg = o_vl + al(sizeof(int32_t) * (V + 1));
   size_t o_pi = o_vg + al(sizeof(int32_t) * (V + 1));
   size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
-  size_t total = o_ro + al(sizeof(int32_t) * (VL + 1));
+  size_t o_vb = o_ro + al(sizeof(int32_t) * (VL + 1));
+  size_t total = o_vb + al(sizeof(int32_t) * (host.n_graphs + 1));
   std::vector<unsigned long long> adj(E2 + 1, 0);
   parallel_ranges(E2, [&](int64_t b, int64_t e, int) {
     for(int64_t k = b; k < e; k++) {
@@ -114,6 +115,10 @@ void Database::upload()
   for(int32_t a = 0; a < VL; a++)
     for(size_t i = 0; i < pairs[a].size(); i++)
       pidx[((int64_t)a * EL + pairs[a][i].first) * VL + pairs[a][i].second] = (int32_t)i;
+  std::vector<int32_t> vb(host.n_graphs + 1);
+  int32_t maxnv = 0;
+  for(int32_t g = 0; g <= host.n_graphs; g++) vb[g] = (int32_t)host.vbase[g];
+  for(int32_t g = 0; g < host.n_graphs; g++) maxnv = std::max(maxnv, host.graph_nv(g));
   CK(cudaMalloc(&d_block, total));
   d_bytes = total;
   char *b = (char *)d_block;
@@ -123,11 +128,14 @@ void Database::upload()
   CK(cudaMemcpy(b + o_vg, vg.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_pi, pidx.data(), sizeof(int32_t) * tab, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_ro, root_off.data(), sizeof(int32_t) * VL, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_vb, vb.data(), sizeof(int32_t) * (host.n_graphs + 1), cudaMemcpyHostToDevice));
   dev.adj = (const unsigned long long *)(b + o_adj);
   dev.adj_off = (const int32_t *)(b + o_off);
   dev.vlabel = (const int32_t *)(b + o_vl);
   dev.vgraph = (const int32_t *)(b + o_vg);
   dev.pair_idx = (const int32_t *)(b + o_pi);
+  dev.vbase = (const int32_t *)(b + o_vb);
+  dev.max_graph_vertices = maxnv;
   dev.VL = VL;
   dev.EL = EL;
   dev.n_graphs = host.n_graphs;
@@ -895,6 +903,7 @@ private:
     int32_t *hl = carve<int32_t>(hb, off, tot_cols);
     const size_t desc_bytes = off;
     int32_t co = 0, so = 0, kmax = 1;
+    bool small = true;  // every database of the wave has graphs of <= 64 vertices
     int64_t rb = 0, bb = 0, tb = 0;
     int32_t kb = 0;
     for(int32_t n = 0; n < W; n++) {
@@ -930,6 +939,7 @@ private:
       co += d.k;
       so += d.nslot;
       kmax = std::max(kmax, d.k);
+      small = small && db.dev.max_graph_vertices <= 64;
       rb += p.nrows;
       tb += (p.nrows + 31) / 32;
       bb += (int64_t)d.nkeys * d.words;
@@ -950,7 +960,7 @@ private:
     CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
     CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
     CK(cudaEventRecord(E.ev[0], E.stream));
-    launch_wave_count(dn, W, tb, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
+    launch_wave_count(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
                       E.stream);
     CK(cudaEventRecord(E.ev[1], E.stream));
     launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
@@ -1084,7 +1094,7 @@ private:
       h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
       CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(E.ev[4], E.stream));
-      launch_wave_materialize(dn, W, tb, kmax, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
+      launch_wave_materialize(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
                               E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
       CK(cudaEventRecord(E.ev[5], E.stream));
       st_.launches++;

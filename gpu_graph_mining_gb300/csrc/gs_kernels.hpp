@@ -26,11 +26,13 @@ void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uin
 // kmax = the largest column count of the wave's nodes (selects the instance
 // sized for 8/16/32/64 pattern vertices); collen[] parallels coltab[]: the
 // length of every column.
-void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
+// small_graphs: every graph of the wave's databases has <= 64 vertices.
+void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax, bool small_graphs,
                        const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
                        const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
                        cudaStream_t s);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
+                             bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,

@@ -55,6 +55,8 @@ struct WaveArgs {
 };
 
 template <int KMAX> struct Smem {
+  unsigned long long mask[32];  // small graphs: the row's graph-local vertex ids as a bit set
+  int gb[32];                   // small graphs: first global vertex of the row's graph
   int phi[KMAX][32];        // graph vertex of pattern vertex t for lane l
   int start[KMAX][32];      // adjacency start of right-most-path slot s
   int pre[KMAX + 1][32];    // degree prefix over slots
@@ -69,7 +71,10 @@ __device__ __forceinline__ unsigned lanemask_lt()
   return m;
 }
 
-template <int KMAX, bool MAT>
+// MASK: every graph of the wave's databases has at most 64 vertices, so
+// "is w already in the embedding" is one bit test of the row's vertex set
+// instead of a loop over its k vertices.
+template <int KMAX, bool MAT, bool MASK>
 __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -99,6 +104,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
     const int32_t *__restrict__ adj_off = dbr.adj_off;
     const int32_t *__restrict__ pair_idx = dbr.pair_idx;
     const int EL = dbr.EL, VL = dbr.VL, nv = dbr.n_vertices;
+    const int32_t *__restrict__ vbase = dbr.vbase;
+    const int32_t *__restrict__ vgraph = dbr.vgraph;
     if(k > KMAX || nslot > KMAX || k < 1 || nslot < 1) {
       if(lane == 0) atomicOr(a.err, 2u);
       continue;
@@ -131,6 +138,18 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
       }
       if(!valid) atomicOr(a.err, 2u);
     }
+    if(MASK && valid) {
+      const int gb = __ldg(&vbase[__ldg(&vgraph[S.phi[0][lane]])]);
+      unsigned long long m = 0;
+      for(int c = 0; c < k; ++c) {
+        const unsigned lv = (unsigned)(S.phi[c][lane] - gb);
+        if(lv >= 64u) { valid = false; break; }
+        m |= 1ull << lv;
+      }
+      if(!valid) atomicOr(a.err, 2u);
+      S.mask[lane] = m;
+      S.gb[lane] = gb;
+    }
     if(valid) {
       for(int s = 0; s < nslot; ++s) {
         const int v = S.phi[S.slot[s].vertex][lane];
@@ -140,7 +159,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         W += a1 - a0;
       }
       S.pre[nslot][lane] = W;
-      mine += 8ull * k + 4 + 8ull * nslot;
+      mine += 8ull * k + 4 + 8ull * nslot + (MASK ? 8 : 0);
     }
     __syncwarp();
     // ---- phase 2: the tile's (row, slot, neighbour) items, 32 at a time
@@ -152,6 +171,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
     const int off = incl - W;
     const int T = __shfl_sync(kFull, incl, 31);
     const int rlab = S.slot[nslot - 1].vlab;
+    if(lane == 0) mine += 8ull * T;  // one packed adjacency entry per item
     for(int base = 0; base < T; base += 32) {
       const int j = base + lane;
       const bool has = j < T;
@@ -177,12 +197,16 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         const unsigned hi = (unsigned)(ent >> 32);
         const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
         const SlotDesc &sd = S.slot[s];
-        mine += 8;
+        bool in_emb = false;
+        if(MASK) {
+          const unsigned lv = (unsigned)(w - S.gb[o]);
+          in_emb = lv < 64u && ((S.mask[o] >> lv) & 1ull);
+        }
         if(s != nslot - 1) {
           // forward from a right-most-path vertex: label and order rules first
           if(wl >= minlabel && (sd.fel < el || (sd.fel == el && sd.ftl <= wl))) {
-            bool in_emb = false;
-            for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
+            if(!MASK)
+              for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
             if(!in_emb) {
               const int pk = __ldg(&pair_idx[((long long)sd.vlab * EL + el) * VL + wl]);
               if(pk < 0) atomicOr(a.err, 2u); else key = sd.fkey_off + pk;
@@ -190,7 +214,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
           }
         } else {
           int jv = -1;
-          for(int t = 0; t < k; ++t) if(S.phi[t][o] == w) jv = t;
+          if(!MASK || in_emb)
+            for(int t = 0; t < k; ++t) if(S.phi[t][o] == w) jv = t;
           if(jv >= 0) {
             // backward edge from the right-most vertex to a right-most-path vertex
             const int bs = S.vtab[jv];
@@ -209,15 +234,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
       }
       // ---- emission, warp converged
       if(!MAT) {
-        if(key >= 0) {
-          atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
-          mine += 8;
-        }
+        if(key >= 0) atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
+        if(lane == 0) mine += 8ull * __popc(__ballot_sync(kFull, key >= 0));
         const unsigned peers = __match_any_sync(kFull, key);
         if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[key_base + key], __popc(peers));
       } else {
         const int c = key >= 0 ? a.childmap[key_base + key] : -1;
-        if(key >= 0) mine += 4;
+        const unsigned ext = __ballot_sync(kFull, key >= 0), sel = __ballot_sync(kFull, c >= 0);
+        if(lane == 0) mine += 4ull * __popc(ext) + 20ull * __popc(sel);
         const unsigned peers = __match_any_sync(kFull, c);
         const int leader = __ffs(peers) - 1;
         int pos = 0;
@@ -234,7 +258,6 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
           } else {
             atomicOr(a.err, 4u);
           }
-          mine += 20;
         }
       }
     }
@@ -246,32 +269,38 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
   }
 }
 
-template <int KMAX, bool MAT> void launch_k(const WaveArgs &a, cudaStream_t s)
+template <int KMAX, bool MAT, bool MASK> void launch_k(const WaveArgs &a, cudaStream_t s)
 {
   const size_t smem = sizeof(Smem<KMAX>) * kWarps;
   static bool configured = false;
   if(!configured) {
-    cudaFuncSetAttribute(k_wave<KMAX, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_wave<KMAX, MAT, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
   const long long cap = 152LL * 32;
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
-  k_wave<KMAX, MAT><<<(int)blocks, kWarps * 32, smem, s>>>(a);
+  k_wave<KMAX, MAT, MASK><<<(int)blocks, kWarps * 32, smem, s>>>(a);
 }
 
-template <bool MAT> void dispatch(int kmax, const WaveArgs &a, cudaStream_t s)
+template <bool MAT, bool MASK> void dispatch_k(int kmax, const WaveArgs &a, cudaStream_t s)
 {
-  if(kmax <= 8) launch_k<8, MAT>(a, s);
-  else if(kmax <= 16) launch_k<16, MAT>(a, s);
-  else if(kmax <= 32) launch_k<32, MAT>(a, s);
-  else launch_k<64, MAT>(a, s);
+  if(kmax <= 8) launch_k<8, MAT, MASK>(a, s);
+  else if(kmax <= 16) launch_k<16, MAT, MASK>(a, s);
+  else if(kmax <= 32) launch_k<32, MAT, MASK>(a, s);
+  else launch_k<64, MAT, MASK>(a, s);
+}
+
+template <bool MAT> void dispatch(int kmax, bool small_graphs, const WaveArgs &a, cudaStream_t s)
+{
+  if(small_graphs) dispatch_k<MAT, true>(kmax, a, s);
+  else dispatch_k<MAT, false>(kmax, a, s);
 }
 
 }  // namespace
 
-void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
+void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax, bool small_graphs,
                        const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
                        const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
                        cudaStream_t s)
@@ -279,10 +308,11 @@ void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_ti
   if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
               nullptr, nullptr, nullptr, bytes, err };
-  dispatch<false>(kmax, a, s);
+  dispatch<false>(kmax, small_graphs, a, s);
 }
 
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
+                             bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
@@ -291,7 +321,7 @@ void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long to
   if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, const_cast<uint32_t *>(bm), bmx,
               nullptr, childmap, cursor, outs, bytes, err };
-  dispatch<true>(kmax, a, s);
+  dispatch<true>(kmax, small_graphs, a, s);
 }
 
 }  // namespace gsgb

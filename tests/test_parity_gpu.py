@@ -74,6 +74,34 @@ def test_generated_vs_oracle(gs, oracle, tmp_path, config, scale, minsups):
         assert got == want, (config, s)
 
 
+@pytest.mark.parametrize("nv_range", [(60, 64), (60, 130)])
+def test_large_graphs_vs_oracle(gs, oracle, tmp_path, nv_range):
+    # graphs around and beyond 64 vertices take the kernels' general
+    # membership path (a loop over the row's vertices) instead of a bit set
+    import random
+    r = random.Random(nv_range[1])
+    lines = []
+    for gi in range(40):
+        nv = r.randint(*nv_range)
+        lines.append("t # %d" % gi)
+        lines += ["v %d %d" % (v, r.choice([0, 0, 1, 2])) for v in range(nv)]
+        edges = set()
+        for v in range(1, nv):
+            edges.add((r.randrange(v), v))
+        for _ in range(nv // 8):
+            a, b = r.sample(range(nv), 2)
+            edges.add((min(a, b), max(a, b)))
+        lines += ["e %d %d %d" % (a, b, r.choice([0, 1])) for a, b in sorted(edges)]
+    p = str(tmp_path / "big.txt")
+    with open(p, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    db = gs.Database.load(p, "txt")
+    for s in (30, 20):
+        want = run_oracle(oracle, "txt", p, s, ["--max-edges", "5"])
+        got, _ = _mine_lines(gs, db, s, max_edges=5)
+        assert got == want, s
+
+
 def test_cudabin_and_bin_inputs(gs, tmp_path):
     src = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
     want = read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s17.txt"))
