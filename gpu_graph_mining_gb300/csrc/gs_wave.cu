@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
       // ---- emission, warp converged
       if(!MAT) {
         if(key >= 0) atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
-        if(lane == 0) mine += 8ull * __popc(__ballot_sync(kFull, key >= 0));
+        const unsigned ext = __ballot_sync(kFull, key >= 0);  // every lane takes part
+        if(lane == 0) mine += 8ull * __popc(ext);
         const unsigned peers = __match_any_sync(kFull, key);
         if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[key_base + key], __popc(peers));
       } else {
