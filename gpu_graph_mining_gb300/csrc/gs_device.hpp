@@ -29,6 +29,7 @@ struct DevDB {
   const int32_t *vlabel;
   const int32_t *vgraph;
   const int32_t *vbase;     // [G+1] first global vertex of each graph
+  const int32_t *adj_pair;  // [E2] pair index of each directed entry: pair_idx(label(source), el, label(nbr))
   const int32_t *pair_idx;
   int32_t VL, EL;
   int32_t n_graphs;
@@ -67,6 +68,11 @@ struct SlotDesc {
                      // for the right-most vertex (no rule)
   int32_t bkey_off;  // backward keys to this vertex: bkey_off + el; -1 if not a target
   int32_t bel, blab; // backward order rule: allowed iff bel < el || (bel == el && blab <= label(rightmost))
+  // the same two rules as single compares against an adjacency entry's high
+  // word hi = (el << 16) | nbr_label: forward allowed iff hi >= frule
+  // (INT32_MIN for the right-most vertex); backward allowed iff el >= bmin
+  int32_t frule;
+  int32_t bmin;
 };
 
 // Output slots of a child node selected for materialisation.

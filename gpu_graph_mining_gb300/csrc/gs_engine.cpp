@@ -95,7 +95,8 @@ void Database::upload()
   size_t o_pi = o_vg + al(sizeof(int32_t) * (V + 1));
   size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
   size_t o_vb = o_ro + al(sizeof(int32_t) * (VL + 1));
-  size_t total = o_vb + al(sizeof(int32_t) * (host.n_graphs + 1));
+  size_t o_ap = o_vb + al(sizeof(int32_t) * (host.n_graphs + 1));
+  size_t total = o_ap + al(sizeof(int32_t) * (E2 + 1));
   std::vector<unsigned long long> adj(E2 + 1, 0);
   parallel_ranges(E2, [&](int64_t b, int64_t e, int) {
     for(int64_t k = b; k < e; k++) {
@@ -115,6 +116,17 @@ void Database::upload()
   for(int32_t a = 0; a < VL; a++)
     for(size_t i = 0; i < pairs[a].size(); i++)
       pidx[((int64_t)a * EL + pairs[a][i].first) * VL + pairs[a][i].second] = (int32_t)i;
+  // per directed entry: dense index of (elabel, nbr label) among the pairs of
+  // the source vertex's label (the forward key offset within a slot, and the
+  // root key offset within root_off[label(source)])
+  std::vector<int32_t> ap(E2 + 1, 0);
+  parallel_ranges(V, [&](int64_t v0, int64_t v1, int) {
+    for(int64_t v = v0; v < v1; v++) {
+      const int64_t a = vl_dense[v];
+      for(int64_t k = host.aoff[v]; k < host.aoff[v + 1]; k++)
+        ap[k] = pidx[(size_t)((a * EL + el_dense[k]) * VL + vl_dense[host.adj_to[k]])];
+    }
+  });
   std::vector<int32_t> vb(host.n_graphs + 1);
   int32_t maxnv = 0;
   for(int32_t g = 0; g <= host.n_graphs; g++) vb[g] = (int32_t)host.vbase[g];
@@ -129,12 +141,14 @@ void Database::upload()
   CK(cudaMemcpy(b + o_pi, pidx.data(), sizeof(int32_t) * tab, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_ro, root_off.data(), sizeof(int32_t) * VL, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_vb, vb.data(), sizeof(int32_t) * (host.n_graphs + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_ap, ap.data(), sizeof(int32_t) * (E2 + 1), cudaMemcpyHostToDevice));
   dev.adj = (const unsigned long long *)(b + o_adj);
   dev.adj_off = (const int32_t *)(b + o_off);
   dev.vlabel = (const int32_t *)(b + o_vl);
   dev.vgraph = (const int32_t *)(b + o_vg);
   dev.pair_idx = (const int32_t *)(b + o_pi);
   dev.vbase = (const int32_t *)(b + o_vb);
+  dev.adj_pair = (const int32_t *)(b + o_ap);
   dev.max_graph_vertices = maxnv;
   dev.VL = VL;
   dev.EL = EL;
@@ -580,8 +594,12 @@ void layout_node(const PNode &n, const Database &db, NodeLayout &L)
     fk += db.pair_cnt[sd.vlab];
     sd.bkey_off = -1;
     sd.bel = sd.blab = 0;
+    // (fel, ftl) <= (el, tl) lexicographically <=> (fel << 16 | ftl) <= (el << 16 | tl)
+    sd.frule = s < L.nrm ? (int32_t)(((uint32_t)sd.fel << 16) | (uint32_t)sd.ftl) : INT32_MIN;
+    sd.bmin = INT32_MAX;
   }
   L.nfwd = fk;
+  const int32_t rlab = L.vlab[L.maxtoc];
   // backward targets: from-vertices of rmpath edges other than the deepest
   // (slots 0..nrm-2), unless the code already joins them to the right-most vertex
   for(int s = 0; s + 1 < L.nrm; s++) {
@@ -593,6 +611,8 @@ void layout_node(const PNode &n, const Database &db, NodeLayout &L)
     sd.bel = e.elabel;
     sd.blab = e.tolabel;
     sd.bkey_off = joined ? -1 : fk + s * db.EL;
+    // bel < el || (bel == el && blab <= label(r))  <=>  el >= bel + (blab > label(r))
+    sd.bmin = joined ? INT32_MAX : e.elabel + (e.tolabel > rlab ? 1 : 0);
   }
 }
 

@@ -91,7 +91,8 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
         const unsigned hi = (unsigned)(ent >> 32);
         const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
         mine += 8;
-        if(fl_o <= wl) key = root_off[fl_o] + __ldg(&db.pair_idx[((long long)fl_o * db.EL + el) * db.VL + wl]);
+        (void)el;
+        if(fl_o <= wl) key = root_off[fl_o] + __ldg(&db.adj_pair[e]);
       }
       if(!MAT) {
         if(key >= 0) {

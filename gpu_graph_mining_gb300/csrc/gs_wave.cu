@@ -102,8 +102,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
     const DevDB &dbr = a.dbs[nd.db];
     const unsigned long long *__restrict__ adj = dbr.adj;
     const int32_t *__restrict__ adj_off = dbr.adj_off;
-    const int32_t *__restrict__ pair_idx = dbr.pair_idx;
-    const int EL = dbr.EL, VL = dbr.VL, nv = dbr.n_vertices;
+    const int32_t *__restrict__ adj_pair = dbr.adj_pair;
+    const int nv = dbr.n_vertices;
     const int32_t *__restrict__ vbase = dbr.vbase;
     const int32_t *__restrict__ vgraph = dbr.vgraph;
     if(k > KMAX || nslot > KMAX || k < 1 || nslot < 1) {
@@ -170,7 +170,6 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
     }
     const int off = incl - W;
     const int T = __shfl_sync(kFull, incl, 31);
-    const int rlab = S.slot[nslot - 1].vlab;
     if(lane == 0) mine += 8ull * T;  // one packed adjacency entry per item
     for(int base = 0; base < T; base += 32) {
       const int j = base + lane;
@@ -194,41 +193,30 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         const int e = S.start[s][o] + (q - S.pre[s][o]);
         const unsigned long long ent = __ldg(&adj[e]);
         w = (int)(unsigned)(ent & 0xffffffffull);
-        const unsigned hi = (unsigned)(ent >> 32);
-        const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
-        const SlotDesc &sd = S.slot[s];
+        const int hi = (int)(ent >> 32);  // (edge label << 16) | neighbour label
+        const int wl = hi & 0xffff;
+        const bool is_r = (s == nslot - 1);
+        // forward: label >= minlabel and the right-most-path order rule (one
+        // compare, INT32_MIN for the right-most vertex); needs a new vertex
+        const bool fwd_rules = wl >= minlabel && hi >= S.slot[s].frule;
         bool in_emb = false;
         if(MASK) {
           const unsigned lv = (unsigned)(w - S.gb[o]);
           in_emb = lv < 64u && ((S.mask[o] >> lv) & 1ull);
+        } else if(fwd_rules || is_r) {
+          for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
         }
-        if(s != nslot - 1) {
-          // forward from a right-most-path vertex: label and order rules first
-          if(wl >= minlabel && (sd.fel < el || (sd.fel == el && sd.ftl <= wl))) {
-            if(!MASK)
-              for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
-            if(!in_emb) {
-              const int pk = __ldg(&pair_idx[((long long)sd.vlab * EL + el) * VL + wl]);
-              if(pk < 0) atomicOr(a.err, 2u); else key = sd.fkey_off + pk;
-            }
-          }
-        } else {
+        if(fwd_rules && !in_emb) {
+          key = S.slot[s].fkey_off + __ldg(&adj_pair[e]);
+        } else if(is_r && in_emb) {
+          // backward edge from the right-most vertex to a right-most-path vertex
           int jv = -1;
-          if(!MASK || in_emb)
-            for(int t = 0; t < k; ++t) if(S.phi[t][o] == w) jv = t;
-          if(jv >= 0) {
-            // backward edge from the right-most vertex to a right-most-path vertex
-            const int bs = S.vtab[jv];
-            if(bs >= 0) {
-              const SlotDesc &bd = S.slot[bs];
-              if(bd.bel < el || (bd.bel == el && bd.blab <= rlab)) {
-                key = bd.bkey_off + el;
-                bwd = true;
-              }
-            }
-          } else if(wl >= minlabel) {
-            const int pk = __ldg(&pair_idx[((long long)sd.vlab * EL + el) * VL + wl]);
-            if(pk < 0) atomicOr(a.err, 2u); else key = sd.fkey_off + pk;
+          for(int t = 0; t < k; ++t) if(S.phi[t][o] == w) jv = t;
+          const int bs = jv >= 0 ? S.vtab[jv] : -1;
+          const int el = hi >> 16;
+          if(bs >= 0 && el >= S.slot[bs].bmin) {
+            key = S.slot[bs].bkey_off + el;
+            bwd = true;
           }
         }
       }
