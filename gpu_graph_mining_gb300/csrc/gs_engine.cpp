@@ -464,6 +464,13 @@ struct Engine {
   DBuf<ChildOut> d_outs;
   DBuf<DevDB> d_dbs;
   DBuf<unsigned long long> d_bytes;
+  // extension records of the count pass (record-driven materialise)
+  DBuf<int4> d_rec;
+  DBuf<unsigned long long> d_recn;
+  DBuf<long long> d_keyword;
+  HBuf<long long> h_keyword;
+  HBuf<unsigned long long> h_recn;
+  bool rec_enabled = true;
   // pinned host mirrors
   HBuf<char> h_desc;
   HBuf<int32_t> h_sup, h_cnt, h_childmap;
@@ -493,7 +500,9 @@ struct Engine {
     pool.destroy();
     d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
     d_outs.free(); d_dbs.free(); d_bytes.free();
+    d_rec.free(); d_recn.free(); d_keyword.free();
     h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free();
+    h_keyword.free(); h_recn.free();
     for(auto &e : ev) cudaEventDestroy(e);
     cudaStreamDestroy(stream);
     cols.clear();
@@ -733,6 +742,7 @@ private:
   std::vector<JobState> js_;
   std::vector<PNode> stack_;
   bool mat_pending_ = false;
+  long long wanted_rec_ = 0;  // record capacity to have before the next wave (after an overflow)
 
   void h2d(void *dst, const void *src, size_t n)
   {
@@ -979,9 +989,34 @@ private:
     h2d(E.d_desc.p, hb, desc_bytes);
     CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
     CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
+    // records: sized from the adjacency entries the wave can scan at most is
+    // unknown up front, so keep the largest count seen (grown after an overflow)
+    int4 *rec = nullptr;
+    long long rec_cap = 0;
+    if(E.rec_enabled && wanted_rec_ > (long long)E.d_rec.cap) {
+      // grow after an overflow; past 2^28 records (4 GiB) or when the device
+      // has no room, keep the enumeration-based materialise instead
+      if(wanted_rec_ > (1ll << 28)) E.rec_enabled = false;
+      else {
+        try {
+          E.d_rec.ensure((size_t)wanted_rec_);
+        } catch(const Error &) {
+          cudaGetLastError();
+          E.rec_enabled = false;
+        }
+      }
+    }
+    if(E.rec_enabled) {
+      E.d_recn.ensure(1);
+      E.h_recn.ensure(1);
+      if(E.d_rec.cap == 0) E.d_rec.ensure((size_t)1 << 22);
+      rec = E.d_rec.p;
+      rec_cap = (long long)E.d_rec.cap;
+      CK(cudaMemsetAsync(E.d_recn.p, 0, sizeof(unsigned long long), E.stream));
+    }
     CK(cudaEventRecord(E.ev[0], E.stream));
     launch_wave_count(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
-                      E.stream);
+                      rec, rec_cap, rec ? E.d_recn.p : nullptr, E.stream);
     CK(cudaEventRecord(E.ev[1], E.stream));
     launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
     CK(cudaEventRecord(E.ev[2], E.stream));
@@ -990,6 +1025,7 @@ private:
     E.h_cnt.ensure(std::max(kb, 1));
     d2h(E.h_sup.p, E.d_sup.p, (size_t)kb * 4);
     d2h(E.h_cnt.p, E.d_cnt.p, (size_t)kb * 4);
+    if(rec) d2h(E.h_recn.p, E.d_recn.p, sizeof(unsigned long long));
     const clk::time_point t_sync = clk::now();
     st_.host_build_ms += std::chrono::duration<double, std::milli>(t_sync - t_begin).count();
     CK(cudaStreamSynchronize(E.stream));
@@ -1114,8 +1150,23 @@ private:
       h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
       CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(E.ev[4], E.stream));
-      launch_wave_materialize(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p, E.d_childmap.p,
-                              E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
+      const long long nrec = rec ? (long long)E.h_recn.p[0] : -1;
+      if(rec && nrec <= rec_cap) {
+        // record-driven: one thread per extension record, no graph access
+        E.h_keyword.ensure(std::max(kb, 1));
+        E.d_keyword.ensure(std::max(kb, 1));
+        for(int32_t n = 0; n < W; n++)
+          for(int32_t k2 = 0; k2 < hn[n].nkeys; k2++)
+            E.h_keyword.p[hn[n].key_base + k2] = hn[n].bm_base + (long long)k2 * hn[n].words;
+        h2d(E.d_keyword.p, E.h_keyword.p, sizeof(long long) * (size_t)kb);
+        launch_materialize_records(rec, nrec, E.d_childmap.p, E.d_keyword.p, E.d_bm.p, E.d_bmx.p, E.d_cursor.p,
+                                   E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
+      } else {
+        // records overflowed (or are disabled): enumerate again
+        launch_wave_materialize(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p,
+                                E.d_childmap.p, E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
+        if(rec) wanted_rec_ = std::max<long long>(wanted_rec_, nrec + nrec / 4);
+      }
       CK(cudaEventRecord(E.ev[5], E.stream));
       st_.launches++;
       mat_pending_ = true;

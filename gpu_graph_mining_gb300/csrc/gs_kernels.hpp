@@ -30,13 +30,20 @@ void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uin
 void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax, bool small_graphs,
                        const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
                        const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
-                       cudaStream_t s);
+                       int4 *rec, long long rec_cap, unsigned long long *rec_n, cudaStream_t s);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
                              unsigned long long *bytes, unsigned int *err, cudaStream_t s);
+
+// Materialise from the count pass's records {wave key, x, y, graph rank}:
+// children whose key is selected get column element (x, y) and their graph
+// rank.  keyword[key] = the key's first support-bitmap word.
+void launch_materialize_records(const int4 *rec, long long n, const int32_t *childmap, const long long *keyword,
+                                const uint32_t *bm, const int32_t *bmx, int32_t *cursor, const ChildOut *outs,
+                                unsigned long long *bytes, unsigned int *err, cudaStream_t s);
 
 // Extension records given as (key, graph id) pairs: sets bit [key][graph].
 // Keys and graph ids must be in range (checked by the caller).

@@ -52,6 +52,11 @@ struct WaveArgs {
   const ChildOut *outs;
   unsigned long long *bytes;
   unsigned int *err;
+  // count pass, optional: one record per extension {wave key, child column
+  // element x, y, graph rank} for the record-driven materialise pass
+  int4 *rec;
+  long long rec_cap;
+  unsigned long long *rec_n;  // records produced (may exceed rec_cap: then none past it are written)
 };
 
 template <int KMAX> struct Smem {
@@ -227,6 +232,18 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         if(lane == 0) mine += 8ull * __popc(ext);
         const unsigned peers = __match_any_sync(kFull, key);
         if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[key_base + key], __popc(peers));
+        if(a.rec && ext) {
+          // append this step's extensions as consecutive records (one atomic per warp)
+          unsigned long long rb = 0;
+          if(lane == 0) rb = atomicAdd(a.rec_n, (unsigned long long)__popc(ext));
+          rb = __shfl_sync(kFull, rb, 0) + __popc(ext & lanemask_lt());
+          if(key >= 0 && (long long)rb < a.rec_cap) {
+            const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
+            a.rec[rb] = bwd ? make_int4(key_base + key, S.phi[k - 1][o], lp_o, g_o)
+                            : make_int4(key_base + key, w, i_o, g_o);
+          }
+          if(lane == 0) mine += 16ull * __popc(ext);
+        }
       } else {
         const int c = key >= 0 ? a.childmap[key_base + key] : -1;
         const unsigned ext = __ballot_sync(kFull, key >= 0), sel = __ballot_sync(kFull, c >= 0);
@@ -292,11 +309,11 @@ template <bool MAT> void dispatch(int kmax, bool small_graphs, const WaveArgs &a
 void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax, bool small_graphs,
                        const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
                        const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
-                       cudaStream_t s)
+                       int4 *rec, long long rec_cap, unsigned long long *rec_n, cudaStream_t s)
 {
   if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
-              nullptr, nullptr, nullptr, bytes, err };
+              nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n };
   dispatch<false>(kmax, small_graphs, a, s);
 }
 
@@ -309,8 +326,68 @@ void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long to
 {
   if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, const_cast<uint32_t *>(bm), bmx,
-              nullptr, childmap, cursor, outs, bytes, err };
+              nullptr, childmap, cursor, outs, bytes, err, nullptr, 0, nullptr };
   dispatch<true>(kmax, small_graphs, a, s);
+}
+
+namespace {
+
+// Materialise from the count pass's records: one thread per record, no graph
+// access.  keyword[key] = the key's first bitmap word (node bm_base + key * words).
+__global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ rec, long long n,
+                                                     const int32_t *__restrict__ childmap,
+                                                     const long long *__restrict__ keyword,
+                                                     const uint32_t *__restrict__ bm, const int32_t *__restrict__ bmx,
+                                                     int32_t *cursor, const ChildOut *__restrict__ outs,
+                                                     unsigned long long *bytes, unsigned int *err)
+{
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long mine = 0;
+  // the loop runs a warp-uniform number of times: lanes past n carry no record
+  const long long n32 = (n + 31) & ~31ll;
+  for(long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n32; r += stride) {
+    int c = -1;
+    int4 x = make_int4(0, 0, 0, 0);
+    if(r < n) {
+      x = __ldg(&rec[r]);
+      c = childmap[x.x];
+      mine += 20;
+    }
+    const unsigned peers = __match_any_sync(kFull, c);
+    const int leader = __ffs(peers) - 1;
+    int pos = 0;
+    if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[c], __popc(peers));
+    pos = __shfl_sync(kFull, pos, leader) + __popc(peers & lanemask_lt());
+    if(c >= 0) {
+      const long long wi = keyword[x.x] + (x.w >> 5);
+      const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (x.w & 31)) - 1u));
+      const ChildOut out = outs[c];
+      if(pos < out.cap) {
+        out.col[pos] = make_int2(x.y, x.z);
+        out.gord[pos] = rank;
+      } else {
+        atomicOr(err, 4u);
+      }
+      mine += 28;
+    }
+  }
+  if(bytes) {
+    for(int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(kFull, mine, o);
+    if(lane == 0 && mine) atomicAdd(bytes, mine);
+  }
+}
+
+}  // namespace
+
+void launch_materialize_records(const int4 *rec, long long n, const int32_t *childmap, const long long *keyword,
+                                const uint32_t *bm, const int32_t *bmx, int32_t *cursor, const ChildOut *outs,
+                                unsigned long long *bytes, unsigned int *err, cudaStream_t s)
+{
+  if(n <= 0) return;
+  long long blocks = ((n + 31) / 32 * 32 + 255) / 256;
+  if(blocks > 152LL * 16) blocks = 152LL * 16;
+  k_mat_records<<<(int)blocks, 256, 0, s>>>(rec, n, childmap, keyword, bm, bmx, cursor, outs, bytes, err);
 }
 
 }  // namespace gsgb
