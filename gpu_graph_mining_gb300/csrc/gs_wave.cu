@@ -34,6 +34,7 @@ namespace {
 
 constexpr int kWarps = 4;  // warps per block
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kRecChunk = 128;  // records a warp reserves at a time
 
 struct WaveArgs {
   const NodeDesc *nodes;
@@ -88,6 +89,10 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
   const long long gwarp = (long long)blockIdx.x * kWarps + warp;
   const long long nwarps = (long long)gridDim.x * kWarps;
   unsigned long long mine = 0;
+  // count pass with records: the warp's current reserved chunk (warp-uniform);
+  // starts "full" so the first batch reserves a chunk
+  long long chunk_base = -1;
+  int chunk_fill = kRecChunk;
 
   for(long long tile = gwarp; tile < a.total_tiles; tile += nwarps) {
     // ---- the tile's node (warp-uniform: tiles never span nodes)
@@ -233,16 +238,30 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         const unsigned peers = __match_any_sync(kFull, key);
         if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[key_base + key], __popc(peers));
         if(a.rec && ext) {
-          // append this step's extensions as consecutive records (one atomic per warp)
-          unsigned long long rb = 0;
-          if(lane == 0) rb = atomicAdd(a.rec_n, (unsigned long long)__popc(ext));
-          rb = __shfl_sync(kFull, rb, 0) + __popc(ext & lanemask_lt());
-          if(key >= 0 && (long long)rb < a.rec_cap) {
-            const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
-            a.rec[rb] = bwd ? make_int4(key_base + key, S.phi[k - 1][o], lp_o, g_o)
-                            : make_int4(key_base + key, w, i_o, g_o);
+          // append this step's extensions to the warp's current chunk of
+          // kRecChunk records; a batch that does not fit is split across a
+          // freshly reserved chunk (one global atomic per chunk, not per step)
+          const int cntx = __popc(ext);
+          const int rank = __popc(ext & lanemask_lt());
+          long long dst = -1;
+          if(chunk_fill + cntx <= kRecChunk) {
+            dst = chunk_base + chunk_fill + rank;
+            chunk_fill += cntx;
+          } else {
+            const int room = kRecChunk - chunk_fill;
+            long long nb = 0;
+            if(lane == 0) nb = (long long)atomicAdd(a.rec_n, (unsigned long long)kRecChunk);
+            nb = __shfl_sync(kFull, nb, 0);
+            dst = rank < room ? chunk_base + chunk_fill + rank : nb + (rank - room);
+            chunk_base = nb;
+            chunk_fill = cntx - room;
           }
-          if(lane == 0) mine += 16ull * __popc(ext);
+          if(key >= 0 && dst >= 0 && dst < a.rec_cap) {
+            const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
+            a.rec[dst] = bwd ? make_int4(key_base + key, S.phi[k - 1][o], lp_o, g_o)
+                             : make_int4(key_base + key, w, i_o, g_o);
+          }
+          if(lane == 0) mine += 16ull * cntx;
         }
       } else {
         const int c = key >= 0 ? a.childmap[key_base + key] : -1;
@@ -268,6 +287,13 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
       }
     }
     __syncwarp();
+  }
+  if(!MAT && a.rec && chunk_base >= 0) {
+    // mark the unused tail of the last chunk as holes (key -1)
+    for(int f = chunk_fill + lane; f < kRecChunk; f += 32) {
+      const long long dst = chunk_base + f;
+      if(dst < a.rec_cap) a.rec[dst] = make_int4(-1, 0, 0, 0);
+    }
   }
   if(a.bytes) {
     for(int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(kFull, mine, o);
@@ -351,7 +377,7 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
     int4 x = make_int4(0, 0, 0, 0);
     if(r < n) {
       x = __ldg(&rec[r]);
-      c = childmap[x.x];
+      if(x.x >= 0) c = childmap[x.x];  // key -1: an unused slot of a reserved chunk
       mine += 20;
     }
     const unsigned peers = __match_any_sync(kFull, c);
