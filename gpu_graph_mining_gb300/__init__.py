@@ -33,6 +33,8 @@ EXPORTS = [
     "gs_mine", "gs_mine_ex", "gs_mine_collect", "gs_patterns_free", "gs_mine_batch", "gs_support_count",
     "gs_support_count_noalloc",
     "gs_dfs_code_is_min", "gs_engine_reset", "gs_engine_set_pool_bytes",
+    "gs_server_opts_default", "gs_server_create", "gs_server_add_db", "gs_server_submit", "gs_server_poll",
+    "gs_server_cancel", "gs_server_get_stats", "gs_server_destroy",
 ]
 
 
@@ -74,6 +76,33 @@ class Patterns(ctypes.Structure):
                 ("offset", ctypes.POINTER(ctypes.c_int64)), ("dfs", ctypes.POINTER(ctypes.c_int32)),
                 ("support", ctypes.POINTER(ctypes.c_int64))]
 
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_int64), ("pool_bytes", ctypes.c_int64),
+                ("max_active", ctypes.c_int32), ("wave_nodes", ctypes.c_int32),
+                ("threads", ctypes.c_int32), ("label_style", ctypes.c_int32)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("status", ctypes.c_int32), ("patterns", ctypes.c_int64),
+                ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double), ("peak_bytes", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_int64) for f in ("submitted", "completed", "cancelled", "failed", "queued",
+                                              "running", "max_running", "patterns")] + \
+               [(f, ctypes.c_double) for f in ("p50_ms", "p99_ms", "mean_ms", "wall_ms", "busy_ms")] + \
+               [(f, ctypes.c_int64) for f in ("budget_bytes", "reserved_bytes", "pool_used_bytes",
+                                              "peak_pool_bytes", "waves", "launches")]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 EMIT_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p)
 BATCH_EMIT_FN = ctypes.CFUNCTYPE(None, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
@@ -135,6 +164,22 @@ def lib():
     L.gs_engine_reset.restype = None
     L.gs_engine_set_pool_bytes.argtypes = [i64]
     L.gs_engine_set_pool_bytes.restype = None
+    L.gs_server_opts_default.argtypes = [ctypes.POINTER(ServerOpts)]
+    L.gs_server_opts_default.restype = None
+    L.gs_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
+    L.gs_server_create.restype = i32
+    L.gs_server_add_db.argtypes = [vp, vp, pi32]
+    L.gs_server_add_db.restype = i32
+    L.gs_server_submit.argtypes = [vp, i32, i32, i32, ctypes.POINTER(i64)]
+    L.gs_server_submit.restype = i32
+    L.gs_server_poll.argtypes = [vp, i64, i32, ctypes.POINTER(RequestInfo), ctypes.POINTER(ctypes.POINTER(Patterns))]
+    L.gs_server_poll.restype = i32
+    L.gs_server_cancel.argtypes = [vp, i64]
+    L.gs_server_cancel.restype = i32
+    L.gs_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+    L.gs_server_get_stats.restype = i32
+    L.gs_server_destroy.argtypes = [vp]
+    L.gs_server_destroy.restype = None
     _lib = L
     return L
 
@@ -285,18 +330,22 @@ def mine_collect(db, minsup, decode=True, **kw):
     st = MineStats()
     p = ctypes.POINTER(Patterns)()
     _check(lib().gs_mine_collect(db.handle, int(minsup), ctypes.byref(o), ctypes.byref(p), ctypes.byref(st)))
+    return _take_patterns(p, decode), st.as_dict()
+
+
+def _take_patterns(p, decode=True):
+    """Converts a native gs_patterns buffer to [(code, support)] and frees it."""
     try:
         P = p.contents
         if not decode:
-            return P.count, st.as_dict()
+            return P.count
         import numpy as np
         off = np.ctypeslib.as_array(P.offset, shape=(P.count + 1,)).copy() if P.count else np.zeros(1, np.int64)
         dfs = (np.ctypeslib.as_array(P.dfs, shape=(5 * P.n_tuples,)).reshape(-1, 5).copy()
                if P.n_tuples else np.zeros((0, 5), np.int32))
         sup = np.ctypeslib.as_array(P.support, shape=(P.count,)).copy() if P.count else np.zeros(0, np.int64)
-        out = [(tuple(tuple(int(x) for x in row) for row in dfs[off[i]:off[i + 1]]), int(sup[i]))
-               for i in range(P.count)]
-        return out, st.as_dict()
+        return [(tuple(tuple(int(x) for x in row) for row in dfs[off[i]:off[i + 1]]), int(sup[i]))
+                for i in range(P.count)]
     finally:
         lib().gs_patterns_free(p)
 
@@ -379,6 +428,77 @@ class GSpanMiner:
 
     def delete_database_from_device(self):
         lib().gs_engine_reset()
+
+
+class Server:
+    """Serving loop (gs_server_*): requests on resident databases, mined with
+    continuous batching by a native server thread."""
+
+    def __init__(self, budget_bytes=0, pool_bytes=0, max_active=0, wave_nodes=0, threads=0,
+                 label_style=LABELS_FULL):
+        o = ServerOpts()
+        lib().gs_server_opts_default(ctypes.byref(o))
+        o.budget_bytes, o.pool_bytes = int(budget_bytes), int(pool_bytes)
+        if max_active:
+            o.max_active = int(max_active)
+        o.wave_nodes, o.threads, o.label_style = int(wave_nodes), int(threads), int(label_style)
+        h = ctypes.c_void_p()
+        _check(lib().gs_server_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._dbs = []   # the server borrows the databases: keep them alive
+
+    def add_db(self, db):
+        i = ctypes.c_int32()
+        _check(lib().gs_server_add_db(self._h, db.handle, ctypes.byref(i)))
+        self._dbs.append(db)
+        return i.value
+
+    def submit(self, db_id, minsup, max_edges=0):
+        rid = ctypes.c_int64()
+        _check(lib().gs_server_submit(self._h, int(db_id), int(minsup), int(max_edges), ctypes.byref(rid)))
+        return rid.value
+
+    def status(self, request_id, wait_ms=0):
+        """Request info without taking the result; None while it is still running."""
+        info = RequestInfo()
+        st = lib().gs_server_poll(self._h, int(request_id), int(wait_ms), ctypes.byref(info), None)
+        if st == 9:
+            return None
+        _check(st)
+        return info.as_dict()
+
+    def result(self, request_id, timeout_ms=-1, decode=True):
+        """Waits for the request; returns (patterns or None, info) and forgets it."""
+        info = RequestInfo()
+        p = ctypes.POINTER(Patterns)()
+        _check(lib().gs_server_poll(self._h, int(request_id), int(timeout_ms), ctypes.byref(info), ctypes.byref(p)))
+        pats = _take_patterns(p, decode) if p else None
+        return pats, info.as_dict()
+
+    def cancel(self, request_id):
+        _check(lib().gs_server_cancel(self._h, int(request_id)))
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().gs_server_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().gs_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def engine_reset():

@@ -22,7 +22,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SRCS = ["gs_kernels.cu", "gs_wave.cu", "gs_noalloc.cu"]
-CPP_SRCS = ["gs_db.cpp", "gs_dfs.cpp", "gs_engine.cpp", "gs_capi.cpp"]
+CPP_SRCS = ["gs_db.cpp", "gs_dfs.cpp", "gs_engine.cpp", "gs_capi.cpp", "gs_server.cpp"]
 
 
 def _run(cmd):

@@ -7,10 +7,7 @@
 
 #include "gs_db.hpp"
 #include "gs_engine.hpp"
-
-struct gs_db {
-  gsgb::Database d;
-};
+#include "gs_handles.hpp"
 
 namespace {
 
@@ -217,45 +214,25 @@ gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs
   return GS_OK;
 }
 
-struct PatternBuf {
-  gs_patterns view;
-  std::vector<int64_t> offset{ 0 };
-  std::vector<int32_t> dfs;
-  std::vector<int64_t> support;
-};
-
-static void collect_emit(const int32_t *d, int32_t n, int64_t sup, void *user)
-{
-  PatternBuf *b = (PatternBuf *)user;
-  b->dfs.insert(b->dfs.end(), d, d + 5 * n);
-  b->offset.push_back(b->offset.back() + n);
-  b->support.push_back(sup);
-}
-
 gs_status gs_mine_collect(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_patterns **out,
                           gs_mine_stats *stats)
 {
   if(!out) return set_err(GS_ERR_USAGE, "null output");
   *out = nullptr;
-  PatternBuf *b = new PatternBuf();
-  gs_status st = gs_mine_ex(db, abs_minsup, opts, collect_emit, b, stats);
+  gsgb::PatternBuf *b = new gsgb::PatternBuf();
+  gs_status st = gs_mine_ex(db, abs_minsup, opts, gsgb::PatternBuf::emit, b, stats);
   if(st != GS_OK) {
     delete b;
     return st;
   }
-  b->view.count = (int64_t)b->support.size();
-  b->view.n_tuples = b->offset.back();
-  b->view.offset = b->offset.data();
-  b->view.dfs = b->dfs.data();
-  b->view.support = b->support.data();
-  *out = &b->view;
+  *out = b->publish();
   return GS_OK;
 }
 
 void gs_patterns_free(gs_patterns *p)
 {
   // view is the first member of PatternBuf
-  delete reinterpret_cast<PatternBuf *>(p);
+  delete reinterpret_cast<gsgb::PatternBuf *>(p);
 }
 
 gs_status gs_mine(gs_db *db, int32_t abs_minsup, int32_t max_edges, gs_emit_fn emit, void *user)

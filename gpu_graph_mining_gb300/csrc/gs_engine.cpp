@@ -411,13 +411,6 @@ struct PatternRec {
   std::vector<int32_t> children;
 };
 
-struct JobState {
-  MineJob *job;
-  int32_t db_slot;
-  std::vector<PatternRec> pats;
-  std::vector<int32_t> roots;
-};
-
 struct PNode {
   int32_t job;
   int32_t pattern;
@@ -427,6 +420,21 @@ struct PNode {
   int32_t gord_blk;
   int64_t nrows;
   int64_t support;
+};
+
+// One mining job inside a scheduler.
+struct JobState {
+  MineJob job;
+  int32_t db_slot = 0;
+  std::vector<PatternRec> pats;
+  std::vector<int32_t> roots;
+  std::vector<PNode> stack;    // DFS-tree nodes waiting for a wave (top = back)
+  int64_t pending = 0;         // nodes on the stack or in a wave in flight
+  int64_t live_bytes = 0;      // embedding-store bytes held by the job's nodes
+  int64_t peak_bytes = 0;
+  int64_t patterns = 0;        // emitted when the job finished
+  bool cancelled = false;
+  bool done = false;
 };
 
 struct Candidate {
@@ -446,9 +454,55 @@ struct NodeLayout {
   std::vector<SlotDesc> slots;
 };
 
+// Device scratch and pinned mirrors of one wave in flight.  Two of them let
+// the host prepare one wave's children while the GPU counts the other's.
+struct WaveCtx {
+  DBuf<char> d_desc;
+  DBuf<uint32_t> d_bm;
+  DBuf<int32_t> d_bmx, d_cnt, d_sup, d_childmap, d_cursor;
+  DBuf<ChildOut> d_outs;
+  // extension records of the count pass (record-driven materialise)
+  DBuf<int4> d_rec;
+  DBuf<unsigned long long> d_recn;
+  DBuf<long long> d_keyword;
+  bool rec_enabled = true;
+  long long wanted_rec = 0;    // record capacity to have before the next wave (after an overflow)
+  // pinned host mirrors
+  HBuf<char> h_desc;
+  HBuf<int32_t> h_sup, h_cnt, h_childmap;
+  HBuf<ChildOut> h_outs;
+  HBuf<long long> h_keyword;
+  HBuf<unsigned long long> h_misc;  // [0] records written, [1] consistency flags
+  // 0/1 count, 1/2 support, 3 results copied, 4/5 materialise
+  cudaEvent_t ev[6] = {};
+  bool have_events = false;
+
+  void init()
+  {
+    if(!have_events) {
+      for(auto &e : ev) CK(cudaEventCreate(&e));
+      have_events = true;
+    }
+    h_misc.ensure(2);
+    d_recn.ensure(1);
+  }
+  void free()
+  {
+    d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
+    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free();
+    h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free(); h_keyword.free(); h_misc.free();
+    if(have_events)
+      for(auto &e : ev) cudaEventDestroy(e);
+    have_events = false;
+    rec_enabled = true;
+    wanted_rec = 0;
+  }
+};
+
+constexpr int kMaxDbSlots = 256;   // databases one scheduler keeps in its device table before it grows
+
 struct Engine {
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev[8];
   Pool pool;
   std::unique_ptr<Workers> workers;
   std::vector<MinChecker> checkers;
@@ -457,24 +511,10 @@ struct Engine {
   std::vector<Block> blocks;
   std::vector<int32_t> free_blocks;
   int64_t pool_limit = 0;
-  // device scratch
-  DBuf<char> d_desc;
-  DBuf<uint32_t> d_bm;
-  DBuf<int32_t> d_bmx, d_cnt, d_sup, d_childmap, d_cursor;
-  DBuf<ChildOut> d_outs;
   DBuf<DevDB> d_dbs;
-  DBuf<unsigned long long> d_bytes;
-  // extension records of the count pass (record-driven materialise)
-  DBuf<int4> d_rec;
-  DBuf<unsigned long long> d_recn;
-  DBuf<long long> d_keyword;
-  HBuf<long long> h_keyword;
-  HBuf<unsigned long long> h_recn;
-  bool rec_enabled = true;
-  // pinned host mirrors
-  HBuf<char> h_desc;
-  HBuf<int32_t> h_sup, h_cnt, h_childmap;
-  HBuf<ChildOut> h_outs;
+  DBuf<unsigned long long> d_bytes;   // [0] count bytes, [1] materialise bytes, [2] root bytes, [3] flags
+  WaveCtx ctx[2];
+  WaveCtx rootc;
   bool ready = false;
 
   void init(int threads)
@@ -482,8 +522,11 @@ struct Engine {
     if(!ready) {
       CK(cudaSetDevice(0));
       CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-      for(auto &e : ev) CK(cudaEventCreate(&e));
       d_bytes.ensure(4);
+      d_dbs.ensure(kMaxDbSlots);
+      CK(cudaMemsetAsync(d_bytes.p, 0, sizeof(unsigned long long) * 4, stream));
+      for(auto &c : ctx) c.init();
+      rootc.init();
       ready = true;
     }
     pool.set_limit(pool_limit);
@@ -498,12 +541,10 @@ struct Engine {
     if(!ready) return;
     cudaStreamSynchronize(stream);
     pool.destroy();
-    d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
-    d_outs.free(); d_dbs.free(); d_bytes.free();
-    d_rec.free(); d_recn.free(); d_keyword.free();
-    h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free();
-    h_keyword.free(); h_recn.free();
-    for(auto &e : ev) cudaEventDestroy(e);
+    d_dbs.free();
+    d_bytes.free();
+    for(auto &c : ctx) c.free();
+    rootc.free();
     cudaStreamDestroy(stream);
     cols.clear();
     free_cols.clear();
@@ -544,15 +585,19 @@ struct Engine {
     return id;
   }
   void ref(int32_t id) { cols[id].refs++; }
-  void unref(int32_t id)
+  // drops one reference; returns the column's bytes when it was the last
+  int64_t unref(int32_t id)
   {
     if(--cols[id].refs == 0) {
       block_unref(cols[id].blk);
       cols[id].ptr = nullptr;
       free_cols.push_back(id);
+      return cols[id].n * (int64_t)sizeof(int2);
     }
+    return 0;
   }
 };
+
 
 // Carves consecutive 256-byte-aligned pieces out of one block.
 struct Carver {
@@ -690,59 +735,167 @@ struct ScopeMs {
   ~ScopeMs() { acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
 };
 
-class Runner {
-public:
-  Runner(Engine &e, std::vector<MineJob> &jobs, const MineOptions &wo, MineStats &st)
-      : E(e), jobs_(jobs), wo_(wo), st_(st) {}
+using clk = std::chrono::steady_clock;
 
-  void run()
+double ms_since(clk::time_point t0) { return std::chrono::duration<double, std::milli>(clk::now() - t0).count(); }
+
+// One wave in flight: its nodes and where their descriptors live.
+struct Flight {
+  bool busy = false;
+  bool mat_pending = false;  // the ctx's materialise events still to be read
+  uint64_t seq = 0;
+  std::vector<PNode> nodes;
+  std::vector<NodeLayout> lays;
+  NodeDesc *hn = nullptr;    // in the ctx's pinned descriptor mirror
+  const NodeDesc *dn = nullptr;
+  const int2 *const *dc = nullptr;
+  const SlotDesc *ds = nullptr;
+  const int32_t *dv = nullptr, *dl = nullptr;
+  int32_t W = 0, kb = 0, kmax = 1;
+  bool small = true;
+  int64_t tb = 0;
+  int4 *rec = nullptr;
+  long long rec_cap = 0;
+};
+
+// The wave scheduler.  Jobs join at any time (add) and leave when their last
+// DFS-tree node is done; each step launches waves into the idle contexts and
+// completes the oldest wave in flight.  With two contexts the host decodes
+// one wave's candidates, checks canonicality and lays out its children while
+// the GPU counts the other wave.  All device work is issued on the engine's
+// one stream, so a wave's children are materialised before any later wave
+// reads them, and pool memory released on the host is only reused by work
+// queued after its last reader.
+class Sched {
+public:
+  Sched(Engine &e, const MineOptions &wo, MineStats &st) : E(e), wo_(wo), st_(st)
   {
-    auto t0 = std::chrono::steady_clock::now();
+    nctx_ = wo_.wave_nodes > 1 ? 2 : 1;
     E.pool.reset_peak();
-    // resident databases
-    std::vector<Database *> dbs;
-    for(auto &j : jobs_) {
-      if(!j.db->resident) {
-        j.db->upload();
-        st_.h2d_bytes += (int64_t)j.db->d_bytes;
-      }
-      int32_t slot = -1;
-      for(size_t i = 0; i < dbs.size(); i++) if(dbs[i] == j.db) slot = (int32_t)i;
-      if(slot < 0) { slot = (int32_t)dbs.size(); dbs.push_back(j.db); }
-      js_.push_back(JobState{ &j, slot, {}, {} });
-    }
-    std::vector<DevDB> tab;
-    for(auto *d : dbs) tab.push_back(d->dev);
-    E.d_dbs.ensure(tab.size());
-    h2d(E.d_dbs.p, tab.data(), sizeof(DevDB) * tab.size());
     CK(cudaMemsetAsync(E.d_bytes.p, 0, sizeof(unsigned long long) * 4, E.stream));
-    for(size_t j = 0; j < js_.size(); j++) root_phase((int32_t)j);
-    while(!stack_.empty()) wave();
-    flush_timing();
+  }
+
+  // Validates the job, makes its database resident, mines its root level and
+  // queues its root nodes.  Returns the job id.
+  int32_t add(const MineJob &j)
+  {
+    if(!j.db) throw Error(ST_ERR_USAGE, "null database");
+    if(j.minsup < 1) throw Error(ST_ERR_MINSUP_TOO_SMALL, "error: absolute_min_support < 1");
+    if(j.minsup >= j.db->host.n_graphs)
+      throw Error(ST_ERR_MINSUP_TOO_LARGE, "error: user specified support " + std::to_string(j.minsup) +
+                                               " is greater then the database size " +
+                                               std::to_string(j.db->host.n_graphs));
+    Database *db = j.db;
+    if(!db->resident) {
+      db->upload();
+      st_.h2d_bytes += (int64_t)db->d_bytes;
+    }
+    int32_t slot = -1;
+    for(size_t i = 0; i < dbs_.size(); i++)
+      if(dbs_[i] == db) slot = (int32_t)i;
+    if(slot < 0) {
+      slot = (int32_t)dbs_.size();
+      dbs_.push_back(db);
+      tab_.push_back(db->dev);
+      if(tab_.size() > E.d_dbs.cap) {
+        // the table is read by waves in flight: let them finish before it moves
+        CK(cudaStreamSynchronize(E.stream));
+        E.d_dbs.ensure(tab_.size());
+        h2d(E.d_dbs.p, tab_.data(), sizeof(DevDB) * tab_.size());
+      } else {
+        h2d(E.d_dbs.p + slot, &tab_[slot], sizeof(DevDB));
+      }
+    }
+    const int32_t id = (int32_t)jobs_.size();
+    jobs_.emplace_back(new JobState());
+    JobState &S = *jobs_.back();
+    S.job = j;
+    S.db_slot = slot;
+    active_++;
+    order_.push_back(id);
+    root_phase(id);
+    if(S.pending == 0) complete(id);
+    return id;
+  }
+
+  bool idle() const { return active_ == 0; }
+
+  void step()
+  {
+    for(int c = 0; c < nctx_; c++)
+      if(!fl_[c].busy) launch(c, nctx_ > 1 && fl_[1 - c].busy);
+    int pick = -1;
+    for(int c = 0; c < nctx_; c++)
+      if(fl_[c].busy && (pick < 0 || fl_[c].seq < fl_[pick].seq)) pick = c;
+    if(pick >= 0) finish(pick);
+  }
+
+  // Stops a job: its queued nodes are dropped now, the children of its nodes
+  // in flight are not made.  It completes (without output) when nothing of it
+  // is in flight.
+  void cancel(int32_t id)
+  {
+    JobState *S = job(id);
+    if(!S || S->done || S->cancelled) return;
+    S->cancelled = true;
+    for(PNode &p : S->stack) drop_node(*S, p);
+    stacked_ -= (int64_t)S->stack.size();
+    S->stack.clear();
+    if(S->pending == 0) complete(id);
+  }
+
+  std::vector<int32_t> take_done()
+  {
+    std::vector<int32_t> v;
+    v.swap(done_);
+    return v;
+  }
+  JobState *job(int32_t id) { return id >= 0 && id < (int32_t)jobs_.size() ? jobs_[id].get() : nullptr; }
+  void forget(int32_t id)
+  {
+    if(job(id) && jobs_[id]->done) jobs_[id].reset();
+  }
+
+  // Waits for the last materialise passes and folds the device counters into
+  // the statistics; checks the kernels' consistency flags.
+  void sync_stats()
+  {
+    for(int c = 0; c < nctx_; c++) {
+      if(fl_[c].mat_pending) {
+        CK(cudaEventSynchronize(E.ctx[c].ev[5]));
+        st_.mat_ms += ms_between(E.ctx[c].ev[4], E.ctx[c].ev[5]);
+        fl_[c].mat_pending = false;
+      }
+    }
     unsigned long long bytes[4] = { 0, 0, 0, 0 };
     d2h(bytes, E.d_bytes.p, sizeof(bytes));
     CK(cudaStreamSynchronize(E.stream));
     CK(cudaGetLastError());
     if(bytes[3]) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(bytes[3]) + ")");
-    st_.count_bytes += (int64_t)bytes[0];
-    st_.mat_bytes += (int64_t)bytes[1];
+    st_.count_bytes += (int64_t)bytes[0] - seen_bytes_[0];
+    st_.mat_bytes += (int64_t)bytes[1] - seen_bytes_[1];
+    seen_bytes_[0] = (int64_t)bytes[0];
+    seen_bytes_[1] = (int64_t)bytes[1];
     st_.peak_pool_bytes = std::max<int64_t>(st_.peak_pool_bytes, (int64_t)E.pool.peak());
-    {
-      ScopeMs t(st_.host_emit_ms);
-      for(auto &s : js_) emit(s);
-    }
-    st_.wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
+
+  int64_t pool_used() const { return (int64_t)E.pool.used(); }
 
 private:
   Engine &E;
-  std::vector<MineJob> &jobs_;
   const MineOptions &wo_;
   MineStats &st_;
-  std::vector<JobState> js_;
-  std::vector<PNode> stack_;
-  bool mat_pending_ = false;
-  long long wanted_rec_ = 0;  // record capacity to have before the next wave (after an overflow)
+  int nctx_ = 2;
+  Flight fl_[2];
+  uint64_t seq_ = 0;
+  std::vector<std::unique_ptr<JobState>> jobs_;
+  std::vector<int32_t> order_;   // unfinished jobs, oldest first
+  std::vector<int32_t> done_;
+  std::vector<Database *> dbs_;
+  std::vector<DevDB> tab_;
+  int64_t active_ = 0;
+  int64_t stacked_ = 0;          // nodes on all jobs' stacks
+  int64_t seen_bytes_[2] = { 0, 0 };
 
   void h2d(void *dst, const void *src, size_t n)
   {
@@ -754,68 +907,91 @@ private:
     CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, E.stream));
     st_.d2h_bytes += (int64_t)n;
   }
-
-  // device error flag of the kernels' consistency checks (slot 3 of the counters)
+  // device consistency flags (slot 3 of the counters)
   unsigned int *err_flag() { return reinterpret_cast<unsigned int *>(E.d_bytes.p + 3); }
-  void check_err()
+  static void check_flags(unsigned long long v)
   {
-    unsigned long long v = 0;
-    CK(cudaMemcpyAsync(&v, E.d_bytes.p + 3, sizeof(v), cudaMemcpyDeviceToHost, E.stream));
-    CK(cudaStreamSynchronize(E.stream));
     if(v) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(v) + ")");
   }
 
-  void flush_timing()
+  // releases a node's columns and graph ranks
+  void drop_node(JobState &S, PNode &p)
   {
-    if(mat_pending_) {
-      CK(cudaEventSynchronize(E.ev[5]));
-      st_.mat_ms += ms_between(E.ev[4], E.ev[5]);
-      mat_pending_ = false;
+    for(int32_t id : p.cols) S.live_bytes -= E.unref(id);
+    S.live_bytes -= p.nrows * (int64_t)sizeof(int32_t);
+    E.block_unref(p.gord_blk);
+    S.pending--;
+  }
+
+  void complete(int32_t id)
+  {
+    JobState &S = *jobs_[id];
+    S.done = true;
+    active_--;
+    order_.erase(std::find(order_.begin(), order_.end(), id));
+    done_.push_back(id);
+    if(!S.cancelled) {
+      ScopeMs t(st_.host_emit_ms);
+      S.patterns = (int64_t)S.pats.size();
+      st_.patterns += S.patterns;
+      emit(S);
     }
+    std::vector<PatternRec>().swap(S.pats);
+    std::vector<int32_t>().swap(S.roots);
   }
 
   // ---- root level: all frequent 1-edge codes of one job
-  void root_phase(int32_t j)
+  void root_phase(int32_t id)
   {
-    JobState &S = js_[j];
-    Database &db = *S.job->db;
+    JobState &S = *jobs_[id];
+    Database &db = *S.job.db;
+    WaveCtx &X = E.rootc;
     const int32_t words = words_for(db.host.n_graphs);
     const int32_t R = db.root_keys;
     if(R == 0) return;
+    // the pinned mirrors below were last read by the previous root phase's copies
+    CK(cudaEventSynchronize(X.ev[5]));
     const size_t nw = (size_t)R * words;
-    E.d_bm.ensure(nw);
-    E.d_bmx.ensure(nw);
-    E.d_cnt.ensure(R);
-    E.d_sup.ensure(R);
-    E.d_childmap.ensure(R);
+    X.d_bm.ensure(nw);
+    X.d_bmx.ensure(nw);
+    X.d_cnt.ensure(R);
+    X.d_sup.ensure(R);
+    X.d_childmap.ensure(R);
     // pseudo node spanning the root keys, for the support kernel
     NodeDesc nd{};
     nd.words = words;
     nd.nkeys = R;
-    E.d_desc.ensure(sizeof(NodeDesc));
-    E.h_desc.ensure(sizeof(NodeDesc));
-    std::memcpy(E.h_desc.p, &nd, sizeof(nd));
-    h2d(E.d_desc.p, E.h_desc.p, sizeof(nd));
-    CK(cudaMemsetAsync(E.d_bm.p, 0, nw * 4, E.stream));
-    CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)R * 4, E.stream));
-    CK(cudaEventRecord(E.ev[0], E.stream));
-    launch_root_count(db.dev, db.d_root_off, E.d_bm.p, E.d_cnt.p, words, E.d_bytes.p + 2, E.stream);
-    launch_support((const NodeDesc *)E.d_desc.p, 1, R, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
-    CK(cudaEventRecord(E.ev[1], E.stream));
+    X.d_desc.ensure(sizeof(NodeDesc));
+    X.h_desc.ensure(sizeof(NodeDesc));
+    std::memcpy(X.h_desc.p, &nd, sizeof(nd));
+    h2d(X.d_desc.p, X.h_desc.p, sizeof(nd));
+    CK(cudaMemsetAsync(X.d_bm.p, 0, nw * 4, E.stream));
+    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)R * 4, E.stream));
+    CK(cudaEventRecord(X.ev[0], E.stream));
+    launch_root_count(db.dev, db.d_root_off, X.d_bm.p, X.d_cnt.p, words, E.d_bytes.p + 2, E.stream);
+    launch_support((const NodeDesc *)X.d_desc.p, 1, R, X.d_bm.p, X.d_bmx.p, X.d_sup.p, E.stream);
+    CK(cudaEventRecord(X.ev[1], E.stream));
     st_.launches += 2;
-    E.h_sup.ensure(R);
-    E.h_cnt.ensure(R);
-    d2h(E.h_sup.p, E.d_sup.p, (size_t)R * 4);
-    d2h(E.h_cnt.p, E.d_cnt.p, (size_t)R * 4);
-    CK(cudaStreamSynchronize(E.stream));
+    X.h_sup.ensure(R);
+    X.h_cnt.ensure(R);
+    d2h(X.h_sup.p, X.d_sup.p, (size_t)R * 4);
+    d2h(X.h_cnt.p, X.d_cnt.p, (size_t)R * 4);
+    d2h(X.h_misc.p + 1, E.d_bytes.p + 3, sizeof(unsigned long long));
+    CK(cudaEventRecord(X.ev[3], E.stream));
+    {
+      const clk::time_point t0 = clk::now();
+      CK(cudaEventSynchronize(X.ev[3]));
+      st_.host_wait_ms += ms_since(t0);
+    }
     CK(cudaGetLastError());
-    st_.root_ms += ms_between(E.ev[0], E.ev[1]);
+    check_flags(X.h_misc.p[1]);
+    st_.root_ms += ms_between(X.ev[0], X.ev[1]);
 
-    const bool extend = S.job->opt.max_edges != 1;
+    const bool extend = S.job.opt.max_edges != 1;
     std::vector<ChildOut> outs;
     std::vector<PNode> made;
-    E.h_childmap.ensure(R);
-    for(int32_t i = 0; i < R; i++) E.h_childmap.p[i] = -1;
+    X.h_childmap.ensure(R);
+    for(int32_t i = 0; i < R; i++) X.h_childmap.p[i] = -1;
     // frequent roots of this job (and partition), in the reference's order
     struct Sel { int32_t key, pid; DFS d; int32_t sup; int64_t n; };
     std::vector<Sel> sel;
@@ -826,17 +1002,17 @@ private:
         const int32_t el = db.pairs[fl][p].first, tl = db.pairs[fl][p].second;
         if(tl < fl) continue;
         const int32_t key = db.root_off[fl] + (int32_t)p;
-        const int32_t sup = E.h_sup.p[key];
-        if(sup < S.job->minsup) continue;
+        const int32_t sup = X.h_sup.p[key];
+        if(sup < S.job.minsup) continue;
         // root-subtree partition: independent subtrees, no exchange between parts
         const int32_t ri = root_index++;
-        if(S.job->opt.root_parts > 1 && ri % S.job->opt.root_parts != S.job->opt.root_part) continue;
+        if(S.job.opt.root_parts > 1 && ri % S.job.opt.root_parts != S.job.opt.root_part) continue;
         PatternRec pr{ -1, DFS{ 0, 1, fl, el, tl }, sup, {} };
         S.pats.push_back(pr);
         const int32_t pid = (int32_t)S.pats.size() - 1;
         S.roots.push_back(pid);
         if(!extend) continue;
-        const int64_t n = E.h_cnt.p[key];
+        const int64_t n = X.h_cnt.p[key];
         sel.push_back(Sel{ key, pid, pr.edge, sup, n });
         bytes += 2 * Carver::round((size_t)n * 8) + Carver::round((size_t)n * 4);
       }
@@ -850,10 +1026,10 @@ private:
         int2 *c0 = cv.take<int2>(s.n);
         int32_t *gord = cv.take<int32_t>(s.n);
         ChildOut o{ c1, c0, gord, 2, (int32_t)s.n };
-        E.h_childmap.p[s.key] = (int32_t)outs.size();
+        X.h_childmap.p[s.key] = (int32_t)outs.size();
         outs.push_back(o);
         PNode nn;
-        nn.job = j;
+        nn.job = id;
         nn.pattern = s.pid;
         nn.code = { s.d };
         nn.cols = { E.new_col(c0, s.n, blk), E.new_col(c1, s.n, blk) };
@@ -862,53 +1038,70 @@ private:
         E.block_ref(blk);
         nn.nrows = s.n;
         nn.support = s.sup;
+        S.live_bytes += s.n * (int64_t)(2 * sizeof(int2) + sizeof(int32_t));
         made.push_back(std::move(nn));
       }
+      S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
     }
     if(!outs.empty()) {
-      E.d_outs.ensure(outs.size());
-      E.d_cursor.ensure(outs.size());
-      E.h_outs.ensure(outs.size());
-      std::memcpy(E.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
-      h2d(E.d_outs.p, E.h_outs.p, sizeof(ChildOut) * outs.size());
-      h2d(E.d_childmap.p, E.h_childmap.p, (size_t)R * 4);
-      CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
-      launch_root_materialize(db.dev, db.d_root_off, E.d_bm.p, E.d_bmx.p, words, E.d_childmap.p, E.d_cursor.p,
-                              E.d_outs.p, err_flag(), E.stream);
+      X.d_outs.ensure(outs.size());
+      X.d_cursor.ensure(outs.size());
+      X.h_outs.ensure(outs.size());
+      std::memcpy(X.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
+      h2d(X.d_outs.p, X.h_outs.p, sizeof(ChildOut) * outs.size());
+      h2d(X.d_childmap.p, X.h_childmap.p, (size_t)R * 4);
+      CK(cudaMemsetAsync(X.d_cursor.p, 0, outs.size() * 4, E.stream));
+      launch_root_materialize(db.dev, db.d_root_off, X.d_bm.p, X.d_bmx.p, words, X.d_childmap.p, X.d_cursor.p,
+                              X.d_outs.p, err_flag(), E.stream);
       st_.launches++;
-      // the pinned childmap/outs mirrors are rewritten by the next phase:
-      // wait for the copies (and the kernel) before reusing them
-      CK(cudaStreamSynchronize(E.stream));
-      CK(cudaGetLastError());
-      check_err();
     }
-    for(auto it = made.rbegin(); it != made.rend(); ++it) stack_.push_back(std::move(*it));
+    CK(cudaEventRecord(X.ev[5], E.stream));
+    S.pending += (int64_t)made.size();
+    stacked_ += (int64_t)made.size();
+    for(auto it = made.rbegin(); it != made.rend(); ++it) S.stack.push_back(std::move(*it));
   }
 
-  // ---- one wave of DFS-tree nodes
-  void wave()
+  // ---- launch one wave into context c: descriptors, count, support, results copy
+  void launch(int c, bool other_busy)
   {
-    using clk = std::chrono::steady_clock;
     const clk::time_point t_begin = clk::now();
-    std::vector<PNode> nodes;
-    std::vector<NodeLayout> lays;
+    WaveCtx &X = E.ctx[c];
+    Flight &f = fl_[c];
+    if(stacked_ == 0) return;
+    // with the other context idle take half of what is queued, so that both
+    // contexts have work and the host's half overlaps the GPU's
+    int64_t limit = std::max(1, wo_.wave_nodes);
+    if(nctx_ > 1 && !other_busy) limit = std::max<int64_t>(1, std::min<int64_t>(limit, (stacked_ + 1) / 2));
+    std::vector<PNode> &nodes = f.nodes;
+    std::vector<NodeLayout> &lays = f.lays;
+    nodes.clear();
+    lays.clear();
     int64_t rows = 0, words = 0;
-    int32_t keys = 0;
-    while(!stack_.empty() && (int32_t)nodes.size() < std::max(1, wo_.wave_nodes)) {
-      PNode &top = stack_.back();
-      NodeLayout L;
-      layout_node(top, *js_[top.job].job->db, L);
-      const int32_t nk = layout_nkeys(L, *js_[top.job].job->db);
-      const int64_t w = (int64_t)nk * words_for(top.support);
-      if(!nodes.empty() && (rows + top.nrows > wo_.wave_rows || words + w > wo_.wave_words)) break;
-      rows += top.nrows;
-      words += w;
-      keys += nk;
-      lays.push_back(std::move(L));
-      nodes.push_back(std::move(top));
-      stack_.pop_back();
+    bool full = false;
+    for(size_t oi = 0; oi < order_.size() && !full; oi++) {
+      JobState &S = *jobs_[order_[oi]];
+      const Database &db = *S.job.db;
+      while(!S.stack.empty() && (int64_t)nodes.size() < limit) {
+        PNode &top = S.stack.back();
+        NodeLayout L;
+        layout_node(top, db, L);
+        const int32_t nk = layout_nkeys(L, db);
+        const int64_t w = (int64_t)nk * words_for(top.support);
+        if(!nodes.empty() && (rows + top.nrows > wo_.wave_rows || words + w > wo_.wave_words)) {
+          full = true;
+          break;
+        }
+        rows += top.nrows;
+        words += w;
+        lays.push_back(std::move(L));
+        nodes.push_back(std::move(top));
+        S.stack.pop_back();
+        stacked_--;
+      }
+      if((int64_t)nodes.size() >= limit) full = true;
     }
     const int32_t W = (int32_t)nodes.size();
+    if(W == 0) return;
     st_.waves++;
     st_.nodes += W;
     st_.rows += rows;
@@ -920,12 +1113,11 @@ private:
       tot_slots += (int32_t)lays[n].slots.size();
     }
     size_t off = 0;
-    char *hb = nullptr;
     size_t need = 256 * 6 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
                   2 * sizeof(int32_t) * tot_cols;
-    E.h_desc.ensure(need);
-    E.d_desc.ensure(need);
-    hb = E.h_desc.p;
+    X.h_desc.ensure(need);
+    X.d_desc.ensure(need);
+    char *hb = X.h_desc.p;
     NodeDesc *hn = carve<NodeDesc>(hb, off, W);
     const int2 **hc = carve<const int2 *>(hb, off, tot_cols);
     SlotDesc *hs = carve<SlotDesc>(hb, off, tot_slots);
@@ -939,7 +1131,8 @@ private:
     for(int32_t n = 0; n < W; n++) {
       const PNode &p = nodes[n];
       const NodeLayout &L = lays[n];
-      const Database &db = *js_[p.job].job->db;
+      const JobState &S = *jobs_[p.job];
+      const Database &db = *S.job.db;
       NodeDesc &d = hn[n];
       d = NodeDesc{};
       d.row_begin = rb;
@@ -956,11 +1149,11 @@ private:
       d.words = words_for(p.support);
       d.key_base = kb;
       d.nkeys = layout_nkeys(L, db);
-      d.db = js_[p.job].db_slot;
-      for(size_t c = 0; c < p.cols.size(); c++) {
-        hc[co + c] = E.cols[p.cols[c]].ptr;
-        hl[co + c] = (int32_t)E.cols[p.cols[c]].n;
-        hv[co + c] = -1;
+      d.db = S.db_slot;
+      for(size_t cc = 0; cc < p.cols.size(); cc++) {
+        hc[co + cc] = E.cols[p.cols[cc]].ptr;
+        hl[co + cc] = (int32_t)E.cols[p.cols[cc]].n;
+        hv[co + cc] = -1;
       }
       for(size_t s = 0; s < L.slots.size(); s++) {
         hs[so + s] = L.slots[s];
@@ -975,108 +1168,135 @@ private:
       bb += (int64_t)d.nkeys * d.words;
       kb += d.nkeys;
     }
-    char *db_ = E.d_desc.p;
-    const NodeDesc *dn = (const NodeDesc *)(db_ + ((char *)hn - hb));
-    const int2 *const *dc = (const int2 *const *)(db_ + ((char *)hc - hb));
-    const SlotDesc *ds = (const SlotDesc *)(db_ + ((char *)hs - hb));
-    const int32_t *dv = (const int32_t *)(db_ + ((char *)hv - hb));
-    const int32_t *dl = (const int32_t *)(db_ + ((char *)hl - hb));
-    E.d_bm.ensure(std::max<int64_t>(bb, 1));
-    E.d_bmx.ensure(std::max<int64_t>(bb, 1));
-    E.d_cnt.ensure(std::max(kb, 1));
-    E.d_sup.ensure(std::max(kb, 1));
-    E.d_childmap.ensure(std::max(kb, 1));
-    h2d(E.d_desc.p, hb, desc_bytes);
-    CK(cudaMemsetAsync(E.d_bm.p, 0, (size_t)bb * 4, E.stream));
-    CK(cudaMemsetAsync(E.d_cnt.p, 0, (size_t)kb * 4, E.stream));
-    // records: sized from the adjacency entries the wave can scan at most is
-    // unknown up front, so keep the largest count seen (grown after an overflow)
-    int4 *rec = nullptr;
-    long long rec_cap = 0;
-    if(E.rec_enabled && wanted_rec_ > (long long)E.d_rec.cap) {
-      // grow after an overflow; past 2^28 records (4 GiB) or when the device
-      // has no room, keep the enumeration-based materialise instead
-      if(wanted_rec_ > (1ll << 28)) E.rec_enabled = false;
+    char *db_ = X.d_desc.p;
+    f.hn = hn;
+    f.dn = (const NodeDesc *)(db_ + ((char *)hn - hb));
+    f.dc = (const int2 *const *)(db_ + ((char *)hc - hb));
+    f.ds = (const SlotDesc *)(db_ + ((char *)hs - hb));
+    f.dv = (const int32_t *)(db_ + ((char *)hv - hb));
+    f.dl = (const int32_t *)(db_ + ((char *)hl - hb));
+    f.W = W;
+    f.kb = kb;
+    f.kmax = kmax;
+    f.small = small;
+    f.tb = tb;
+    X.d_bm.ensure(std::max<int64_t>(bb, 1));
+    X.d_bmx.ensure(std::max<int64_t>(bb, 1));
+    X.d_cnt.ensure(std::max(kb, 1));
+    X.d_sup.ensure(std::max(kb, 1));
+    X.d_childmap.ensure(std::max(kb, 1));
+    h2d(X.d_desc.p, hb, desc_bytes);
+    CK(cudaMemsetAsync(X.d_bm.p, 0, (size_t)bb * 4, E.stream));
+    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)kb * 4, E.stream));
+    // records: how many the wave appends is not known up front, so keep the
+    // largest count seen (grown after an overflow)
+    f.rec = nullptr;
+    f.rec_cap = 0;
+    if(X.rec_enabled && X.wanted_rec > (long long)X.d_rec.cap) {
+      // past 2^28 records (4 GiB) or when the device has no room, keep the
+      // enumeration-based materialise instead
+      if(X.wanted_rec > (1ll << 28)) X.rec_enabled = false;
       else {
         try {
-          E.d_rec.ensure((size_t)wanted_rec_);
+          X.d_rec.ensure((size_t)X.wanted_rec);
         } catch(const Error &) {
           cudaGetLastError();
-          E.rec_enabled = false;
+          X.rec_enabled = false;
         }
       }
     }
-    if(E.rec_enabled) {
-      E.d_recn.ensure(1);
-      E.h_recn.ensure(1);
-      if(E.d_rec.cap == 0) E.d_rec.ensure((size_t)1 << 22);
-      rec = E.d_rec.p;
-      rec_cap = (long long)E.d_rec.cap;
-      CK(cudaMemsetAsync(E.d_recn.p, 0, sizeof(unsigned long long), E.stream));
+    if(X.rec_enabled) {
+      if(X.d_rec.cap == 0) X.d_rec.ensure((size_t)1 << 22);
+      f.rec = X.d_rec.p;
+      f.rec_cap = (long long)X.d_rec.cap;
+      CK(cudaMemsetAsync(X.d_recn.p, 0, sizeof(unsigned long long), E.stream));
     }
-    CK(cudaEventRecord(E.ev[0], E.stream));
-    launch_wave_count(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_cnt.p, E.d_bytes.p + 0, err_flag(),
-                      rec, rec_cap, rec ? E.d_recn.p : nullptr, E.stream);
-    CK(cudaEventRecord(E.ev[1], E.stream));
-    launch_support(dn, W, kb, E.d_bm.p, E.d_bmx.p, E.d_sup.p, E.stream);
-    CK(cudaEventRecord(E.ev[2], E.stream));
+    CK(cudaEventRecord(X.ev[0], E.stream));
+    launch_wave_count(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, X.d_bm.p, X.d_cnt.p,
+                      E.d_bytes.p + 0, err_flag(), f.rec, f.rec_cap, f.rec ? X.d_recn.p : nullptr, E.stream);
+    CK(cudaEventRecord(X.ev[1], E.stream));
+    launch_support(f.dn, W, kb, X.d_bm.p, X.d_bmx.p, X.d_sup.p, E.stream);
+    CK(cudaEventRecord(X.ev[2], E.stream));
     st_.launches += 2;
-    E.h_sup.ensure(std::max(kb, 1));
-    E.h_cnt.ensure(std::max(kb, 1));
-    d2h(E.h_sup.p, E.d_sup.p, (size_t)kb * 4);
-    d2h(E.h_cnt.p, E.d_cnt.p, (size_t)kb * 4);
-    if(rec) d2h(E.h_recn.p, E.d_recn.p, sizeof(unsigned long long));
-    const clk::time_point t_sync = clk::now();
-    st_.host_build_ms += std::chrono::duration<double, std::milli>(t_sync - t_begin).count();
-    CK(cudaStreamSynchronize(E.stream));
+    X.h_sup.ensure(std::max(kb, 1));
+    X.h_cnt.ensure(std::max(kb, 1));
+    d2h(X.h_sup.p, X.d_sup.p, (size_t)kb * 4);
+    d2h(X.h_cnt.p, X.d_cnt.p, (size_t)kb * 4);
+    if(f.rec) d2h(X.h_misc.p, X.d_recn.p, sizeof(unsigned long long));
+    d2h(X.h_misc.p + 1, E.d_bytes.p + 3, sizeof(unsigned long long));
+    CK(cudaEventRecord(X.ev[3], E.stream));
+    f.busy = true;
+    f.seq = ++seq_;
+    st_.host_build_ms += ms_since(t_begin);
+  }
+
+  // ---- complete the wave in context c: candidates, canonicality, children
+  void finish(int c)
+  {
+    WaveCtx &X = E.ctx[c];
+    Flight &f = fl_[c];
+    {
+      const clk::time_point t0 = clk::now();
+      CK(cudaEventSynchronize(X.ev[3]));
+      st_.host_wait_ms += ms_since(t0);
+    }
     CK(cudaGetLastError());
-    check_err();
-    flush_timing();
+    check_flags(X.h_misc.p[1]);
     const clk::time_point t_ready = clk::now();
-    st_.host_wait_ms += std::chrono::duration<double, std::milli>(t_ready - t_sync).count();
     const double min_before = st_.host_min_ms;
-    st_.count_ms += ms_between(E.ev[0], E.ev[1]);
-    st_.support_ms += ms_between(E.ev[1], E.ev[2]);
+    if(f.mat_pending) {
+      // this context's previous materialise ran before the count just read
+      st_.mat_ms += ms_between(X.ev[4], X.ev[5]);
+      f.mat_pending = false;
+    }
+    st_.count_ms += ms_between(X.ev[0], X.ev[1]);
+    st_.support_ms += ms_between(X.ev[1], X.ev[2]);
+    std::vector<PNode> &nodes = f.nodes;
+    std::vector<NodeLayout> &lays = f.lays;
+    const NodeDesc *hn = f.hn;
+    const int32_t W = f.W, kb = f.kb;
 
     // frequent candidates
     std::vector<Candidate> cands;
     for(int32_t n = 0; n < W; n++) {
       const PNode &p = nodes[n];
-      const Database &db = *js_[p.job].job->db;
+      const JobState &S = *jobs_[p.job];
+      const Database &db = *S.job.db;
       const int32_t base = hn[n].key_base;
+      for(int32_t k = 0; k < hn[n].nkeys; k++) st_.extensions += X.h_cnt.p[base + k];
+      if(S.cancelled) continue;
       for(int32_t k = 0; k < hn[n].nkeys; k++) {
-        st_.extensions += E.h_cnt.p[base + k];
-        if(E.h_sup.p[base + k] < js_[p.job].job->minsup) continue;
-        Candidate c;
-        c.node = n;
-        c.key = k;
-        c.support = E.h_sup.p[base + k];
-        c.cnt = E.h_cnt.p[base + k];
-        c.ok = false;
-        if(!decode_key(lays[n], db, k, c.dfs)) continue;
-        cands.push_back(c);
+        if(X.h_sup.p[base + k] < S.job.minsup) continue;
+        Candidate cd;
+        cd.node = n;
+        cd.key = k;
+        cd.support = X.h_sup.p[base + k];
+        cd.cnt = X.h_cnt.p[base + k];
+        cd.ok = false;
+        if(!decode_key(lays[n], db, k, cd.dfs)) continue;
+        cands.push_back(cd);
       }
     }
     st_.candidates += (int64_t)cands.size();
     // canonicality on the host, in parallel
     {
-      auto t0 = std::chrono::steady_clock::now();
+      const clk::time_point t0 = clk::now();
       E.workers->run((int64_t)cands.size(), [&](int64_t i, int w) {
-        Candidate &c = cands[i];
-        const Code &code = nodes[c.node].code;
+        Candidate &cd = cands[i];
+        const Code &code = nodes[cd.node].code;
         DFS buf[kMaxPatternEdges + 1];
         const size_t n = code.size();
-        if(n + 1 > (size_t)kMaxPatternEdges) { c.ok = false; return; }
+        if(n + 1 > (size_t)kMaxPatternEdges) { cd.ok = false; return; }
         std::copy(code.begin(), code.end(), buf);
-        buf[n] = c.dfs;
-        c.ok = E.checkers[w].is_min(buf, (int)n + 1);
+        buf[n] = cd.dfs;
+        cd.ok = E.checkers[w].is_min(buf, (int)n + 1);
       });
-      st_.host_min_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      st_.host_min_ms += ms_since(t0);
     }
 
     // accepted children: output tree, materialisation slots
-    E.h_childmap.ensure(std::max(kb, 1));
-    for(int32_t i = 0; i < kb; i++) E.h_childmap.p[i] = -1;
+    X.h_childmap.ensure(std::max(kb, 1));
+    for(int32_t i = 0; i < kb; i++) X.h_childmap.p[i] = -1;
     std::vector<ChildOut> outs;
     std::vector<std::vector<PNode>> made(W);
     {
@@ -1091,20 +1311,20 @@ private:
         auto &v = per[n];
         std::sort(v.begin(), v.end(), [&](int32_t a, int32_t b) { return seq_before(cands[a].dfs, cands[b].dfs); });
         PNode &p = nodes[n];
-        JobState &S = js_[p.job];
-        const int32_t max_edges = S.job->opt.max_edges;
+        JobState &S = *jobs_[p.job];
+        const int32_t max_edges = S.job.opt.max_edges;
         for(int32_t ci : v) {
-          const Candidate &c = cands[ci];
-          PatternRec pr{ p.pattern, c.dfs, c.support, {} };
+          const Candidate &cd = cands[ci];
+          PatternRec pr{ p.pattern, cd.dfs, cd.support, {} };
           S.pats.push_back(pr);
           const int32_t pid = (int32_t)S.pats.size() - 1;
           S.pats[p.pattern].children.push_back(pid);
           const int32_t child_edges = (int32_t)p.code.size() + 1;
           if(max_edges > 0 && child_edges >= max_edges) continue;
-          if(child_edges >= kMaxPatternEdges || (c.dfs.is_forward() && c.dfs.to + 1 > 64))
+          if(child_edges >= kMaxPatternEdges || (cd.dfs.is_forward() && cd.dfs.to + 1 > 64))
             throw Error(ST_ERR_LIMIT, "pattern exceeds 64 vertices or 127 edges");
           mats.push_back(Mat{ n, ci, pid });
-          bytes += Carver::round((size_t)c.cnt * 8) + Carver::round((size_t)c.cnt * 4);
+          bytes += Carver::round((size_t)cd.cnt * 8) + Carver::round((size_t)cd.cnt * 4);
         }
       }
       // pass 2: every child's new column and graph ranks carved from one block
@@ -1112,22 +1332,23 @@ private:
         const int32_t blk = E.new_block(bytes);
         Carver cv{ (char *)E.blocks[blk].base };
         for(const Mat &m : mats) {
-          const Candidate &c = cands[m.cand];
+          const Candidate &cd = cands[m.cand];
           PNode &p = nodes[m.node];
-          const int64_t rowsn = c.cnt;
+          JobState &S = *jobs_[p.job];
+          const int64_t rowsn = cd.cnt;
           int2 *col = cv.take<int2>(rowsn);
           int32_t *gord = cv.take<int32_t>(rowsn);
-          ChildOut o{ col, nullptr, gord, c.dfs.is_forward() ? 0 : 1, (int32_t)rowsn };
-          E.h_childmap.p[hn[m.node].key_base + c.key] = (int32_t)outs.size();
+          ChildOut o{ col, nullptr, gord, cd.dfs.is_forward() ? 0 : 1, (int32_t)rowsn };
+          X.h_childmap.p[hn[m.node].key_base + cd.key] = (int32_t)outs.size();
           outs.push_back(o);
           PNode nn;
           nn.job = p.job;
           nn.pattern = m.pid;
           nn.code.reserve(p.code.size() + 1);
           nn.code = p.code;
-          nn.code.push_back(c.dfs);
+          nn.code.push_back(cd.dfs);
           // forward children append a column, backward children replace the last
-          const size_t keep = c.dfs.is_forward() ? p.cols.size() : p.cols.size() - 1;
+          const size_t keep = cd.dfs.is_forward() ? p.cols.size() : p.cols.size() - 1;
           nn.cols.reserve(keep + 1);
           nn.cols.assign(p.cols.begin(), p.cols.begin() + keep);
           for(int32_t id : nn.cols) E.ref(id);
@@ -1136,68 +1357,82 @@ private:
           nn.gord_blk = blk;
           E.block_ref(blk);
           nn.nrows = rowsn;
-          nn.support = c.support;
+          nn.support = cd.support;
+          S.live_bytes += rowsn * (int64_t)(sizeof(int2) + sizeof(int32_t));
+          S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
           made[m.node].push_back(std::move(nn));
         }
       }
     }
     if(!outs.empty()) {
-      E.d_outs.ensure(outs.size());
-      E.d_cursor.ensure(outs.size());
-      E.h_outs.ensure(outs.size());
-      std::memcpy(E.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
-      h2d(E.d_outs.p, E.h_outs.p, sizeof(ChildOut) * outs.size());
-      h2d(E.d_childmap.p, E.h_childmap.p, (size_t)kb * 4);
-      CK(cudaMemsetAsync(E.d_cursor.p, 0, outs.size() * 4, E.stream));
-      CK(cudaEventRecord(E.ev[4], E.stream));
-      const long long nrec = rec ? (long long)E.h_recn.p[0] : -1;
-      if(rec && nrec <= rec_cap) {
+      X.d_outs.ensure(outs.size());
+      X.d_cursor.ensure(outs.size());
+      X.h_outs.ensure(outs.size());
+      std::memcpy(X.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
+      h2d(X.d_outs.p, X.h_outs.p, sizeof(ChildOut) * outs.size());
+      h2d(X.d_childmap.p, X.h_childmap.p, (size_t)kb * 4);
+      CK(cudaMemsetAsync(X.d_cursor.p, 0, outs.size() * 4, E.stream));
+      CK(cudaEventRecord(X.ev[4], E.stream));
+      const long long nrec = f.rec ? (long long)X.h_misc.p[0] : -1;
+      if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
-        E.h_keyword.ensure(std::max(kb, 1));
-        E.d_keyword.ensure(std::max(kb, 1));
+        X.h_keyword.ensure(std::max(kb, 1));
+        X.d_keyword.ensure(std::max(kb, 1));
         for(int32_t n = 0; n < W; n++)
           for(int32_t k2 = 0; k2 < hn[n].nkeys; k2++)
-            E.h_keyword.p[hn[n].key_base + k2] = hn[n].bm_base + (long long)k2 * hn[n].words;
-        h2d(E.d_keyword.p, E.h_keyword.p, sizeof(long long) * (size_t)kb);
-        launch_materialize_records(rec, nrec, E.d_childmap.p, E.d_keyword.p, E.d_bm.p, E.d_bmx.p, E.d_cursor.p,
-                                   E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
+            X.h_keyword.p[hn[n].key_base + k2] = hn[n].bm_base + (long long)k2 * hn[n].words;
+        h2d(X.d_keyword.p, X.h_keyword.p, sizeof(long long) * (size_t)kb);
+        launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, X.d_bm.p, X.d_bmx.p, X.d_cursor.p,
+                                   X.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
       } else {
         // records overflowed (or are disabled): enumerate again
-        launch_wave_materialize(dn, W, tb, kmax, small, dc, dl, ds, dv, E.d_dbs.p, E.d_bm.p, E.d_bmx.p,
-                                E.d_childmap.p, E.d_cursor.p, E.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
-        if(rec) wanted_rec_ = std::max<long long>(wanted_rec_, nrec + nrec / 4);
+        launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, X.d_bm.p,
+                                X.d_bmx.p, X.d_childmap.p, X.d_cursor.p, X.d_outs.p, E.d_bytes.p + 1, err_flag(),
+                                E.stream);
+        if(f.rec) X.wanted_rec = std::max<long long>(X.wanted_rec, nrec + nrec / 4);
       }
-      CK(cudaEventRecord(E.ev[5], E.stream));
+      CK(cudaEventRecord(X.ev[5], E.stream));
       st_.launches++;
-      mat_pending_ = true;
+      f.mat_pending = true;
     }
     // the parents are done: drop their column references and graph ranks
     // (stream order keeps the materialise kernel ahead of any reuse)
+    std::vector<int32_t> touched;
     for(auto &p : nodes) {
-      for(int32_t id : p.cols) E.unref(id);
-      E.block_unref(p.gord_blk);
+      JobState &S = *jobs_[p.job];
+      drop_node(S, p);
+      if(touched.empty() || touched.back() != p.job) touched.push_back(p.job);
     }
-    for(int32_t n = W - 1; n >= 0; n--)
-      for(auto it = made[n].rbegin(); it != made[n].rend(); ++it) stack_.push_back(std::move(*it));
-    st_.host_select_ms += std::chrono::duration<double, std::milli>(clk::now() - t_ready).count() -
-                          (st_.host_min_ms - min_before);
+    for(int32_t n = W - 1; n >= 0; n--) {
+      JobState &S = *jobs_[nodes[n].job];
+      for(auto it = made[n].rbegin(); it != made[n].rend(); ++it) S.stack.push_back(std::move(*it));
+      S.pending += (int64_t)made[n].size();
+      stacked_ += (int64_t)made[n].size();
+    }
+    nodes.clear();
+    lays.clear();
+    f.busy = false;
+    st_.host_select_ms += ms_since(t_ready) - (st_.host_min_ms - min_before);
+    std::sort(touched.begin(), touched.end());
+    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+    for(int32_t id : touched)
+      if(!jobs_[id]->done && jobs_[id]->pending == 0) complete(id);
   }
 
   // pre-order traversal of a job's pattern tree, codes in the caller's labels
   void emit(JobState &S)
   {
-    const MineJob &j = *S.job;
-    st_.patterns += (int64_t)S.pats.size();
+    const MineJob &j = S.job;
     if(!j.emit) return;
     const LabelMap &lm = j.db->labels;
-    std::vector<DFS> path, styled;
+    std::vector<DFS> path, styled, orig;
     std::vector<int32_t> flat;
     struct Frame { int32_t pat; size_t next; };
     std::vector<Frame> st;
     auto out = [&](int32_t pid) {
       const size_t n = path.size();
       styled.resize(n);
-      std::vector<DFS> orig(n);
+      orig.resize(n);
       for(size_t i = 0; i < n; i++) {
         orig[i] = path[i];
         orig[i].fromlabel = lm.vlabel_of[path[i].fromlabel];
@@ -1220,13 +1455,13 @@ private:
       out(r);
       st.assign(1, Frame{ r, 0 });
       while(!st.empty()) {
-        Frame &f = st.back();
-        const auto &ch = S.pats[f.pat].children;
-        if(f.next < ch.size()) {
-          const int32_t c = ch[f.next++];
-          path.push_back(S.pats[c].edge);
-          out(c);
-          st.push_back(Frame{ c, 0 });
+        Frame &fr = st.back();
+        const auto &ch = S.pats[fr.pat].children;
+        if(fr.next < ch.size()) {
+          const int32_t cc = ch[fr.next++];
+          path.push_back(S.pats[cc].edge);
+          out(cc);
+          st.push_back(Frame{ cc, 0 });
         } else {
           st.pop_back();
           path.pop_back();
@@ -1235,6 +1470,16 @@ private:
     }
   }
 };
+
+// failure cleanup: finish queued work, drop pooled memory
+void engine_fail(Engine &e)
+{
+  if(e.ready) {
+    cudaStreamSynchronize(e.stream);
+    cudaGetLastError();
+    e.destroy();
+  }
+}
 
 }  // namespace
 
@@ -1252,28 +1497,77 @@ int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats 
                                                  " is greater then the database size " +
                                                  std::to_string(j.db->host.n_graphs));
     }
+    const clk::time_point t0 = clk::now();
     g_engine.init(wave_opt.threads);
-    Runner r(g_engine, jobs, wave_opt, st);
-    r.run();
+    Sched s(g_engine, wave_opt, st);
+    for(auto &j : jobs) s.add(j);
+    while(!s.idle()) s.step();
+    s.sync_stats();
+    st.wall_ms += ms_since(t0);
   } catch(const Error &e) {
     err = e.what();
-    // leave the engine usable: finish queued work, drop pooled memory
-    if(g_engine.ready) {
-      cudaStreamSynchronize(g_engine.stream);
-      cudaGetLastError();
-      g_engine.destroy();
-    }
+    engine_fail(g_engine);
     return e.code;
   } catch(const std::exception &e) {
     err = e.what();
-    if(g_engine.ready) {
-      cudaStreamSynchronize(g_engine.stream);
-      cudaGetLastError();
-      g_engine.destroy();
-    }
+    engine_fail(g_engine);
     return ST_ERR_STATE;
   }
   return ST_OK;
+}
+
+// ------------------------------------------------------------ public scheduler
+
+struct Scheduler::Impl {
+  Engine eng;
+  MineOptions wo;
+  MineStats st;
+  std::unique_ptr<Sched> s;
+};
+
+Scheduler::Scheduler(const MineOptions &wave_opt, int64_t pool_bytes) : p_(new Impl())
+{
+  p_->wo = wave_opt;
+  p_->eng.pool_limit = pool_bytes;
+  reset();
+}
+
+Scheduler::~Scheduler()
+{
+  if(!p_) return;
+  p_->s.reset();
+  p_->eng.destroy();
+}
+
+void Scheduler::reset()
+{
+  p_->s.reset();
+  engine_fail(p_->eng);
+  p_->eng.init(p_->wo.threads);
+  p_->s.reset(new Sched(p_->eng, p_->wo, p_->st));
+}
+
+int32_t Scheduler::add(const MineJob &job) { return p_->s->add(job); }
+bool Scheduler::idle() const { return p_->s->idle(); }
+void Scheduler::step() { p_->s->step(); }
+void Scheduler::cancel(int32_t id) { p_->s->cancel(id); }
+std::vector<int32_t> Scheduler::take_done() { return p_->s->take_done(); }
+void Scheduler::forget(int32_t id) { p_->s->forget(id); }
+void Scheduler::sync_stats() { p_->s->sync_stats(); }
+MineStats &Scheduler::stats() { return p_->st; }
+int64_t Scheduler::pool_used() const { return p_->s->pool_used(); }
+
+bool Scheduler::job_info(int32_t id, JobInfo &out)
+{
+  JobState *S = p_->s->job(id);
+  if(!S) return false;
+  out.live_bytes = S->live_bytes;
+  out.peak_bytes = S->peak_bytes;
+  out.patterns = S->patterns;
+  out.pending = S->pending;
+  out.done = S->done;
+  out.cancelled = S->cancelled;
+  return true;
 }
 
 int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,

@@ -115,6 +115,44 @@ struct MineJob {
 // Jobs with emit == nullptr still count their patterns in stats.
 int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats *stats, std::string &err);
 
+struct JobInfo {
+  int64_t live_bytes = 0;   // embedding-store bytes held by the job's pending nodes
+  int64_t peak_bytes = 0;
+  int64_t patterns = 0;     // set when the job finished
+  int64_t pending = 0;      // DFS-tree nodes queued or in flight
+  bool done = false;
+  bool cancelled = false;
+};
+
+// A long-lived mining context with its own stream, device pool and scratch.
+// Jobs are added at any time and advance together, wave by wave: each step
+// launches waves of pending DFS-tree nodes (oldest jobs first) and completes
+// the oldest wave in flight.  A job's emit callback runs inside the step that
+// finishes it.  Not thread-safe: one thread drives it.  Errors throw Error;
+// after one, reset() drops every job and the device state.
+class Scheduler {
+public:
+  Scheduler(const MineOptions &wave_opt, int64_t pool_bytes);
+  ~Scheduler();
+  Scheduler(const Scheduler &) = delete;
+  Scheduler &operator=(const Scheduler &) = delete;
+  int32_t add(const MineJob &job);   // validates, mines the root level; returns the job id
+  bool idle() const;                 // no unfinished job
+  void step();
+  void cancel(int32_t id);
+  std::vector<int32_t> take_done();  // jobs finished or cancelled since the last call
+  bool job_info(int32_t id, JobInfo &out);
+  void forget(int32_t id);           // drops a finished job's bookkeeping
+  void sync_stats();                 // folds device counters into stats()
+  MineStats &stats();
+  int64_t pool_used() const;
+  void reset();
+
+private:
+  struct Impl;
+  std::unique_ptr<Impl> p_;
+};
+
 // support[k] = number of distinct graph ids among the records with key k
 // (host arrays; records must satisfy 0 <= key < n_keys, 0 <= graph < n_graphs).
 int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,

@@ -189,6 +189,74 @@ typedef void (*gs_batch_emit_fn)(int32_t db_index, const int32_t *dfs5xN, int32_
 GS_API gs_status gs_mine_batch(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, const gs_mine_opts *opts,
                                gs_batch_emit_fn emit, void *user, gs_mine_stats *stats);
 
+/* ---------------------------------------------------------------- serving
+ * A request loop over resident databases: mining requests (database,
+ * minsup, pattern-size cap) are submitted at any time from any thread and
+ * mined by one server thread with continuous batching.  Requests that arrive
+ * while others are on the GPU are admitted as active slots and embedding-
+ * store memory free up, and their DFS-tree nodes share launches with the
+ * requests already running (oldest first).  Admission charges each request
+ * an embedding-store estimate (the peak seen for the same database, minsup
+ * and cap, else 20 bytes per adjacency entry) against budget_bytes; a
+ * request is always admitted when nothing else runs.  No counterpart in the
+ * reference, which mines one database per process (common_main.cpp:28-80).
+ * A request's result is the same pattern list gs_mine_collect returns. */
+typedef struct gs_server gs_server;
+
+typedef struct gs_server_opts {
+  int64_t budget_bytes; /* embedding-store bytes for admission; 0 = half the free device memory */
+  int64_t pool_bytes;   /* hard cap of the server's device pool; 0 = 70% of free device memory */
+  int32_t max_active;   /* requests mined at once; 0 = 64 */
+  int32_t wave_nodes;   /* DFS-tree nodes per launch; 0 = default */
+  int32_t threads;      /* host threads for the canonicality check; 0 = all cores */
+  int32_t label_style;  /* GS_LABELS_FULL or GS_LABELS_SEQ for the results */
+} gs_server_opts;
+
+enum { GS_REQ_QUEUED = 0, GS_REQ_RUNNING = 1, GS_REQ_DONE = 2, GS_REQ_CANCELLED = 3, GS_REQ_FAILED = 4 };
+
+typedef struct gs_request_info {
+  int32_t state;       /* GS_REQ_* */
+  gs_status status;    /* the error of a failed request, else GS_OK */
+  int64_t patterns;    /* frequent patterns found (when done) */
+  double queue_ms;     /* submission to admission */
+  double latency_ms;   /* submission to completion (when done) */
+  int64_t peak_bytes;  /* embedding-store bytes the request held at its peak */
+} gs_request_info;
+
+typedef struct gs_server_stats {
+  int64_t submitted, completed, cancelled, failed, queued, running;
+  int64_t max_running;     /* most requests mined at once so far */
+  int64_t patterns;        /* over completed requests */
+  double p50_ms, p99_ms, mean_ms;  /* latency of completed requests, nearest rank */
+  double wall_ms;          /* since creation */
+  double busy_ms;          /* time with at least one request admitted */
+  int64_t budget_bytes, reserved_bytes, pool_used_bytes, peak_pool_bytes;
+  int64_t waves, launches;
+} gs_server_stats;
+
+GS_API void gs_server_opts_default(gs_server_opts *opts);
+/* Starts the server thread; the GPU is first touched by the first request. */
+GS_API gs_status gs_server_create(const gs_server_opts *opts, gs_server **out);
+/* Registers a database (borrowed: it must outlive the server).  It is made
+ * resident on the device by the first request that uses it. */
+GS_API gs_status gs_server_add_db(gs_server *srv, gs_db *db, int32_t *db_id);
+/* Queues a request.  minsup is checked now (GS_ERR_MINSUP_TOO_SMALL /
+ * GS_ERR_MINSUP_TOO_LARGE as gs_mine); max_edges 0 = no cap. */
+GS_API gs_status gs_server_submit(gs_server *srv, int32_t db_id, int32_t abs_minsup, int32_t max_edges,
+                                  int64_t *request_id);
+/* Waits up to wait_ms (0 = do not wait, < 0 = until it ends) for the request
+ * to end, then fills info.  Returns GS_ERR_TIMEOUT if it is still queued or
+ * running.  Once it has ended and out is not NULL, *out receives its
+ * patterns (free with gs_patterns_free; NULL unless done) and the request is
+ * forgotten: later calls with its id return GS_ERR_USAGE. */
+GS_API gs_status gs_server_poll(gs_server *srv, int64_t request_id, int32_t wait_ms, gs_request_info *info,
+                                gs_patterns **out);
+/* Cancels a queued or running request (a running one stops at its next wave). */
+GS_API gs_status gs_server_cancel(gs_server *srv, int64_t request_id);
+GS_API gs_status gs_server_get_stats(gs_server *srv, gs_server_stats *stats);
+/* Cancels what is left, stops the thread, frees the server's device memory. */
+GS_API void gs_server_destroy(gs_server *srv);
+
 /* Support of candidate DFS edges from extension records: support[k] = the
  * number of distinct graph ids among the records whose key is k, computed on
  * the GPU with one support bitmap per key.  The GPU form of

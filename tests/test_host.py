@@ -187,3 +187,24 @@ def test_cli_exit_codes(gs):
     assert r.returncode == 2
     r = subprocess.run([gs.CLI_PATH, "txt", db, "0"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     assert r.returncode == 3
+
+
+def test_server_validates_requests_on_the_host(gs):
+    # argument checks need no GPU: nothing is admitted
+    db = gs.Database.load(os.path.join(GOLDEN, "fixture_get_test_database.txt"), "txt")
+    with gs.Server() as srv:
+        d = srv.add_db(db)
+        with pytest.raises(gs.GSpanError) as e:
+            srv.submit(d + 1, 2)
+        assert e.value.status == 1
+        with pytest.raises(gs.GSpanError) as e:
+            srv.submit(d, 0)
+        assert e.value.status == 7
+        with pytest.raises(gs.GSpanError) as e:
+            srv.submit(d, len(db))
+        assert e.value.status == 6
+        with pytest.raises(gs.GSpanError) as e:
+            srv.result(12345, timeout_ms=0)
+        assert e.value.status == 1
+        s = srv.stats()
+        assert s["submitted"] == 0 and s["running"] == 0
