@@ -57,6 +57,10 @@ def parse():
     p.add_argument("--wave-nodes", type=int, default=None)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="mine", choices=["mine", "batch", "serving"],
+                   help="mine: one database (the default line); batch: 64 databases mined together vs one at "
+                        "a time; serving: Poisson request streams against 8 resident databases")
+    p.add_argument("--requests", type=float, default=1.0, help="serving: scale of the request counts")
     return p.parse_args()
 
 
@@ -169,12 +173,153 @@ def cpu_oracle(db_txt, minsup, seconds, cores):
     return pats, elapsed, stopped, wall
 
 
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return r, (time.perf_counter() - t0) * 1000.0
+
+
+def bench_batch(a, g):
+    """64 databases (generator configuration 3, seeds 1000..1063: 1,000-50,000
+    graphs log-uniform, 2-20 vertex and edge labels, 10-40 mean edges) at
+    minsup 5%: all mined in shared waves by one gs_mine_batch call, against the
+    same 64 mined one at a time (batched engine, and the plain one-node-per-
+    launch form).  No pattern output in any arm (patterns are counted)."""
+    import torch
+    dbs = [g.Database.generate(3, seed=1000 + i, scale=a.scale) for i in range(64)]
+    sups = [max(1, int(round(0.05 * len(d)))) for d in dbs]
+    for d in dbs:
+        d.upload()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda:0")
+    for _ in range(max(3, a.warmup)):
+        g.mine_batch(dbs, sups, collect=False)
+    clocks = Clocks()
+    clocks.start()
+    tb, st_b = [], None
+    for _ in range(a.steps):
+        flush.fill_(1)
+        (_, st_b), ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False))
+        tb.append(ms)
+    clk = clocks.stop()
+    pats = st_b["patterns"]
+
+    def one_at_a_time(**kw):
+        tot, n = 0.0, 0
+        for d, s in zip(dbs, sups):
+            flush.fill_(1)
+            (_, st), ms = _timed(lambda: g.mine(d, s, collect=False, **kw))
+            tot += ms
+            n += st["patterns"]
+        return tot, n
+    one_at_a_time()  # warm-up
+    t_solo, n_solo = one_at_a_time()
+    t_plain, n_plain = one_at_a_time(wave_nodes=1)
+    assert n_solo == pats == n_plain, (n_solo, pats, n_plain)
+    ms = sum(tb) / len(tb)
+    line = {"metric": "frequent patterns/sec", "value": pats / (ms / 1000.0), "unit": "patterns/s", "n_gpus": 1,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "batch: 64 databases of generator configuration 3 (seeds 1000-1063), minsup 5%, "
+                                   "one gs_mine_batch call", "graphs": sum(len(d) for d in dbs),
+                       "l2": "flushed between steps (256 MiB write)"},
+            "patterns_per_step": pats,
+            "one_at_a_time": {"ms": t_solo, "patterns_per_s": pats / (t_solo / 1000.0)},
+            "plain_one_at_a_time": {"ms": t_plain, "patterns_per_s": pats / (t_plain / 1000.0)},
+            "speedup_vs_one_at_a_time": t_solo / ms, "speedup_vs_plain": t_plain / ms,
+            "clocks": clk, "gpu_launches": int(st_b["launches"]) * a.steps, "stats_last_step": st_b}
+    print(json.dumps(line))
+
+
+def bench_serving(a, g):
+    """8 resident databases (generator configuration 4, seeds 2000..2007:
+    10,000-200,000 graphs); Poisson request streams at 5, 20, 50 and 200
+    requests/s (seed 7), each request = (database uniform, minsup uniform from
+    1/2/5/10%, max pattern edges uniform 4..8).  Latency = submission to
+    completion; throughput = patterns of the stream / (first submission to
+    last completion).  The same requests are then mined serially, one at a
+    time, by the plain one-node-per-launch form and by the batched engine."""
+    import random
+    dbs = [g.Database.generate(4, seed=2000 + i, scale=a.scale) for i in range(8)]
+    for d in dbs:
+        d.upload()
+    rng = random.Random(7)
+    plan = [(5, 30), (20, 60), (50, 100), (200, 200)]
+    out = {}
+    with g.Server(max_active=64) as srv:
+        ids = [srv.add_db(d) for d in dbs]
+        for i in range(8):  # warm-up
+            srv.result(srv.submit(ids[i], max(1, int(0.1 * len(dbs[i]))), 4), decode=False)
+        clocks = Clocks()
+        clocks.start()
+        last_reqs = None
+        for lam, n in plan:
+            n = max(4, int(n * a.requests))
+            reqs = []
+            for _ in range(n):
+                d = rng.randrange(8)
+                reqs.append((d, max(1, int(round(rng.choice([0.01, 0.02, 0.05, 0.10]) * len(dbs[d])))),
+                             rng.randint(4, 8)))
+            gaps = [rng.expovariate(lam) for _ in range(n)]
+            t0 = time.perf_counter()
+            t, rids = t0, []
+            for (d, s, me), gap in zip(reqs, gaps):
+                t += gap
+                now = time.perf_counter()
+                if t > now:
+                    time.sleep(t - now)
+                rids.append(srv.submit(ids[d], s, me))
+            infos = [srv.result(r, decode=False)[1] for r in rids]
+            wall = time.perf_counter() - t0
+            lat = sorted(i["latency_ms"] for i in infos)
+            rank = lambda q: lat[max(1, int(-(-q * len(lat) // 1))) - 1]  # noqa: E731 nearest rank
+            pats = sum(i["patterns"] for i in infos)
+            out[str(lam)] = {"requests": n, "p50_ms": rank(0.5), "p99_ms": rank(0.99),
+                             "mean_ms": sum(lat) / len(lat), "patterns": pats, "wall_s": wall,
+                             "patterns_per_s": pats / wall, "offered_s": t - t0}
+            last_reqs = reqs
+        clk = clocks.stop()
+        sst = srv.stats()
+
+    def serial(**kw):
+        tot, n = 0.0, 0
+        for d, s, me in last_reqs:
+            (_, st), ms = _timed(lambda: g.mine(dbs[d], s, max_edges=me, collect=False, **kw))
+            tot += ms
+            n += st["patterns"]
+        return tot, n
+    serial()  # warm-up
+    t_b, n_b = serial()
+    t_p, n_p = serial(wave_nodes=1)
+    top = out[str(plan[-1][0])]
+    assert n_b == n_p == top["patterns"], (n_b, n_p, top["patterns"])
+    line = {"metric": "frequent patterns/sec (served)", "value": top["patterns_per_s"], "unit": "patterns/s",
+            "n_gpus": 1, "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic",
+            "config": {"workload": "serving: 8 databases of generator configuration 4 (seeds 2000-2007), Poisson "
+                                   "arrivals (seed 7), minsup 1/2/5/10%, max edges 4-8; value at 200 req/s",
+                       "graphs": [len(d) for d in dbs]},
+            "streams": out,
+            "serial_plain_at_200": {"ms": t_p, "patterns_per_s": n_p / (t_p / 1000.0)},
+            "serial_batched_at_200": {"ms": t_b, "patterns_per_s": n_b / (t_b / 1000.0)},
+            "server": {"max_running": sst["max_running"], "completed": sst["completed"], "waves": sst["waves"],
+                       "peak_pool_bytes": sst["peak_pool_bytes"]},
+            "clocks": clk}
+    print(json.dumps(line))
+
+
 def main():
     a = parse()
     import gpu_graph_mining_gb300 as g
     if not os.path.exists(g.LIB_PATH):
         from gpu_graph_mining_gb300 import build as b
         b.build()
+    if a.workload != "mine" and a.impl == "gb300":
+        if RANK == 0:
+            (bench_batch if a.workload == "batch" else bench_serving)(a, g)
+        return
 
     workload = "config%d: generator configuration %d x%.3g, minsup %.2f%%" % (a.config, a.config, a.scale,
                                                                              100 * a.minsup_frac)
