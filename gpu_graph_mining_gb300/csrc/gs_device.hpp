@@ -55,7 +55,7 @@ struct NodeDesc {
   int32_t key_base;      // first key of the node in the wave's key space
   int32_t nkeys;
   int32_t db;            // index into the resident-database table
-  int32_t pad;
+  int32_t minsup;        // the node's job's minimum support (candidate selection)
 };
 
 // One right-most-path vertex of a node.

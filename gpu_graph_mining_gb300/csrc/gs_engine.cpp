@@ -465,6 +465,15 @@ struct WaveCtx {
   DBuf<int4> d_rec;
   DBuf<unsigned long long> d_recn;
   DBuf<long long> d_keyword;
+  // candidate selection: frequent keys {key, support, embeddings, 0}, and
+  // the (key, child) pairs of the children to materialise
+  DBuf<int4> d_sel;
+  DBuf<int2> d_listed;               // keys with enough embeddings to be counted
+  DBuf<unsigned long long> d_selc;   // [0] selected keys, [1] embeddings of all keys, [2] listed keys
+  DBuf<int2> d_pairs;
+  HBuf<int4> h_sel;
+  HBuf<int2> h_pairs;
+  int64_t sel_hint = 4096;           // selected entries copied back with the wave's results
   bool rec_enabled = true;
   long long wanted_rec = 0;    // record capacity to have before the next wave (after an overflow)
   // pinned host mirrors
@@ -472,7 +481,7 @@ struct WaveCtx {
   HBuf<int32_t> h_sup, h_cnt, h_childmap;
   HBuf<ChildOut> h_outs;
   HBuf<long long> h_keyword;
-  HBuf<unsigned long long> h_misc;  // [0] records written, [1] consistency flags
+  HBuf<unsigned long long> h_misc;  // [0] records written, [1] consistency flags, [2..3] = d_selc
   // 0/1 count, 1/2 support, 3 results copied, 4/5 materialise
   cudaEvent_t ev[6] = {};
   bool have_events = false;
@@ -483,14 +492,17 @@ struct WaveCtx {
       for(auto &e : ev) CK(cudaEventCreate(&e));
       have_events = true;
     }
-    h_misc.ensure(2);
+    h_misc.ensure(4);
     d_recn.ensure(1);
+    d_selc.ensure(3);
   }
   void free()
   {
     d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
-    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free();
+    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free(); d_sel.free(); d_listed.free(); d_selc.free(); d_pairs.free();
     h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free(); h_keyword.free(); h_misc.free();
+    h_sel.free(); h_pairs.free();
+    sel_hint = 4096;
     if(have_events)
       for(auto &e : ev) cudaEventDestroy(e);
     have_events = false;
@@ -503,6 +515,7 @@ constexpr int kMaxDbSlots = 256;   // databases one scheduler keeps in its devic
 
 struct Engine {
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;   // catch-up copies that must not wait for queued waves
   Pool pool;
   std::unique_ptr<Workers> workers;
   std::vector<MinChecker> checkers;
@@ -522,6 +535,7 @@ struct Engine {
     if(!ready) {
       CK(cudaSetDevice(0));
       CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+      CK(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
       d_bytes.ensure(4);
       d_dbs.ensure(kMaxDbSlots);
       CK(cudaMemsetAsync(d_bytes.p, 0, sizeof(unsigned long long) * 4, stream));
@@ -545,6 +559,8 @@ struct Engine {
     d_bytes.free();
     for(auto &c : ctx) c.free();
     rootc.free();
+    cudaStreamSynchronize(aux);
+    cudaStreamDestroy(aux);
     cudaStreamDestroy(stream);
     cols.clear();
     free_cols.clear();
@@ -756,6 +772,7 @@ struct Flight {
   int64_t tb = 0;
   int4 *rec = nullptr;
   long long rec_cap = 0;
+  int64_t sel_copied = 0;    // selected entries copied back with the results
 };
 
 // The wave scheduler.  Jobs join at any time (add) and leave when their last
@@ -1150,6 +1167,7 @@ private:
       d.key_base = kb;
       d.nkeys = layout_nkeys(L, db);
       d.db = S.db_slot;
+      d.minsup = S.job.minsup;
       for(size_t cc = 0; cc < p.cols.size(); cc++) {
         hc[co + cc] = E.cols[p.cols[cc]].ptr;
         hl[co + cc] = (int32_t)E.cols[p.cols[cc]].n;
@@ -1183,8 +1201,10 @@ private:
     X.d_bm.ensure(std::max<int64_t>(bb, 1));
     X.d_bmx.ensure(std::max<int64_t>(bb, 1));
     X.d_cnt.ensure(std::max(kb, 1));
-    X.d_sup.ensure(std::max(kb, 1));
     X.d_childmap.ensure(std::max(kb, 1));
+    X.d_keyword.ensure(std::max(kb, 1));
+    X.d_sel.ensure(std::max(kb, 1));
+    X.d_listed.ensure(std::max(kb, 1));
     h2d(X.d_desc.p, hb, desc_bytes);
     CK(cudaMemsetAsync(X.d_bm.p, 0, (size_t)bb * 4, E.stream));
     CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)kb * 4, E.stream));
@@ -1215,15 +1235,19 @@ private:
     launch_wave_count(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, X.d_bm.p, X.d_cnt.p,
                       E.d_bytes.p + 0, err_flag(), f.rec, f.rec_cap, f.rec ? X.d_recn.p : nullptr, E.stream);
     CK(cudaEventRecord(X.ev[1], E.stream));
-    launch_support(f.dn, W, kb, X.d_bm.p, X.d_bmx.p, X.d_sup.p, E.stream);
+    CK(cudaMemsetAsync(X.d_selc.p, 0, 3 * sizeof(unsigned long long), E.stream));
+    launch_support_select(f.dn, W, kb, X.d_bm.p, X.d_cnt.p, X.d_bmx.p, X.d_childmap.p, X.d_keyword.p, X.d_listed.p,
+                          X.d_sel.p, kb, X.d_selc.p, E.stream);
     CK(cudaEventRecord(X.ev[2], E.stream));
-    st_.launches += 2;
-    X.h_sup.ensure(std::max(kb, 1));
-    X.h_cnt.ensure(std::max(kb, 1));
-    d2h(X.h_sup.p, X.d_sup.p, (size_t)kb * 4);
-    d2h(X.h_cnt.p, X.d_cnt.p, (size_t)kb * 4);
+    st_.launches += 3;
+    // the frequent candidates come back compacted: a prefix sized from earlier
+    // waves, the rest (rarely) by a second copy
+    f.sel_copied = std::min<int64_t>(kb, X.sel_hint);
+    X.h_sel.ensure((size_t)std::max<int64_t>(f.sel_copied, 1));
+    if(f.sel_copied > 0) d2h(X.h_sel.p, X.d_sel.p, sizeof(int4) * (size_t)f.sel_copied);
     if(f.rec) d2h(X.h_misc.p, X.d_recn.p, sizeof(unsigned long long));
     d2h(X.h_misc.p + 1, E.d_bytes.p + 3, sizeof(unsigned long long));
+    d2h(X.h_misc.p + 2, X.d_selc.p, 2 * sizeof(unsigned long long));
     CK(cudaEventRecord(X.ev[3], E.stream));
     f.busy = true;
     f.seq = ++seq_;
@@ -1256,26 +1280,38 @@ private:
     const NodeDesc *hn = f.hn;
     const int32_t W = f.W, kb = f.kb;
 
-    // frequent candidates
+    // frequent candidates (compacted on the device)
+    const int64_t nsel = (int64_t)X.h_misc.p[2];
+    st_.extensions += (int64_t)X.h_misc.p[3];
+    if(nsel > kb) throw Error(ST_ERR_STATE, "candidate selection overflow");
+    if(nsel > f.sel_copied) {
+      // copies the whole list again (growing the pinned buffer drops its
+      // contents) on the side stream: the wave's results are complete, and the
+      // main stream already holds the other context's wave
+      X.h_sel.ensure((size_t)nsel);
+      CK(cudaMemcpyAsync(X.h_sel.p, X.d_sel.p, sizeof(int4) * (size_t)nsel, cudaMemcpyDeviceToHost, E.aux));
+      CK(cudaStreamSynchronize(E.aux));
+      st_.d2h_bytes += (int64_t)sizeof(int4) * nsel;
+    }
+    X.sel_hint = std::max<int64_t>(X.sel_hint, 2 * nsel);
+    std::sort(X.h_sel.p, X.h_sel.p + nsel, [](const int4 &a, const int4 &b) { return a.x < b.x; });
     std::vector<Candidate> cands;
-    for(int32_t n = 0; n < W; n++) {
-      const PNode &p = nodes[n];
-      const JobState &S = *jobs_[p.job];
-      const Database &db = *S.job.db;
-      const int32_t base = hn[n].key_base;
-      for(int32_t k = 0; k < hn[n].nkeys; k++) st_.extensions += X.h_cnt.p[base + k];
+    cands.reserve((size_t)nsel);
+    int32_t n = 0;
+    for(int64_t i = 0; i < nsel; i++) {
+      const int4 e = X.h_sel.p[i];
+      while(n + 1 < W && hn[n + 1].key_base <= e.x) n++;
+      const JobState &S = *jobs_[nodes[n].job];
       if(S.cancelled) continue;
-      for(int32_t k = 0; k < hn[n].nkeys; k++) {
-        if(X.h_sup.p[base + k] < S.job.minsup) continue;
-        Candidate cd;
-        cd.node = n;
-        cd.key = k;
-        cd.support = X.h_sup.p[base + k];
-        cd.cnt = X.h_cnt.p[base + k];
-        cd.ok = false;
-        if(!decode_key(lays[n], db, k, cd.dfs)) continue;
-        cands.push_back(cd);
-      }
+      Candidate cd;
+      cd.node = n;
+      cd.key = e.x - hn[n].key_base;
+      cd.support = e.y;
+      cd.cnt = e.z;
+      cd.ok = false;
+      if(cd.key < 0 || cd.key >= hn[n].nkeys) throw Error(ST_ERR_STATE, "selected key outside its node");
+      if(!decode_key(lays[n], *S.job.db, cd.key, cd.dfs)) continue;
+      cands.push_back(cd);
     }
     st_.candidates += (int64_t)cands.size();
     // canonicality on the host, in parallel
@@ -1295,9 +1331,8 @@ private:
     }
 
     // accepted children: output tree, materialisation slots
-    X.h_childmap.ensure(std::max(kb, 1));
-    for(int32_t i = 0; i < kb; i++) X.h_childmap.p[i] = -1;
     std::vector<ChildOut> outs;
+    std::vector<int2> pairs;
     std::vector<std::vector<PNode>> made(W);
     {
       std::vector<std::vector<int32_t>> per(W);
@@ -1339,7 +1374,7 @@ private:
           int2 *col = cv.take<int2>(rowsn);
           int32_t *gord = cv.take<int32_t>(rowsn);
           ChildOut o{ col, nullptr, gord, cd.dfs.is_forward() ? 0 : 1, (int32_t)rowsn };
-          X.h_childmap.p[hn[m.node].key_base + cd.key] = (int32_t)outs.size();
+          pairs.push_back(make_int2(hn[m.node].key_base + cd.key, (int32_t)outs.size()));
           outs.push_back(o);
           PNode nn;
           nn.job = p.job;
@@ -1370,18 +1405,16 @@ private:
       X.h_outs.ensure(outs.size());
       std::memcpy(X.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
       h2d(X.d_outs.p, X.h_outs.p, sizeof(ChildOut) * outs.size());
-      h2d(X.d_childmap.p, X.h_childmap.p, (size_t)kb * 4);
+      X.d_pairs.ensure(pairs.size());
+      X.h_pairs.ensure(pairs.size());
+      std::memcpy(X.h_pairs.p, pairs.data(), sizeof(int2) * pairs.size());
+      h2d(X.d_pairs.p, X.h_pairs.p, sizeof(int2) * pairs.size());
       CK(cudaMemsetAsync(X.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(X.ev[4], E.stream));
+      launch_scatter_childmap(X.d_pairs.p, (int32_t)pairs.size(), X.d_childmap.p, E.stream);
       const long long nrec = f.rec ? (long long)X.h_misc.p[0] : -1;
       if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
-        X.h_keyword.ensure(std::max(kb, 1));
-        X.d_keyword.ensure(std::max(kb, 1));
-        for(int32_t n = 0; n < W; n++)
-          for(int32_t k2 = 0; k2 < hn[n].nkeys; k2++)
-            X.h_keyword.p[hn[n].key_base + k2] = hn[n].bm_base + (long long)k2 * hn[n].words;
-        h2d(X.d_keyword.p, X.h_keyword.p, sizeof(long long) * (size_t)kb);
         launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, X.d_bm.p, X.d_bmx.p, X.d_cursor.p,
                                    X.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
       } else {
@@ -1392,7 +1425,7 @@ private:
         if(f.rec) X.wanted_rec = std::max<long long>(X.wanted_rec, nrec + nrec / 4);
       }
       CK(cudaEventRecord(X.ev[5], E.stream));
-      st_.launches++;
+      st_.launches += 2;
       f.mat_pending = true;
     }
     // the parents are done: drop their column references and graph ranks

@@ -167,6 +167,93 @@ __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__
   }
 }
 
+// Support of the candidates of one wave, and their selection, in two passes.
+// Screening, one thread per key: a key with fewer embeddings than its node's
+// minsup cannot be found in that many graphs, so only keys with cnt >= minsup
+// are listed for counting; every key with embeddings gets childmap -1
+// (overwritten afterwards for the children that are materialised).
+// Counting, one warp per listed key: popcount of its bitmap with prefix
+// counts for the materialise pass; the frequent keys are appended to sel as
+// {key, support, embeddings, 0} (order unspecified) and get keyword = their
+// first bitmap word.  counters: [0] selected, [1] embeddings of all keys,
+// [2] listed keys.
+__global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restrict__ nodes, int nnodes,
+                                                         int total_keys, const int32_t *__restrict__ cnt,
+                                                         int32_t *childmap, int2 *listed,
+                                                         unsigned long long *counters)
+{
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long ext = 0;
+  // warp-uniform trip count: the list append below is warp-aggregated
+  const long long n32 = ((long long)total_keys + 31) & ~31ll;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n32; i += stride) {
+    const int key = (int)i;
+    const int c = key < total_keys ? cnt[key] : 0;
+    int n = 0;
+    bool cand = false;
+    if(c > 0) {
+      childmap[key] = -1;
+      ext += (unsigned long long)c;
+      n = find_node_by_key(nodes, nnodes, key);
+      cand = c >= nodes[n].minsup;
+    }
+    const unsigned m = __ballot_sync(full, cand);
+    if(m) {
+      unsigned long long at = 0;
+      if(lane == 0) at = atomicAdd(&counters[2], (unsigned long long)__popc(m));
+      at = __shfl_sync(full, at, 0);
+      if(cand) listed[at + __popc(m & lanemask_lt())] = make_int2(key, n);
+    }
+  }
+  for(int o = 16; o > 0; o >>= 1) ext += __shfl_down_sync(full, ext, o);
+  if(lane == 0 && ext) atomicAdd(&counters[1], ext);
+}
+
+__global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restrict__ nodes,
+                                                          const int2 *__restrict__ listed,
+                                                          const uint32_t *__restrict__ bm,
+                                                          const int32_t *__restrict__ cnt, int32_t *bmx,
+                                                          long long *keyword, int4 *sel, int sel_cap,
+                                                          unsigned long long *counters)
+{
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long nlisted = (long long)counters[2];
+  for(long long li = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < nlisted; li += warps) {
+    const int2 kn = listed[li];
+    const NodeDesc &nd = nodes[kn.y];
+    const long long wbase = nd.bm_base + (long long)(kn.x - nd.key_base) * nd.words;
+    int running = 0;
+    for(int w0 = 0; w0 < nd.words; w0 += 32) {
+      const int w = w0 + lane;
+      const int pc = (w < nd.words) ? __popc(bm[wbase + w]) : 0;
+      int incl = pc;
+      for(int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(full, incl, o);
+        if(lane >= o) incl += t;
+      }
+      if(w < nd.words) bmx[wbase + w] = running + incl - pc;
+      running += __shfl_sync(full, incl, 31);
+    }
+    if(lane == 0 && running >= nd.minsup) {
+      keyword[kn.x] = wbase;
+      const unsigned long long at = atomicAdd(&counters[0], 1ull);
+      if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], 0);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter_childmap(const int2 *__restrict__ pairs, int n, int32_t *childmap)
+{
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 p = pairs[i];
+    childmap[p.x] = p.y;
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_records_bitmap(const int32_t *__restrict__ keys,
                                                             const int32_t *__restrict__ gids, long long n, int words,
                                                             uint32_t *bm)
@@ -207,6 +294,22 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 {
   if(n <= 0) return;
   k_records_bitmap<<<grid_for(n), kBlock, 0, s>>>(keys, gids, n, words, bm);
+}
+
+void launch_support_select(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm,
+                           const int32_t *cnt, int32_t *bmx, int32_t *childmap, long long *keyword, int2 *listed,
+                           int4 *sel, int32_t sel_cap, unsigned long long *counters, cudaStream_t s)
+{
+  if(total_keys <= 0) return;
+  k_screen_keys<<<grid_for(((long long)total_keys + 31) / 32 * 32), kBlock, 0, s>>>(nodes, nnodes, total_keys, cnt,
+                                                                                    childmap, listed, counters);
+  k_count_listed<<<152 * 8, kBlock, 0, s>>>(nodes, listed, bm, cnt, bmx, keyword, sel, sel_cap, counters);
+}
+
+void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, cudaStream_t s)
+{
+  if(n <= 0) return;
+  k_scatter_childmap<<<grid_for(n), kBlock, 0, s>>>(pairs, n, childmap);
 }
 
 void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,

@@ -52,6 +52,14 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 
 // One warp per key: support = popcount of the key's bitmap words; bmx gets
 // the exclusive prefix popcount of each word (for graph-rank lookups).
+// Wave support with candidate selection (k_screen_keys, k_count_listed).
+// counters: [0] selected keys, [1] embeddings of all keys, [2] keys listed for
+// counting; listed and sel hold total_keys entries.
+void launch_support_select(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm,
+                           const int32_t *cnt, int32_t *bmx, int32_t *childmap, long long *keyword, int2 *listed,
+                           int4 *sel, int32_t sel_cap, unsigned long long *counters, cudaStream_t s);
+// childmap[pairs[i].x] = pairs[i].y
+void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, cudaStream_t s);
 void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,
                     int32_t *support, cudaStream_t s);
 
