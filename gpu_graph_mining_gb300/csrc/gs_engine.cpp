@@ -404,18 +404,102 @@ struct Column {
   int32_t blk = -1;
 };
 
+// One frequent pattern of a job's output tree; children in traversal order
+// as a linked list.
 struct PatternRec {
   int32_t parent;
   DFS edge;
   int64_t support;
-  std::vector<int32_t> children;
+  int32_t first_child = -1, last_child = -1, next_sibling = -1;
+};
+
+// A vector with room for N elements inline; longer contents move to the
+// heap.  DFS-tree nodes are created and dropped by the hundred thousand per
+// second, and nearly all patterns have few edges and vertices.
+template <class T, int N> class SmallVec {
+public:
+  SmallVec() = default;
+  SmallVec(const SmallVec &o) { assign(o.data(), o.size()); }
+  SmallVec(SmallVec &&o) noexcept { take(o); }
+  SmallVec &operator=(const SmallVec &o)
+  {
+    if(this != &o) assign(o.data(), o.size());
+    return *this;
+  }
+  SmallVec &operator=(SmallVec &&o) noexcept
+  {
+    if(this != &o) {
+      release();
+      take(o);
+    }
+    return *this;
+  }
+  ~SmallVec() { release(); }
+  size_t size() const { return n_; }
+  bool empty() const { return n_ == 0; }
+  T *data() { return heap_ ? heap_ : inl_; }
+  const T *data() const { return heap_ ? heap_ : inl_; }
+  T &operator[](size_t i) { return data()[i]; }
+  const T &operator[](size_t i) const { return data()[i]; }
+  T *begin() { return data(); }
+  T *end() { return data() + n_; }
+  const T *begin() const { return data(); }
+  const T *end() const { return data() + n_; }
+  void reserve(size_t c)
+  {
+    if(c <= cap()) return;
+    T *h = new T[c];
+    std::copy(data(), data() + n_, h);
+    delete[] heap_;
+    heap_ = h;
+    hcap_ = c;
+  }
+  void push_back(const T &v)
+  {
+    if(n_ == cap()) reserve(std::max<size_t>(2 * cap(), N));
+    data()[n_++] = v;
+  }
+  void assign(const T *p, size_t n)
+  {
+    n_ = 0;
+    reserve(n);
+    std::copy(p, p + n, data());
+    n_ = n;
+  }
+
+private:
+  size_t cap() const { return heap_ ? hcap_ : (size_t)N; }
+  void release()
+  {
+    delete[] heap_;
+    heap_ = nullptr;
+    hcap_ = 0;
+    n_ = 0;
+  }
+  void take(SmallVec &o)
+  {
+    n_ = o.n_;
+    if(o.heap_) {
+      heap_ = o.heap_;
+      hcap_ = o.hcap_;
+      o.heap_ = nullptr;
+      o.hcap_ = 0;
+    } else {
+      std::copy(o.inl_, o.inl_ + o.n_, inl_);
+    }
+    o.n_ = 0;
+  }
+  T inl_[N];
+  T *heap_ = nullptr;
+  size_t hcap_ = 0;
+  size_t n_ = 0;
 };
 
 struct PNode {
   int32_t job;
   int32_t pattern;
-  Code code;
-  std::vector<int32_t> cols;
+  SmallVec<DFS, 12> code;
+  SmallVec<int32_t, 12> cols;
   int32_t *gord;
   int32_t gord_blk;
   int64_t nrows;
@@ -636,7 +720,7 @@ inline int32_t words_for(int64_t support) { return (int32_t)((support + 31) / 32
 // Right-most-path slots and key layout of one node (see NodeDesc/SlotDesc).
 void layout_node(const PNode &n, const Database &db, NodeLayout &L)
 {
-  const Code &c = n.code;
+  const auto &c = n.code;
   int rm[kMaxPatternEdges];
   L.nrm = build_rmpath(c.data(), (int)c.size(), rm);
   L.maxtoc = c[rm[0]].to;
@@ -1024,7 +1108,7 @@ private:
         // root-subtree partition: independent subtrees, no exchange between parts
         const int32_t ri = root_index++;
         if(S.job.opt.root_parts > 1 && ri % S.job.opt.root_parts != S.job.opt.root_part) continue;
-        PatternRec pr{ -1, DFS{ 0, 1, fl, el, tl }, sup, {} };
+        PatternRec pr{ -1, DFS{ 0, 1, fl, el, tl }, sup };
         S.pats.push_back(pr);
         const int32_t pid = (int32_t)S.pats.size() - 1;
         S.roots.push_back(pid);
@@ -1048,8 +1132,9 @@ private:
         PNode nn;
         nn.job = id;
         nn.pattern = s.pid;
-        nn.code = { s.d };
-        nn.cols = { E.new_col(c0, s.n, blk), E.new_col(c1, s.n, blk) };
+        nn.code.push_back(s.d);
+        nn.cols.push_back(E.new_col(c0, s.n, blk));
+        nn.cols.push_back(E.new_col(c1, s.n, blk));
         nn.gord = gord;
         nn.gord_blk = blk;
         E.block_ref(blk);
@@ -1090,9 +1175,8 @@ private:
     int64_t limit = std::max(1, wo_.wave_nodes);
     if(nctx_ > 1 && !other_busy) limit = std::max<int64_t>(1, std::min<int64_t>(limit, (stacked_ + 1) / 2));
     std::vector<PNode> &nodes = f.nodes;
-    std::vector<NodeLayout> &lays = f.lays;
+    std::vector<NodeLayout> &lays = f.lays;  // kept between waves: layouts reuse their vectors
     nodes.clear();
-    lays.clear();
     int64_t rows = 0, words = 0;
     bool full = false;
     for(size_t oi = 0; oi < order_.size() && !full; oi++) {
@@ -1100,7 +1184,8 @@ private:
       const Database &db = *S.job.db;
       while(!S.stack.empty() && (int64_t)nodes.size() < limit) {
         PNode &top = S.stack.back();
-        NodeLayout L;
+        if(lays.size() <= nodes.size()) lays.emplace_back();
+        NodeLayout &L = lays[nodes.size()];
         layout_node(top, db, L);
         const int32_t nk = layout_nkeys(L, db);
         const int64_t w = (int64_t)nk * words_for(top.support);
@@ -1110,7 +1195,6 @@ private:
         }
         rows += top.nrows;
         words += w;
-        lays.push_back(std::move(L));
         nodes.push_back(std::move(top));
         S.stack.pop_back();
         stacked_--;
@@ -1319,7 +1403,7 @@ private:
       const clk::time_point t0 = clk::now();
       E.workers->run((int64_t)cands.size(), [&](int64_t i, int w) {
         Candidate &cd = cands[i];
-        const Code &code = nodes[cd.node].code;
+        const auto &code = nodes[cd.node].code;
         DFS buf[kMaxPatternEdges + 1];
         const size_t n = code.size();
         if(n + 1 > (size_t)kMaxPatternEdges) { cd.ok = false; return; }
@@ -1333,27 +1417,38 @@ private:
     // accepted children: output tree, materialisation slots
     std::vector<ChildOut> outs;
     std::vector<int2> pairs;
-    std::vector<std::vector<PNode>> made(W);
+    // children in node order (a node's children are contiguous, from made_at[n])
+    std::vector<PNode> made;
+    std::vector<int32_t> made_at(W + 1, 0);
     {
-      std::vector<std::vector<int32_t>> per(W);
+      // accepted candidates; cands is in key order, so each node's are contiguous
+      std::vector<int32_t> acc;
+      acc.reserve(cands.size());
       for(int32_t i = 0; i < (int32_t)cands.size(); i++)
-        if(cands[i].ok) per[cands[i].node].push_back(i);
+        if(cands[i].ok) acc.push_back(i);
       // pass 1: output tree (reference order) and which children to materialise
       struct Mat { int32_t node, cand, pid; };
       std::vector<Mat> mats;
+      mats.reserve(acc.size());
       size_t bytes = 0;
-      for(int32_t n = 0; n < W; n++) {
-        auto &v = per[n];
-        std::sort(v.begin(), v.end(), [&](int32_t a, int32_t b) { return seq_before(cands[a].dfs, cands[b].dfs); });
+      for(size_t a0 = 0; a0 < acc.size();) {
+        const int32_t n = cands[acc[a0]].node;
+        size_t a1 = a0;
+        while(a1 < acc.size() && cands[acc[a1]].node == n) a1++;
+        std::sort(acc.begin() + a0, acc.begin() + a1,
+                  [&](int32_t a, int32_t b) { return seq_before(cands[a].dfs, cands[b].dfs); });
         PNode &p = nodes[n];
         JobState &S = *jobs_[p.job];
         const int32_t max_edges = S.job.opt.max_edges;
-        for(int32_t ci : v) {
+        for(size_t ai = a0; ai < a1; ai++) {
+          const int32_t ci = acc[ai];
           const Candidate &cd = cands[ci];
-          PatternRec pr{ p.pattern, cd.dfs, cd.support, {} };
-          S.pats.push_back(pr);
+          S.pats.push_back(PatternRec{ p.pattern, cd.dfs, cd.support });
           const int32_t pid = (int32_t)S.pats.size() - 1;
-          S.pats[p.pattern].children.push_back(pid);
+          PatternRec &par = S.pats[p.pattern];
+          if(par.last_child < 0) par.first_child = pid;
+          else S.pats[par.last_child].next_sibling = pid;
+          par.last_child = pid;
           const int32_t child_edges = (int32_t)p.code.size() + 1;
           if(max_edges > 0 && child_edges >= max_edges) continue;
           if(child_edges >= kMaxPatternEdges || (cd.dfs.is_forward() && cd.dfs.to + 1 > 64))
@@ -1361,12 +1456,17 @@ private:
           mats.push_back(Mat{ n, ci, pid });
           bytes += Carver::round((size_t)cd.cnt * 8) + Carver::round((size_t)cd.cnt * 4);
         }
+        a0 = a1;
       }
       // pass 2: every child's new column and graph ranks carved from one block
       if(!mats.empty()) {
         const int32_t blk = E.new_block(bytes);
         Carver cv{ (char *)E.blocks[blk].base };
+        made.reserve(mats.size());
+        outs.reserve(mats.size());
+        pairs.reserve(mats.size());
         for(const Mat &m : mats) {
+          made_at[m.node + 1]++;
           const Candidate &cd = cands[m.cand];
           PNode &p = nodes[m.node];
           JobState &S = *jobs_[p.job];
@@ -1380,12 +1480,12 @@ private:
           nn.job = p.job;
           nn.pattern = m.pid;
           nn.code.reserve(p.code.size() + 1);
-          nn.code = p.code;
+          nn.code.assign(p.code.data(), p.code.size());
           nn.code.push_back(cd.dfs);
           // forward children append a column, backward children replace the last
           const size_t keep = cd.dfs.is_forward() ? p.cols.size() : p.cols.size() - 1;
           nn.cols.reserve(keep + 1);
-          nn.cols.assign(p.cols.begin(), p.cols.begin() + keep);
+          nn.cols.assign(p.cols.data(), keep);
           for(int32_t id : nn.cols) E.ref(id);
           nn.cols.push_back(E.new_col(col, rowsn, blk));
           nn.gord = gord;
@@ -1395,9 +1495,10 @@ private:
           nn.support = cd.support;
           S.live_bytes += rowsn * (int64_t)(sizeof(int2) + sizeof(int32_t));
           S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
-          made[m.node].push_back(std::move(nn));
+          made.push_back(std::move(nn));
         }
       }
+      for(int32_t n = 0; n < W; n++) made_at[n + 1] += made_at[n];
     }
     if(!outs.empty()) {
       X.d_outs.ensure(outs.size());
@@ -1438,12 +1539,11 @@ private:
     }
     for(int32_t n = W - 1; n >= 0; n--) {
       JobState &S = *jobs_[nodes[n].job];
-      for(auto it = made[n].rbegin(); it != made[n].rend(); ++it) S.stack.push_back(std::move(*it));
-      S.pending += (int64_t)made[n].size();
-      stacked_ += (int64_t)made[n].size();
+      for(int32_t i = made_at[n + 1] - 1; i >= made_at[n]; i--) S.stack.push_back(std::move(made[i]));
+      S.pending += made_at[n + 1] - made_at[n];
+      stacked_ += made_at[n + 1] - made_at[n];
     }
     nodes.clear();
-    lays.clear();
     f.busy = false;
     st_.host_select_ms += ms_since(t_ready) - (st_.host_min_ms - min_before);
     std::sort(touched.begin(), touched.end());
@@ -1460,7 +1560,7 @@ private:
     const LabelMap &lm = j.db->labels;
     std::vector<DFS> path, styled, orig;
     std::vector<int32_t> flat;
-    struct Frame { int32_t pat; size_t next; };
+    struct Frame { int32_t pat; int32_t next; };
     std::vector<Frame> st;
     auto out = [&](int32_t pid) {
       const size_t n = path.size();
@@ -1486,15 +1586,15 @@ private:
     for(int32_t r : S.roots) {
       path.assign(1, S.pats[r].edge);
       out(r);
-      st.assign(1, Frame{ r, 0 });
+      st.assign(1, Frame{ r, S.pats[r].first_child });
       while(!st.empty()) {
         Frame &fr = st.back();
-        const auto &ch = S.pats[fr.pat].children;
-        if(fr.next < ch.size()) {
-          const int32_t cc = ch[fr.next++];
+        if(fr.next >= 0) {
+          const int32_t cc = fr.next;
+          fr.next = S.pats[cc].next_sibling;
           path.push_back(S.pats[cc].edge);
           out(cc);
-          st.push_back(Frame{ cc, 0 });
+          st.push_back(Frame{ cc, S.pats[cc].first_child });
         } else {
           st.pop_back();
           path.pop_back();
