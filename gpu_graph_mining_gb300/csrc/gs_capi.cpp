@@ -47,6 +47,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   if(o->threads > 0) m.threads = o->threads;
   if(o->wave_rows > 0) m.wave_rows = o->wave_rows;
   if(o->wave_words > 0) m.wave_words = o->wave_words;
+  m.min_check = o->min_check == 1 ? 1 : 0;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -78,6 +79,7 @@ void fill_stats(const gsgb::MineStats &s, gs_mine_stats *o)
   o->host_wait_ms = s.host_wait_ms;
   o->host_select_ms = s.host_select_ms;
   o->host_emit_ms = s.host_emit_ms;
+  o->min_host_checks = s.min_host;
 }
 
 struct BatchCtx {
@@ -191,6 +193,8 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->wave_words = m.wave_words;
   o->root_part = 0;
   o->root_parts = 1;
+  o->min_check = m.min_check;
+  o->pad = 0;
 }
 
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,

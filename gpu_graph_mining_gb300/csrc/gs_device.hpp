@@ -36,6 +36,8 @@ struct DevDB {
   int32_t n_vertices;
   int32_t max_graph_vertices;
   int32_t pad;
+  const int32_t *root_off;   // [VL+1] first key of each vertex label's (elabel, tolabel) pairs
+  const int32_t *pair_code;  // [root_off[VL]] (elabel << 16) | tolabel of each pair
 };
 
 // Per DFS-tree node of a wave (a batch of nodes extended together).
@@ -56,6 +58,10 @@ struct NodeDesc {
   int32_t nkeys;
   int32_t db;            // index into the resident-database table
   int32_t minsup;        // the node's job's minimum support (candidate selection)
+  int32_t code_off;      // the node's DFS code: edges code_off.. of the wave's code table
+  int32_t code_len;      //   (5 int32 per edge: from, to, fromlabel, elabel, tolabel)
+  int32_t nfwd;          // keys below nfwd are forward extensions
+  int32_t pad2;
 };
 
 // One right-most-path vertex of a node.

@@ -96,7 +96,8 @@ void Database::upload()
   size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
   size_t o_vb = o_ro + al(sizeof(int32_t) * (VL + 1));
   size_t o_ap = o_vb + al(sizeof(int32_t) * (host.n_graphs + 1));
-  size_t total = o_ap + al(sizeof(int32_t) * (E2 + 1));
+  size_t o_pc = o_ap + al(sizeof(int32_t) * (E2 + 1));
+  size_t total = o_pc + al(sizeof(int32_t) * (root_keys + 1));
   std::vector<unsigned long long> adj(E2 + 1, 0);
   parallel_ranges(E2, [&](int64_t b, int64_t e, int) {
     for(int64_t k = b; k < e; k++) {
@@ -139,7 +140,14 @@ void Database::upload()
   if(V) CK(cudaMemcpy(b + o_vl, vl_dense.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_vg, vg.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_pi, pidx.data(), sizeof(int32_t) * tab, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(b + o_ro, root_off.data(), sizeof(int32_t) * VL, cudaMemcpyHostToDevice));
+  std::vector<int32_t> ro(root_off);
+  ro.push_back(root_keys);
+  std::vector<int32_t> pc(root_keys + 1, 0);
+  for(int32_t a = 0; a < VL; a++)
+    for(size_t i = 0; i < pairs[a].size(); i++)
+      pc[root_off[a] + i] = (pairs[a][i].first << 16) | pairs[a][i].second;
+  CK(cudaMemcpy(b + o_ro, ro.data(), sizeof(int32_t) * (VL + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_pc, pc.data(), sizeof(int32_t) * (root_keys + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_vb, vb.data(), sizeof(int32_t) * (host.n_graphs + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_ap, ap.data(), sizeof(int32_t) * (E2 + 1), cudaMemcpyHostToDevice));
   dev.adj = (const unsigned long long *)(b + o_adj);
@@ -155,6 +163,8 @@ void Database::upload()
   dev.n_graphs = host.n_graphs;
   dev.n_vertices = (int32_t)V;
   d_root_off = (int32_t *)(b + o_ro);
+  dev.root_off = d_root_off;
+  dev.pair_code = (const int32_t *)(b + o_pc);
   resident = true;
 }
 
@@ -527,6 +537,7 @@ struct Candidate {
   DFS dfs;
   int32_t support;
   int32_t cnt;
+  int32_t verdict;  // canonicality from the GPU: 1 / 0, or 2 = check on the host
   bool ok;
 };
 
@@ -1208,14 +1219,15 @@ private:
     st_.rows += rows;
 
     // descriptors
-    int32_t tot_cols = 0, tot_slots = 0;
+    int32_t tot_cols = 0, tot_slots = 0, tot_edges = 0;
     for(int32_t n = 0; n < W; n++) {
       tot_cols += (int32_t)nodes[n].cols.size();
       tot_slots += (int32_t)lays[n].slots.size();
+      tot_edges += (int32_t)nodes[n].code.size();
     }
     size_t off = 0;
-    size_t need = 256 * 6 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
-                  2 * sizeof(int32_t) * tot_cols;
+    size_t need = 256 * 7 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
+                  2 * sizeof(int32_t) * tot_cols + 5 * sizeof(int32_t) * tot_edges;
     X.h_desc.ensure(need);
     X.d_desc.ensure(need);
     char *hb = X.h_desc.p;
@@ -1224,7 +1236,9 @@ private:
     SlotDesc *hs = carve<SlotDesc>(hb, off, tot_slots);
     int32_t *hv = carve<int32_t>(hb, off, tot_cols);
     int32_t *hl = carve<int32_t>(hb, off, tot_cols);
+    int32_t *hcode = carve<int32_t>(hb, off, 5 * (size_t)tot_edges);
     const size_t desc_bytes = off;
+    int32_t eo = 0;
     int32_t co = 0, so = 0, kmax = 1;
     bool small = true;  // every database of the wave has graphs of <= 64 vertices
     int64_t rb = 0, bb = 0, tb = 0;
@@ -1252,6 +1266,17 @@ private:
       d.nkeys = layout_nkeys(L, db);
       d.db = S.db_slot;
       d.minsup = S.job.minsup;
+      d.code_off = eo;
+      d.code_len = (int32_t)p.code.size();
+      d.nfwd = L.nfwd;
+      for(const DFS &e : p.code) {
+        int32_t *c = hcode + 5 * (size_t)eo++;
+        c[0] = e.from;
+        c[1] = e.to;
+        c[2] = e.fromlabel;
+        c[3] = e.elabel;
+        c[4] = e.tolabel;
+      }
       for(size_t cc = 0; cc < p.cols.size(); cc++) {
         hc[co + cc] = E.cols[p.cols[cc]].ptr;
         hl[co + cc] = (int32_t)E.cols[p.cols[cc]].n;
@@ -1277,6 +1302,7 @@ private:
     f.ds = (const SlotDesc *)(db_ + ((char *)hs - hb));
     f.dv = (const int32_t *)(db_ + ((char *)hv - hb));
     f.dl = (const int32_t *)(db_ + ((char *)hl - hb));
+    const int32_t *dcode = (const int32_t *)(db_ + ((char *)hcode - hb));
     f.W = W;
     f.kb = kb;
     f.kmax = kmax;
@@ -1322,6 +1348,10 @@ private:
     CK(cudaMemsetAsync(X.d_selc.p, 0, 3 * sizeof(unsigned long long), E.stream));
     launch_support_select(f.dn, W, kb, X.d_bm.p, X.d_cnt.p, X.d_bmx.p, X.d_childmap.p, X.d_keyword.p, X.d_listed.p,
                           X.d_sel.p, kb, X.d_selc.p, E.stream);
+    if(wo_.min_check == 0) {
+      launch_is_min(f.dn, W, f.ds, E.d_dbs.p, dcode, X.d_sel.p, kb, X.d_selc.p, E.stream);
+      st_.launches++;
+    }
     CK(cudaEventRecord(X.ev[2], E.stream));
     st_.launches += 3;
     // the frequent candidates come back compacted: a prefix sized from earlier
@@ -1392,17 +1422,22 @@ private:
       cd.key = e.x - hn[n].key_base;
       cd.support = e.y;
       cd.cnt = e.z;
-      cd.ok = false;
+      cd.verdict = wo_.min_check == 0 ? e.w : 2;
+      cd.ok = cd.verdict == 1;
       if(cd.key < 0 || cd.key >= hn[n].nkeys) throw Error(ST_ERR_STATE, "selected key outside its node");
       if(!decode_key(lays[n], *S.job.db, cd.key, cd.dfs)) continue;
       cands.push_back(cd);
     }
     st_.candidates += (int64_t)cands.size();
-    // canonicality on the host, in parallel
+    // canonicality: the GPU's verdicts; the rest on the host, in parallel
     {
       const clk::time_point t0 = clk::now();
-      E.workers->run((int64_t)cands.size(), [&](int64_t i, int w) {
-        Candidate &cd = cands[i];
+      std::vector<int32_t> todo;
+      for(int32_t i = 0; i < (int32_t)cands.size(); i++)
+        if(cands[i].verdict != 0 && cands[i].verdict != 1) todo.push_back(i);
+      st_.min_host += (int64_t)todo.size();
+      E.workers->run((int64_t)todo.size(), [&](int64_t ti, int w) {
+        Candidate &cd = cands[todo[ti]];
         const auto &code = nodes[cd.node].code;
         DFS buf[kMaxPatternEdges + 1];
         const size_t n = code.size();

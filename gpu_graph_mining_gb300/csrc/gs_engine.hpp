@@ -74,6 +74,7 @@ struct MineOptions {
   int32_t threads = 0;        // host threads for the canonicality check (0 = hardware)
   int32_t root_part = 0;      // mine only the root subtrees with index % root_parts == root_part
   int32_t root_parts = 1;
+  int32_t min_check = 0;      // canonicality: 0 on the GPU (host for oversized patterns), 1 on the host
 };
 
 struct MineStats {
@@ -99,6 +100,7 @@ struct MineStats {
   double host_wait_ms = 0;   // blocked on the device (stream synchronisations)
   double host_select_ms = 0; // candidate decoding, child allocation, child tables
   double host_emit_ms = 0;   // pattern-tree traversal and output
+  int64_t min_host = 0;      // candidates whose canonicality was checked on the host
 };
 
 struct MineJob {

@@ -58,6 +58,11 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 void launch_support_select(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm,
                            const int32_t *cnt, int32_t *bmx, int32_t *childmap, long long *keyword, int2 *listed,
                            int4 *sel, int32_t sel_cap, unsigned long long *counters, cudaStream_t s);
+// Canonicality of the selected candidates (gs_ismin.cu): sel[i].w = 1 minimal,
+// 0 not minimal, 2 left to the host.  codes = the wave's code table.
+void launch_is_min(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
+                   const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters,
+                   cudaStream_t s);
 // childmap[pairs[i].x] = pairs[i].y
 void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, cudaStream_t s);
 void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,

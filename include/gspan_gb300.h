@@ -128,6 +128,9 @@ typedef struct gs_mine_opts {
   int64_t wave_words;  /* support-bitmap words per launch (soft cap; 0 = default) */
   int32_t root_part;   /* mine only the root subtrees whose index (in the reference's root */
   int32_t root_parts;  /* order) is root_part modulo root_parts; root_parts <= 1 = all */
+  int32_t min_check;   /* canonicality check: 0 = on the GPU (patterns over 32 vertices or 64 edges,
+                          or with too many self-embeddings, on the host), 1 = on the host */
+  int32_t pad;
 } gs_mine_opts;
 
 typedef struct gs_mine_stats {
@@ -153,6 +156,7 @@ typedef struct gs_mine_stats {
   double host_wait_ms;     /* host: blocked on the device */
   double host_select_ms;   /* host: candidate decoding and child allocation */
   double host_emit_ms;     /* host: output */
+  int64_t min_host_checks; /* candidates whose canonicality was checked on the host */
 } gs_mine_stats;
 
 GS_API void gs_mine_opts_default(gs_mine_opts *opts);

@@ -221,3 +221,17 @@ def test_full_size_checksums(gs, tmp_path, row):
         if len(parts) > 1:
             parent = ";".join(parts[:-1])
             assert parent in sup and sup[parent] >= v
+
+
+@pytest.mark.parametrize("config,scale,frac", [(1, 1.0, 0.05), (2, 0.02, 0.02), (3, 0.05, 0.05), (5, 0.002, 0.005)])
+def test_gpu_canonicality_matches_host(gs, config, scale, frac):
+    # the warp-parallel check decides (nearly) every candidate; the host
+    # checker on the same candidates must agree pattern for pattern
+    db = gs.Database.generate(config, scale=scale)
+    s = max(2, int(frac * len(db)))
+    a, sa = gs.mine(db, s, min_check=0)
+    b, sb = gs.mine(db, s, min_check=1)
+    assert a == b
+    assert sb["min_host_checks"] == sb["candidates"]
+    assert sa["candidates"] == sb["candidates"]
+    assert sa["min_host_checks"] * 10 <= sa["candidates"]
