@@ -32,7 +32,19 @@ namespace gsgb {
 
 namespace {
 
-constexpr int kWarps = 4;  // warps per block
+// Launch shape (compile-time tunables): warps per block, the minimum blocks
+// per SM the register allocation must allow (0 = no constraint), and the
+// grid cap in blocks per SM (warps loop over tiles beyond it).
+#ifndef GS_WAVE_WARPS
+#define GS_WAVE_WARPS 4
+#endif
+#ifndef GS_WAVE_MINB
+#define GS_WAVE_MINB 0
+#endif
+#ifndef GS_WAVE_GRID
+#define GS_WAVE_GRID 32
+#endif
+constexpr int kWarps = GS_WAVE_WARPS;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kRecChunk = 128;  // records a warp reserves at a time
 
@@ -81,7 +93,13 @@ __device__ __forceinline__ unsigned lanemask_lt()
 // "is w already in the embedding" is one bit test of the row's vertex set
 // instead of a loop over its k vertices.
 template <int KMAX, bool MAT, bool MASK>
-__global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
+__global__ void
+#if GS_WAVE_MINB > 0
+__launch_bounds__(kWarps * 32, GS_WAVE_MINB)
+#else
+__launch_bounds__(kWarps * 32)
+#endif
+k_wave(const WaveArgs a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -181,9 +199,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
     const int off = incl - W;
     const int T = __shfl_sync(kFull, incl, 31);
     if(lane == 0) mine += 8ull * T;  // one packed adjacency entry per item
-    for(int base = 0; base < T; base += 32) {
-      const int j = base + lane;
-      const bool has = j < T;
+    // Items are located and their adjacency entries (and pair indices) loaded
+    // one batch ahead: the next batch's loads are in flight while this batch
+    // is decided and emitted.
+    int o_n = 0, s_n = 0;
+    bool has_n = false;
+    unsigned long long ent_n = 0;
+    int pr_n = 0;
+    auto locate = [&](int j) {
       // owner lane: the largest o with off_o <= j (it has W_o > 0)
       int o = 0;
 #pragma unroll
@@ -193,22 +216,38 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
         if(oc <= j) o = c;
       }
       const int q = j - __shfl_sync(kFull, off, o);
+      o_n = o;
+      s_n = 0;
+      has_n = j < T;
+      if(has_n) {
+        int sl = 0;
+        while(S.pre[sl + 1][o] <= q) sl++;
+        s_n = sl;
+        const int e = S.start[sl][o] + (q - S.pre[sl][o]);
+        ent_n = __ldg(&adj[e]);
+        pr_n = __ldg(&adj_pair[e]);
+      }
+    };
+    if(T > 0) locate(lane);
+    for(int base = 0; base < T; base += 32) {
+      const int o = o_n, s = s_n;
+      const bool has = has_n;
+      const unsigned long long ent = ent_n;
+      const int pr = pr_n;
+      if(base + 32 < T) locate(base + 32 + lane);  // warp-uniform condition
       const int g_o = __shfl_sync(kFull, g, o);
       const int lp_o = __shfl_sync(kFull, last_prev, o);
       int key = -1, w = 0;
       bool bwd = false;
       if(has) {
-        int s = 0;
-        while(S.pre[s + 1][o] <= q) s++;
-        const int e = S.start[s][o] + (q - S.pre[s][o]);
-        const unsigned long long ent = __ldg(&adj[e]);
+        const int frule = S.slot[s].frule, fko = S.slot[s].fkey_off;
         w = (int)(unsigned)(ent & 0xffffffffull);
         const int hi = (int)(ent >> 32);  // (edge label << 16) | neighbour label
         const int wl = hi & 0xffff;
         const bool is_r = (s == nslot - 1);
         // forward: label >= minlabel and the right-most-path order rule (one
         // compare, INT32_MIN for the right-most vertex); needs a new vertex
-        const bool fwd_rules = wl >= minlabel && hi >= S.slot[s].frule;
+        const bool fwd_rules = wl >= minlabel && hi >= frule;
         bool in_emb = false;
         if(MASK) {
           const unsigned lv = (unsigned)(w - S.gb[o]);
@@ -217,7 +256,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_wave(const WaveArgs a)
           for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
         }
         if(fwd_rules && !in_emb) {
-          key = S.slot[s].fkey_off + __ldg(&adj_pair[e]);
+          key = fko + pr;
         } else if(is_r && in_emb) {
           // backward edge from the right-most vertex to a right-most-path vertex
           int jv = -1;
@@ -310,7 +349,7 @@ template <int KMAX, bool MAT, bool MASK> void launch_k(const WaveArgs &a, cudaSt
     configured = true;
   }
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
-  const long long cap = 152LL * 32;
+  const long long cap = 152LL * GS_WAVE_GRID;
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
   k_wave<KMAX, MAT, MASK><<<(int)blocks, kWarps * 32, smem, s>>>(a);
