@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--minsup-frac", type=float, default=0.01)
     p.add_argument("--wave-nodes", type=int, default=None)
+    p.add_argument("--launch-mode", type=int, default=0, help="0: per-wave CUDA graphs, 1: direct launches")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="mine", choices=["mine", "batch", "serving"],
@@ -378,6 +379,8 @@ def main():
     kw = dict(part)
     if a.wave_nodes is not None:
         kw["wave_nodes"] = a.wave_nodes
+    if a.launch_mode:
+        kw["launch_mode"] = a.launch_mode
     # warm-up (also creates the engine's pool and scratch)
     for _ in range(max(3, a.warmup)):
         g.mine_collect(db, minsup, decode=False, **kw)

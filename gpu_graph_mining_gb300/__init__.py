@@ -49,7 +49,7 @@ class MineOpts(ctypes.Structure):
                 ("wave_nodes", ctypes.c_int32), ("threads", ctypes.c_int32),
                 ("wave_rows", ctypes.c_int64), ("wave_words", ctypes.c_int64),
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
-                ("min_check", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32)]
 
 
 class MineStats(ctypes.Structure):
@@ -280,7 +280,7 @@ def code_to_string(code):
 
 
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
-          root_part=0, root_parts=1, min_check=0):
+          root_part=0, root_parts=1, min_check=0, launch_mode=0):
     o = MineOpts()
     lib().gs_mine_opts_default(ctypes.byref(o))
     o.max_edges = int(max_edges)
@@ -296,11 +296,12 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
     o.root_part = int(root_part)
     o.root_parts = int(root_parts)
     o.min_check = int(min_check)
+    o.launch_mode = int(launch_mode)
     return o
 
 
 def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
-         wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0):
+         wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0):
     """Mines db at absolute support minsup.
 
     Returns (patterns, stats): patterns is a list of (code, support) with code a
@@ -317,7 +318,8 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
             sink(code, support)
 
     fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
-    o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check)
+    o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check,
+              launch_mode)
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()

@@ -48,6 +48,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   if(o->wave_rows > 0) m.wave_rows = o->wave_rows;
   if(o->wave_words > 0) m.wave_words = o->wave_words;
   m.min_check = o->min_check == 1 ? 1 : 0;
+  m.launch_mode = o->launch_mode == 1 ? 1 : 0;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -194,7 +195,7 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->root_part = 0;
   o->root_parts = 1;
   o->min_check = m.min_check;
-  o->pad = 0;
+  o->launch_mode = m.launch_mode;
 }
 
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,

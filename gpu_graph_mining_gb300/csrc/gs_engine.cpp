@@ -549,6 +549,64 @@ struct NodeLayout {
   std::vector<SlotDesc> slots;
 };
 
+// The device work of one wave up to its results copy: descriptor upload,
+// scratch clears, count, selection, canonicality, results download, with the
+// context's events between them.
+struct WaveSeq {
+  void *desc_dst = nullptr;
+  const void *desc_src = nullptr;
+  size_t desc_bytes = 0;
+  void *zero = nullptr;
+  size_t zero_bytes = 0;
+  void *head = nullptr;
+  void *head_host = nullptr;
+  size_t d2h_bytes = 0;
+  KernelCall count, screen, listed, ismin;
+  bool with_min = false;
+};
+
+// WaveSeq as an instantiated CUDA graph, one per count-kernel variant and
+// context: each wave updates the nodes' parameters and launches the graph.
+struct WaveGraph {
+  const void *count_func = nullptr;
+  bool with_min = false;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t x = nullptr;
+  cudaGraphNode_t h2d, mz, mh, count, screen, listed, ismin, d2h;
+};
+
+inline cudaMemsetParams clear_params(void *dst, size_t bytes)
+{
+  cudaMemsetParams m{};
+  m.dst = dst;
+  m.pitch = 0;
+  m.value = 0;
+  m.elementSize = 1;
+  m.width = bytes;
+  m.height = 1;
+  return m;
+}
+
+inline cudaKernelNodeParams kernel_params(KernelCall &c)
+{
+  cudaKernelNodeParams k{};
+  k.func = const_cast<void *>(c.func);
+  k.gridDim = c.grid;
+  k.blockDim = c.block;
+  k.sharedMemBytes = c.smem;
+  k.kernelParams = c.params();
+  k.extra = nullptr;
+  return k;
+}
+
+// Header slots of a wave's results (unsigned long long each).
+constexpr int kHeadRecords = 0;   // extension records written by the count pass
+constexpr int kHeadFlags = 1;     // consistency flags after the count pass
+constexpr int kHeadSelected = 2;  // selected candidates   } counters of
+constexpr int kHeadExt = 3;       // embeddings of all keys } the support
+constexpr int kHeadListed = 4;    // keys counted          } selection
+constexpr size_t kHeadBytes = 64;
+
 // Device scratch and pinned mirrors of one wave in flight.  Two of them let
 // the host prepare one wave's children while the GPU counts the other's.
 struct WaveCtx {
@@ -560,14 +618,14 @@ struct WaveCtx {
   DBuf<int4> d_rec;
   DBuf<unsigned long long> d_recn;
   DBuf<long long> d_keyword;
-  // candidate selection: frequent keys {key, support, embeddings, 0}, and
-  // the (key, child) pairs of the children to materialise
-  DBuf<int4> d_sel;
+  // A wave's results, copied back in one piece: a 64-byte header (kHead*
+  // slots) followed by the selected candidates {key, support, embeddings,
+  // verdict}.  The zeroed region holds the embedding counts and the support
+  // bitmaps (one memset).  The child table holds the children's outputs and
+  // (key, child) pairs (one upload).
+  DBuf<char> d_head, d_zero, d_mat;
+  HBuf<char> h_head, h_mat;
   DBuf<int2> d_listed;               // keys with enough embeddings to be counted
-  DBuf<unsigned long long> d_selc;   // [0] selected keys, [1] embeddings of all keys, [2] listed keys
-  DBuf<int2> d_pairs;
-  HBuf<int4> h_sel;
-  HBuf<int2> h_pairs;
   int64_t sel_hint = 4096;           // selected entries copied back with the wave's results
   bool rec_enabled = true;
   long long wanted_rec = 0;    // record capacity to have before the next wave (after an overflow)
@@ -580,6 +638,7 @@ struct WaveCtx {
   // 0/1 count, 1/2 support, 3 results copied, 4/5 materialise
   cudaEvent_t ev[6] = {};
   bool have_events = false;
+  std::vector<WaveGraph> graphs;
 
   void init()
   {
@@ -588,16 +647,19 @@ struct WaveCtx {
       have_events = true;
     }
     h_misc.ensure(4);
-    d_recn.ensure(1);
-    d_selc.ensure(3);
   }
   void free()
   {
     d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
-    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free(); d_sel.free(); d_listed.free(); d_selc.free(); d_pairs.free();
+    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free(); d_listed.free();
+    d_head.free(); d_zero.free(); d_mat.free(); h_head.free(); h_mat.free();
     h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free(); h_keyword.free(); h_misc.free();
-    h_sel.free(); h_pairs.free();
     sel_hint = 4096;
+    for(auto &g : graphs) {
+      if(g.x) cudaGraphExecDestroy(g.x);
+      if(g.g) cudaGraphDestroy(g.g);
+    }
+    graphs.clear();
     if(have_events)
       for(auto &e : ev) cudaEventDestroy(e);
     have_events = false;
@@ -868,6 +930,7 @@ struct Flight {
   int4 *rec = nullptr;
   long long rec_cap = 0;
   int64_t sel_copied = 0;    // selected entries copied back with the results
+  uint32_t *bm = nullptr;    // the wave's support bitmaps (in the zeroed region)
 };
 
 // The wave scheduler.  Jobs join at any time (add) and leave when their last
@@ -1174,6 +1237,75 @@ private:
     for(auto it = made.rbegin(); it != made.rend(); ++it) S.stack.push_back(std::move(*it));
   }
 
+  // Queues a wave's device work: replayed from the context's CUDA graph for
+  // its count-kernel variant (node parameters updated), or launched directly.
+  void issue(WaveCtx &X, WaveSeq &q)
+  {
+    st_.h2d_bytes += (int64_t)q.desc_bytes;
+    st_.d2h_bytes += (int64_t)q.d2h_bytes;
+    if(wo_.launch_mode != 0) {
+      CK(cudaMemcpyAsync(q.desc_dst, q.desc_src, q.desc_bytes, cudaMemcpyHostToDevice, E.stream));
+      CK(cudaMemsetAsync(q.zero, 0, q.zero_bytes, E.stream));
+      CK(cudaMemsetAsync(q.head, 0, kHeadBytes, E.stream));
+      CK(cudaEventRecord(X.ev[0], E.stream));
+      CK(q.count.run(E.stream));
+      CK(cudaEventRecord(X.ev[1], E.stream));
+      CK(q.screen.run(E.stream));
+      CK(q.listed.run(E.stream));
+      if(q.with_min) CK(q.ismin.run(E.stream));
+      CK(cudaEventRecord(X.ev[2], E.stream));
+      CK(cudaMemcpyAsync(q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost, E.stream));
+      CK(cudaEventRecord(X.ev[3], E.stream));
+      return;
+    }
+    WaveGraph *G = nullptr;
+    for(auto &g : X.graphs)
+      if(g.count_func == q.count.func && g.with_min == q.with_min) G = &g;
+    const cudaMemsetParams mz = clear_params(q.zero, q.zero_bytes), mh = clear_params(q.head, kHeadBytes);
+    cudaKernelNodeParams kc = kernel_params(q.count), ks = kernel_params(q.screen), kl = kernel_params(q.listed);
+    cudaKernelNodeParams km{};
+    if(q.with_min) km = kernel_params(q.ismin);
+    if(!G) {
+      X.graphs.emplace_back();
+      G = &X.graphs.back();
+      G->count_func = q.count.func;
+      G->with_min = q.with_min;
+      cudaGraph_t g;
+      CK(cudaGraphCreate(&g, 0));
+      G->g = g;
+      cudaGraphNode_t e0, e1, e2, e3, last;
+      CK(cudaGraphAddMemcpyNode1D(&G->h2d, g, nullptr, 0, q.desc_dst, q.desc_src, q.desc_bytes,
+                                  cudaMemcpyHostToDevice));
+      CK(cudaGraphAddMemsetNode(&G->mz, g, &G->h2d, 1, &mz));
+      CK(cudaGraphAddMemsetNode(&G->mh, g, &G->mz, 1, &mh));
+      CK(cudaGraphAddEventRecordNode(&e0, g, &G->mh, 1, X.ev[0]));
+      CK(cudaGraphAddKernelNode(&G->count, g, &e0, 1, &kc));
+      CK(cudaGraphAddEventRecordNode(&e1, g, &G->count, 1, X.ev[1]));
+      CK(cudaGraphAddKernelNode(&G->screen, g, &e1, 1, &ks));
+      CK(cudaGraphAddKernelNode(&G->listed, g, &G->screen, 1, &kl));
+      last = G->listed;
+      if(q.with_min) {
+        CK(cudaGraphAddKernelNode(&G->ismin, g, &last, 1, &km));
+        last = G->ismin;
+      }
+      CK(cudaGraphAddEventRecordNode(&e2, g, &last, 1, X.ev[2]));
+      CK(cudaGraphAddMemcpyNode1D(&G->d2h, g, &e2, 1, q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost));
+      CK(cudaGraphAddEventRecordNode(&e3, g, &G->d2h, 1, X.ev[3]));
+      CK(cudaGraphInstantiate(&G->x, g, 0));
+    } else {
+      CK(cudaGraphExecMemcpyNodeSetParams1D(G->x, G->h2d, q.desc_dst, q.desc_src, q.desc_bytes,
+                                            cudaMemcpyHostToDevice));
+      CK(cudaGraphExecMemsetNodeSetParams(G->x, G->mz, &mz));
+      CK(cudaGraphExecMemsetNodeSetParams(G->x, G->mh, &mh));
+      CK(cudaGraphExecKernelNodeSetParams(G->x, G->count, &kc));
+      CK(cudaGraphExecKernelNodeSetParams(G->x, G->screen, &ks));
+      CK(cudaGraphExecKernelNodeSetParams(G->x, G->listed, &kl));
+      if(q.with_min) CK(cudaGraphExecKernelNodeSetParams(G->x, G->ismin, &km));
+      CK(cudaGraphExecMemcpyNodeSetParams1D(G->x, G->d2h, q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost));
+    }
+    CK(cudaGraphLaunch(G->x, E.stream));
+  }
+
   // ---- launch one wave into context c: descriptors, count, support, results copy
   void launch(int c, bool other_busy)
   {
@@ -1308,16 +1440,18 @@ private:
     f.kmax = kmax;
     f.small = small;
     f.tb = tb;
-    X.d_bm.ensure(std::max<int64_t>(bb, 1));
+    const size_t cnt_bytes = Carver::round(sizeof(int32_t) * (size_t)std::max(kb, 1));
+    const size_t zero_bytes = cnt_bytes + sizeof(uint32_t) * (size_t)std::max<int64_t>(bb, 1);
+    X.d_zero.ensure(zero_bytes);
+    X.d_head.ensure(kHeadBytes + sizeof(int4) * (size_t)std::max(kb, 1));
     X.d_bmx.ensure(std::max<int64_t>(bb, 1));
-    X.d_cnt.ensure(std::max(kb, 1));
     X.d_childmap.ensure(std::max(kb, 1));
     X.d_keyword.ensure(std::max(kb, 1));
-    X.d_sel.ensure(std::max(kb, 1));
     X.d_listed.ensure(std::max(kb, 1));
-    h2d(X.d_desc.p, hb, desc_bytes);
-    CK(cudaMemsetAsync(X.d_bm.p, 0, (size_t)bb * 4, E.stream));
-    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)kb * 4, E.stream));
+    int32_t *cnt = (int32_t *)X.d_zero.p;
+    f.bm = (uint32_t *)(X.d_zero.p + cnt_bytes);
+    unsigned long long *head = (unsigned long long *)X.d_head.p;
+    int4 *sel = (int4 *)(X.d_head.p + kHeadBytes);
     // records: how many the wave appends is not known up front, so keep the
     // largest count seen (grown after an overflow)
     f.rec = nullptr;
@@ -1339,30 +1473,30 @@ private:
       if(X.d_rec.cap == 0) X.d_rec.ensure((size_t)1 << 22);
       f.rec = X.d_rec.p;
       f.rec_cap = (long long)X.d_rec.cap;
-      CK(cudaMemsetAsync(X.d_recn.p, 0, sizeof(unsigned long long), E.stream));
     }
-    CK(cudaEventRecord(X.ev[0], E.stream));
-    launch_wave_count(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, X.d_bm.p, X.d_cnt.p,
-                      E.d_bytes.p + 0, err_flag(), f.rec, f.rec_cap, f.rec ? X.d_recn.p : nullptr, E.stream);
-    CK(cudaEventRecord(X.ev[1], E.stream));
-    CK(cudaMemsetAsync(X.d_selc.p, 0, 3 * sizeof(unsigned long long), E.stream));
-    launch_support_select(f.dn, W, kb, X.d_bm.p, X.d_cnt.p, X.d_bmx.p, X.d_childmap.p, X.d_keyword.p, X.d_listed.p,
-                          X.d_sel.p, kb, X.d_selc.p, E.stream);
-    if(wo_.min_check == 0) {
-      launch_is_min(f.dn, W, f.ds, E.d_dbs.p, dcode, X.d_sel.p, kb, X.d_selc.p, E.stream);
-      st_.launches++;
-    }
-    CK(cudaEventRecord(X.ev[2], E.stream));
-    st_.launches += 3;
     // the frequent candidates come back compacted: a prefix sized from earlier
     // waves, the rest (rarely) by a second copy
     f.sel_copied = std::min<int64_t>(kb, X.sel_hint);
-    X.h_sel.ensure((size_t)std::max<int64_t>(f.sel_copied, 1));
-    if(f.sel_copied > 0) d2h(X.h_sel.p, X.d_sel.p, sizeof(int4) * (size_t)f.sel_copied);
-    if(f.rec) d2h(X.h_misc.p, X.d_recn.p, sizeof(unsigned long long));
-    d2h(X.h_misc.p + 1, E.d_bytes.p + 3, sizeof(unsigned long long));
-    d2h(X.h_misc.p + 2, X.d_selc.p, 2 * sizeof(unsigned long long));
-    CK(cudaEventRecord(X.ev[3], E.stream));
+    X.h_head.ensure(kHeadBytes + sizeof(int4) * (size_t)std::max<int64_t>(f.sel_copied, 1));
+    WaveSeq q;
+    q.desc_dst = X.d_desc.p;
+    q.desc_src = hb;
+    q.desc_bytes = desc_bytes;
+    q.zero = X.d_zero.p;
+    q.zero_bytes = zero_bytes;
+    q.head = X.d_head.p;
+    q.head_host = X.h_head.p;
+    q.d2h_bytes = kHeadBytes + sizeof(int4) * (size_t)f.sel_copied;
+    q.count = wave_count_call(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, cnt, E.d_bytes.p + 0,
+                              err_flag(), f.rec, f.rec_cap, f.rec ? head + kHeadRecords : nullptr);
+    q.screen = screen_keys_call(f.dn, W, kb, cnt, X.d_childmap.p, X.d_listed.p, head + kHeadSelected, err_flag(),
+                                head + kHeadFlags);
+    q.listed = count_listed_call(f.dn, X.d_listed.p, f.bm, cnt, X.d_bmx.p, X.d_keyword.p, sel, kb,
+                                 head + kHeadSelected);
+    q.with_min = wo_.min_check == 0;
+    if(q.with_min) q.ismin = is_min_call(f.dn, W, f.ds, E.d_dbs.p, dcode, sel, kb, head + kHeadSelected);
+    issue(X, q);
+    st_.launches += q.with_min ? 4 : 3;
     f.busy = true;
     f.seq = ++seq_;
     st_.host_build_ms += ms_since(t_begin);
@@ -1379,7 +1513,8 @@ private:
       st_.host_wait_ms += ms_since(t0);
     }
     CK(cudaGetLastError());
-    check_flags(X.h_misc.p[1]);
+    const unsigned long long *hh = (const unsigned long long *)X.h_head.p;
+    check_flags(hh[kHeadFlags]);
     const clk::time_point t_ready = clk::now();
     const double min_before = st_.host_min_ms;
     if(f.mat_pending) {
@@ -1395,25 +1530,28 @@ private:
     const int32_t W = f.W, kb = f.kb;
 
     // frequent candidates (compacted on the device)
-    const int64_t nsel = (int64_t)X.h_misc.p[2];
-    st_.extensions += (int64_t)X.h_misc.p[3];
+    const int64_t nsel = (int64_t)hh[kHeadSelected];
+    const long long nrec = f.rec ? (long long)hh[kHeadRecords] : -1;
+    st_.extensions += (int64_t)hh[kHeadExt];
     if(nsel > kb) throw Error(ST_ERR_STATE, "candidate selection overflow");
     if(nsel > f.sel_copied) {
       // copies the whole list again (growing the pinned buffer drops its
       // contents) on the side stream: the wave's results are complete, and the
       // main stream already holds the other context's wave
-      X.h_sel.ensure((size_t)nsel);
-      CK(cudaMemcpyAsync(X.h_sel.p, X.d_sel.p, sizeof(int4) * (size_t)nsel, cudaMemcpyDeviceToHost, E.aux));
+      X.h_head.ensure(kHeadBytes + sizeof(int4) * (size_t)nsel);
+      CK(cudaMemcpyAsync(X.h_head.p, X.d_head.p, kHeadBytes + sizeof(int4) * (size_t)nsel, cudaMemcpyDeviceToHost,
+                         E.aux));
       CK(cudaStreamSynchronize(E.aux));
-      st_.d2h_bytes += (int64_t)sizeof(int4) * nsel;
+      st_.d2h_bytes += (int64_t)(kHeadBytes + sizeof(int4) * nsel);
     }
+    int4 *hsel = (int4 *)(X.h_head.p + kHeadBytes);
     X.sel_hint = std::max<int64_t>(X.sel_hint, 2 * nsel);
-    std::sort(X.h_sel.p, X.h_sel.p + nsel, [](const int4 &a, const int4 &b) { return a.x < b.x; });
+    std::sort(hsel, hsel + nsel, [](const int4 &a, const int4 &b) { return a.x < b.x; });
     std::vector<Candidate> cands;
     cands.reserve((size_t)nsel);
     int32_t n = 0;
     for(int64_t i = 0; i < nsel; i++) {
-      const int4 e = X.h_sel.p[i];
+      const int4 e = hsel[i];
       while(n + 1 < W && hn[n + 1].key_base <= e.x) n++;
       const JobState &S = *jobs_[nodes[n].job];
       if(S.cancelled) continue;
@@ -1536,28 +1674,27 @@ private:
       for(int32_t n = 0; n < W; n++) made_at[n + 1] += made_at[n];
     }
     if(!outs.empty()) {
-      X.d_outs.ensure(outs.size());
+      // one upload: children's outputs, then the (key, child) pairs
+      const size_t outs_bytes = Carver::round(sizeof(ChildOut) * outs.size());
+      const size_t mat_bytes = outs_bytes + sizeof(int2) * pairs.size();
+      X.d_mat.ensure(mat_bytes);
+      X.h_mat.ensure(mat_bytes);
+      std::memcpy(X.h_mat.p, outs.data(), sizeof(ChildOut) * outs.size());
+      std::memcpy(X.h_mat.p + outs_bytes, pairs.data(), sizeof(int2) * pairs.size());
+      h2d(X.d_mat.p, X.h_mat.p, mat_bytes);
+      const ChildOut *douts = (const ChildOut *)X.d_mat.p;
       X.d_cursor.ensure(outs.size());
-      X.h_outs.ensure(outs.size());
-      std::memcpy(X.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
-      h2d(X.d_outs.p, X.h_outs.p, sizeof(ChildOut) * outs.size());
-      X.d_pairs.ensure(pairs.size());
-      X.h_pairs.ensure(pairs.size());
-      std::memcpy(X.h_pairs.p, pairs.data(), sizeof(int2) * pairs.size());
-      h2d(X.d_pairs.p, X.h_pairs.p, sizeof(int2) * pairs.size());
-      CK(cudaMemsetAsync(X.d_cursor.p, 0, outs.size() * 4, E.stream));
       CK(cudaEventRecord(X.ev[4], E.stream));
-      launch_scatter_childmap(X.d_pairs.p, (int32_t)pairs.size(), X.d_childmap.p, E.stream);
-      const long long nrec = f.rec ? (long long)X.h_misc.p[0] : -1;
+      launch_scatter_childmap((const int2 *)(X.d_mat.p + outs_bytes), (int32_t)pairs.size(), X.d_childmap.p,
+                              X.d_cursor.p, (int32_t)outs.size(), E.stream);
       if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
-        launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, X.d_bm.p, X.d_bmx.p, X.d_cursor.p,
-                                   X.d_outs.p, E.d_bytes.p + 1, err_flag(), E.stream);
+        launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, f.bm, X.d_bmx.p, X.d_cursor.p, douts,
+                                   E.d_bytes.p + 1, err_flag(), E.stream);
       } else {
         // records overflowed (or are disabled): enumerate again
-        launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, X.d_bm.p,
-                                X.d_bmx.p, X.d_childmap.p, X.d_cursor.p, X.d_outs.p, E.d_bytes.p + 1, err_flag(),
-                                E.stream);
+        launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, X.d_bmx.p,
+                                X.d_childmap.p, X.d_cursor.p, douts, E.d_bytes.p + 1, err_flag(), E.stream);
         if(f.rec) X.wanted_rec = std::max<long long>(X.wanted_rec, nrec + nrec / 4);
       }
       CK(cudaEventRecord(X.ev[5], E.stream));

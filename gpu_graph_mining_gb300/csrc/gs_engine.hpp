@@ -75,6 +75,7 @@ struct MineOptions {
   int32_t root_part = 0;      // mine only the root subtrees with index % root_parts == root_part
   int32_t root_parts = 1;
   int32_t min_check = 0;      // canonicality: 0 on the GPU (host for oversized patterns), 1 on the host
+  int32_t launch_mode = 0;    // a wave's device work: 0 replayed from a CUDA graph, 1 launched directly
 };
 
 struct MineStats {

@@ -401,9 +401,8 @@ __global__ void __launch_bounds__(kMinWarps * 32) k_is_min(const NodeDesc *__res
 
 }  // namespace
 
-void launch_is_min(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
-                   const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters,
-                   cudaStream_t s)
+KernelCall is_min_call(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
+                       const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters)
 {
   const size_t smem = sizeof(MinSmem) * kMinWarps;
   static bool configured = false;
@@ -411,7 +410,20 @@ void launch_is_min(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots,
     cudaFuncSetAttribute(k_is_min, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
-  k_is_min<<<152 * 2, kMinWarps * 32, smem, s>>>(nodes, nnodes, slots, dbs, codes, sel, sel_cap, counters);
+  KernelCall c;
+  c.func = (const void *)k_is_min;
+  c.grid = dim3(152 * 2);
+  c.block = dim3(kMinWarps * 32);
+  c.smem = (unsigned)smem;
+  c.arg(nodes);
+  c.arg(nnodes);
+  c.arg(slots);
+  c.arg(dbs);
+  c.arg(codes);
+  c.arg(sel);
+  c.arg(sel_cap);
+  c.arg(counters);
+  return c;
 }
 
 }  // namespace gsgb

@@ -180,12 +180,16 @@ __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__
 __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restrict__ nodes, int nnodes,
                                                          int total_keys, const int32_t *__restrict__ cnt,
                                                          int32_t *childmap, int2 *listed,
-                                                         unsigned long long *counters)
+                                                         unsigned long long *counters,
+                                                         const unsigned int *err, unsigned long long *err_copy)
 {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
   unsigned long long ext = 0;
+  // the consistency flags so far (the count pass has finished) travel back
+  // with the wave's results
+  if(blockIdx.x == 0 && threadIdx.x == 0) *err_copy = *err;
   // warp-uniform trip count: the list append below is warp-aggregated
   const long long n32 = ((long long)total_keys + 31) & ~31ll;
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n32; i += stride) {
@@ -246,11 +250,18 @@ __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restr
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_scatter_childmap(const int2 *__restrict__ pairs, int n, int32_t *childmap)
+// childmap[pairs[i].x] = pairs[i].y for the children to materialise, and
+// their output cursors reset
+__global__ void __launch_bounds__(kBlock) k_scatter_childmap(const int2 *__restrict__ pairs, int n, int32_t *childmap,
+                                                              int32_t *cursor, int ncursor)
 {
-  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int2 p = pairs[i];
-    childmap[p.x] = p.y;
+  const int m = n > ncursor ? n : ncursor;
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    if(i < n) {
+      const int2 p = pairs[i];
+      childmap[p.x] = p.y;
+    }
+    if(i < ncursor) cursor[i] = 0;
   }
 }
 
@@ -296,20 +307,52 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
   k_records_bitmap<<<grid_for(n), kBlock, 0, s>>>(keys, gids, n, words, bm);
 }
 
-void launch_support_select(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm,
-                           const int32_t *cnt, int32_t *bmx, int32_t *childmap, long long *keyword, int2 *listed,
-                           int4 *sel, int32_t sel_cap, unsigned long long *counters, cudaStream_t s)
+KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const int32_t *cnt,
+                            int32_t *childmap, int2 *listed, unsigned long long *counters, const unsigned int *err,
+                            unsigned long long *err_copy)
 {
-  if(total_keys <= 0) return;
-  k_screen_keys<<<grid_for(((long long)total_keys + 31) / 32 * 32), kBlock, 0, s>>>(nodes, nnodes, total_keys, cnt,
-                                                                                    childmap, listed, counters);
-  k_count_listed<<<152 * 8, kBlock, 0, s>>>(nodes, listed, bm, cnt, bmx, keyword, sel, sel_cap, counters);
+  KernelCall c;
+  c.func = (const void *)k_screen_keys;
+  c.grid = dim3((unsigned)grid_for(((long long)total_keys + 31) / 32 * 32));
+  c.block = dim3(kBlock);
+  c.arg(nodes);
+  c.arg(nnodes);
+  c.arg(total_keys);
+  c.arg(cnt);
+  c.arg(childmap);
+  c.arg(listed);
+  c.arg(counters);
+  c.arg(err);
+  c.arg(err_copy);
+  return c;
 }
 
-void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, cudaStream_t s)
+KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, const int32_t *cnt,
+                             int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
+                             unsigned long long *counters)
 {
-  if(n <= 0) return;
-  k_scatter_childmap<<<grid_for(n), kBlock, 0, s>>>(pairs, n, childmap);
+  KernelCall c;
+  c.func = (const void *)k_count_listed;
+  c.grid = dim3(152 * 8);
+  c.block = dim3(kBlock);
+  c.arg(nodes);
+  c.arg(listed);
+  c.arg(bm);
+  c.arg(cnt);
+  c.arg(bmx);
+  c.arg(keyword);
+  c.arg(sel);
+  c.arg(sel_cap);
+  c.arg(counters);
+  return c;
+}
+
+void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, int32_t *cursor, int32_t ncursor,
+                             cudaStream_t s)
+{
+  const int32_t m = n > ncursor ? n : ncursor;
+  if(m <= 0) return;
+  k_scatter_childmap<<<grid_for(m), kBlock, 0, s>>>(pairs, n, childmap, cursor, ncursor);
 }
 
 void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,

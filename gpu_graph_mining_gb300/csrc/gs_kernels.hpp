@@ -5,11 +5,41 @@
 // offending access is skipped, never performed.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "gs_device.hpp"
 
 namespace gsgb {
+
+// A kernel launch as data: function, shape and argument values.  run()
+// launches it on a stream; params() gives the argument pointers a CUDA graph
+// kernel node takes (the graph copies the values when the node is set).
+struct KernelCall {
+  const void *func = nullptr;
+  dim3 grid, block;
+  unsigned smem = 0;
+  template <class T> void arg(const T &v)
+  {
+    used_ = (used_ + alignof(T) - 1) & ~(alignof(T) - 1);
+    std::memcpy(store_ + used_, &v, sizeof(T));
+    off_[n_++] = (unsigned short)used_;
+    used_ += sizeof(T);
+  }
+  void **params()
+  {
+    for(int i = 0; i < n_; i++) ptr_[i] = store_ + off_[i];
+    return ptr_;
+  }
+  cudaError_t run(cudaStream_t s) { return cudaLaunchKernel(func, grid, block, params(), smem, s); }
+
+private:
+  alignas(16) unsigned char store_[384];
+  unsigned short off_[16];
+  void *ptr_[16];
+  int n_ = 0;
+  size_t used_ = 0;
+};
 
 // Root level: one thread per vertex walks its adjacency; every directed
 // entry (v -> w) with label(v) <= label(w) is a 1-edge embedding
@@ -27,10 +57,11 @@ void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uin
 // sized for 8/16/32/64 pattern vertices); collen[] parallels coltab[]: the
 // length of every column.
 // small_graphs: every graph of the wave's databases has <= 64 vertices.
-void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax, bool small_graphs,
-                       const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
-                       const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
-                       int4 *rec, long long rec_cap, unsigned long long *rec_n, cudaStream_t s);
+KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
+                           bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
+                           const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
+                           unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
+                           unsigned long long *rec_n);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
@@ -54,17 +85,21 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 // the exclusive prefix popcount of each word (for graph-rank lookups).
 // Wave support with candidate selection (k_screen_keys, k_count_listed).
 // counters: [0] selected keys, [1] embeddings of all keys, [2] keys listed for
-// counting; listed and sel hold total_keys entries.
-void launch_support_select(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm,
-                           const int32_t *cnt, int32_t *bmx, int32_t *childmap, long long *keyword, int2 *listed,
-                           int4 *sel, int32_t sel_cap, unsigned long long *counters, cudaStream_t s);
+// counting; listed and sel hold total_keys entries.  *err_copy = *err (the
+// consistency flags after the count pass).
+KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const int32_t *cnt,
+                            int32_t *childmap, int2 *listed, unsigned long long *counters, const unsigned int *err,
+                            unsigned long long *err_copy);
+KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, const int32_t *cnt,
+                             int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
+                             unsigned long long *counters);
 // Canonicality of the selected candidates (gs_ismin.cu): sel[i].w = 1 minimal,
 // 0 not minimal, 2 left to the host.  codes = the wave's code table.
-void launch_is_min(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
-                   const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters,
-                   cudaStream_t s);
-// childmap[pairs[i].x] = pairs[i].y
-void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, cudaStream_t s);
+KernelCall is_min_call(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
+                       const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters);
+// childmap[pairs[i].x] = pairs[i].y, and cursor[0..ncursor) = 0
+void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, int32_t *cursor, int32_t ncursor,
+                             cudaStream_t s);
 void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,
                     int32_t *support, cudaStream_t s);
 

@@ -369,17 +369,46 @@ template <bool MAT> void dispatch(int kmax, bool small_graphs, const WaveArgs &a
   else dispatch_k<MAT, false>(kmax, a, s);
 }
 
+template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a)
+{
+  const size_t smem = sizeof(Smem<KMAX>) * kWarps;
+  static bool configured = false;
+  if(!configured) {
+    cudaFuncSetAttribute(k_wave<KMAX, false, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = true;
+  }
+  long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
+  const long long cap = 152LL * GS_WAVE_GRID;
+  if(blocks > cap) blocks = cap;
+  if(blocks < 1) blocks = 1;
+  KernelCall c;
+  c.func = (const void *)k_wave<KMAX, false, MASK>;
+  c.grid = dim3((unsigned)blocks);
+  c.block = dim3(kWarps * 32);
+  c.smem = (unsigned)smem;
+  c.arg(a);
+  return c;
+}
+
+template <bool MASK> KernelCall count_call(int kmax, const WaveArgs &a)
+{
+  if(kmax <= 8) return count_call_k<8, MASK>(a);
+  if(kmax <= 16) return count_call_k<16, MASK>(a);
+  if(kmax <= 32) return count_call_k<32, MASK>(a);
+  return count_call_k<64, MASK>(a);
+}
+
 }  // namespace
 
-void launch_wave_count(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax, bool small_graphs,
-                       const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots, const int32_t *vtab,
-                       const DevDB *dbs, uint32_t *bm, int32_t *cnt, unsigned long long *bytes, unsigned int *err,
-                       int4 *rec, long long rec_cap, unsigned long long *rec_n, cudaStream_t s)
+KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
+                           bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
+                           const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
+                           unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
+                           unsigned long long *rec_n)
 {
-  if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
               nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n };
-  dispatch<false>(kmax, small_graphs, a, s);
+  return small_graphs ? count_call<true>(kmax, a) : count_call<false>(kmax, a);
 }
 
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,

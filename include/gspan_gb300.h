@@ -130,7 +130,8 @@ typedef struct gs_mine_opts {
   int32_t root_parts;  /* order) is root_part modulo root_parts; root_parts <= 1 = all */
   int32_t min_check;   /* canonicality check: 0 = on the GPU (patterns over 32 vertices or 64 edges,
                           or with too many self-embeddings, on the host), 1 = on the host */
-  int32_t pad;
+  int32_t launch_mode; /* a wave's device work (uploads, clears, count, selection, check, results
+                          copy): 0 = replayed from a per-variant CUDA graph, 1 = launched directly */
 } gs_mine_opts;
 
 typedef struct gs_mine_stats {

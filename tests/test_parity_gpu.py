@@ -235,3 +235,11 @@ def test_gpu_canonicality_matches_host(gs, config, scale, frac):
     assert sb["min_host_checks"] == sb["candidates"]
     assert sa["candidates"] == sb["candidates"]
     assert sa["min_host_checks"] * 10 <= sa["candidates"]
+
+
+def test_direct_launches_equal_graph_replay(gs):
+    db = gs.Database.generate(2, scale=0.02)
+    s = max(2, int(0.02 * len(db)))
+    a, sa = gs.mine(db, s, launch_mode=0)
+    b, sb = gs.mine(db, s, launch_mode=1)
+    assert a == b and sa["waves"] == sb["waves"]
