@@ -127,6 +127,25 @@ class Clocks:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
 
 
+def count_traffic(a, alg_bytes_per_step, launches_per_step):
+    """DRAM bytes per count-kernel launch from the committed ncu capture
+    (profiles/k_wave_count_traffic_config2.json): as captured for the same
+    workload, else scaled by this run's algorithmic bytes per launch."""
+    try:
+        with open(os.path.join(REPO, "profiles", "k_wave_count_traffic_config2.json")) as f:
+            p = json.load(f)
+    except Exception:
+        return None, None
+    if launches_per_step <= 0:
+        return None, None
+    per_launch = alg_bytes_per_step / launches_per_step
+    if a.config == 2 and a.scale == 1.0 and abs(a.minsup_frac - 0.01) < 1e-12:
+        return float(p["dram_bytes_per_launch"]), "ncu capture of this workload: " + p["command"]
+    ratio = p["dram_bytes_per_pass"] / p["algorithmic_bytes_per_pass"]
+    return ratio * per_launch, ("scaled from the configuration-2 capture by algorithmic bytes per launch "
+                                "(traffic/algorithmic = %.3f)" % ratio)
+
+
 def cudabin_arrays(db, tmpdir):
     """The reference's flat cudabin arrays of a database (host memory)."""
     import numpy as np
@@ -430,6 +449,7 @@ def main():
     else:
         dom, achieved, dom_bytes, dom_ms, other = "k_wave count", count_gbps, cb, cms, ("k_wave materialise", mat_gbps)
     launches_per_step = sum(s["launches"] for s in stats_all) / len(stats_all)
+    traffic, traffic_note = count_traffic(a, cb, waves) if dom == "k_wave count" else (None, None)
 
     # ---- end-to-end through the C ABI from host arrays
     e2e_times, h2d, d2h = [], 0, 0
@@ -487,7 +507,8 @@ def main():
         "e2e": {"value": e2e, "unit": unit, "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "peak_kind": peak_kind, "traffic": None,
+                     "frac": achieved / peak if peak else None, "peak_kind": peak_kind, "traffic": traffic,
+                     "traffic_source": traffic_note,
                      "algorithmic_bytes_per_step": dom_bytes, "kernel_ms_per_step": dom_ms,
                      "launches_per_step": waves, "other_kernel": {"kernel": other[0], "achieved": other[1]}},
         "cpu_baseline": cpu,
