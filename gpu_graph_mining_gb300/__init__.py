@@ -28,7 +28,8 @@ STATUS_NAMES = {
 
 # every symbol include/gspan_gb300.h declares
 EXPORTS = [
-    "gs_last_error", "gs_filetype_from_name", "gs_db_load", "gs_db_from_arrays", "gs_db_generate",
+    "gs_last_error", "gs_filetype_from_name", "gs_db_load", "gs_db_from_arrays", "gs_db_from_arrays_device",
+    "gs_db_generate",
     "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
     "gs_mine", "gs_mine_ex", "gs_mine_collect", "gs_patterns_free", "gs_mine_batch", "gs_support_count",
     "gs_support_count_noalloc",
@@ -130,6 +131,8 @@ def lib():
     L.gs_db_load.restype = vp
     L.gs_db_from_arrays.argtypes = [i32, i32, i32, i32, pi32, pi32, pi32, pi32, pi32]
     L.gs_db_from_arrays.restype = vp
+    L.gs_db_from_arrays_device.argtypes = [i32, i32, i32, i32, pi32, pi32, pi32, pi32, pi32]
+    L.gs_db_from_arrays_device.restype = vp
     L.gs_db_generate.argtypes = [i32, ctypes.c_uint64, ctypes.c_double, pi32]
     L.gs_db_generate.restype = vp
     L.gs_db_write.argtypes = [vp, ctypes.c_char_p, i32]
@@ -224,20 +227,18 @@ class Database:
 
     @classmethod
     def from_arrays(cls, db_size, max_graph_vertex_count, edges, edges_labels, vertex_labels, vertex_offsets,
-                    vertex_count=-1):
-        """The reference's cudabin arrays (graph_database_cuda); sequences of int32."""
-        def arr(x):
-            x = list(x)
-            return (ctypes.c_int32 * max(1, len(x)))(*x), len(x)
-        e, ne = arr(edges)
-        el, _ = arr(edges_labels)
-        vl, _ = arr(vertex_labels)
-        vo, _ = arr(vertex_offsets)
-        st = ctypes.c_int32(0)
+                    vertex_count=-1, device=False):
+        """The reference's cudabin arrays (graph_database_cuda): int32 numpy arrays
+        or sequences.  device=True converts on the GPU (gs_db_from_arrays_device)."""
+        import numpy as np
+        keep = [np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+                for x in (edges, edges_labels, vertex_labels, vertex_offsets)]
         P = ctypes.POINTER(ctypes.c_int32)
-        h = lib().gs_db_from_arrays(int(db_size), ne, int(max_graph_vertex_count), int(vertex_count),
-                                    ctypes.cast(e, P), ctypes.cast(el, P), ctypes.cast(vl, P), ctypes.cast(vo, P),
-                                    ctypes.byref(st))
+        e, el, vl, vo = (x.ctypes.data_as(P) for x in keep)
+        st = ctypes.c_int32(0)
+        fn = lib().gs_db_from_arrays_device if device else lib().gs_db_from_arrays
+        h = fn(int(db_size), int(keep[0].size), int(max_graph_vertex_count), int(vertex_count), e, el, vl, vo,
+               ctypes.byref(st))
         if not h:
             _check(st.value or 3)
         return cls(h)

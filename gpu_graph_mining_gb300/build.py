@@ -21,7 +21,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SRCS = ["gs_kernels.cu", "gs_wave.cu", "gs_ismin.cu", "gs_noalloc.cu"]
+CU_SRCS = ["gs_kernels.cu", "gs_wave.cu", "gs_ismin.cu", "gs_ingest.cu", "gs_noalloc.cu"]
 CPP_SRCS = ["gs_db.cpp", "gs_dfs.cpp", "gs_engine.cpp", "gs_capi.cpp", "gs_server.cpp"]
 
 

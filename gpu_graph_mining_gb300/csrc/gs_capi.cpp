@@ -135,6 +135,31 @@ gs_db *gs_db_from_arrays(int32_t db_size, int32_t edges_sizes, int32_t max_graph
   return finish_load(r, db, status);
 }
 
+gs_db *gs_db_from_arrays_device(int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
+                                int32_t vertex_count, const int32_t *edges, const int32_t *edges_labels,
+                                const int32_t *vertex_labels, const int32_t *vertex_offsets, gs_status *status)
+{
+  (void)vertex_count;
+  if(db_size < 0 || edges_sizes < 0 || max_graph_vertex_count < 0 ||
+     (edges_sizes > 0 && (!edges || !edges_labels)) || !vertex_offsets ||
+     ((int64_t)db_size * max_graph_vertex_count > 0 && !vertex_labels)) {
+    if(status) *status = set_err(GS_ERR_USAGE, "invalid arrays");
+    return nullptr;
+  }
+  gs_db *db = new gs_db();
+  try {
+    gsgb::ingest_cudabin_device(db->d, db_size, edges_sizes, max_graph_vertex_count, edges, edges_labels,
+                                vertex_labels, vertex_offsets);
+  } catch(const gsgb::Error &e) {
+    delete db;
+    if(status) *status = set_err(e.code, e.what());
+    return nullptr;
+  }
+  if(status) *status = GS_OK;
+  t_err.clear();
+  return db;
+}
+
 gs_db *gs_db_generate(int32_t config, uint64_t seed, double scale, gs_status *status)
 {
   gsgb::GenParams p;
@@ -150,6 +175,11 @@ gs_db *gs_db_generate(int32_t config, uint64_t seed, double scale, gs_status *st
 gs_status gs_db_write(const gs_db *db, const char *path, int32_t filetype)
 {
   if(!db || !path) return set_err(GS_ERR_USAGE, "null argument");
+  try {
+    const_cast<gs_db *>(db)->d.ensure_host();
+  } catch(const gsgb::Error &e) {
+    return set_err(e.code, e.what());
+  }
   gsgb::LoadResult r = gsgb::write_database(db->d.host, path, filetype);
   if(!r.error.empty()) return set_err(r.code ? r.code : GS_ERR_IO, r.error);
   return GS_OK;
@@ -161,8 +191,8 @@ gs_status gs_db_get_info(const gs_db *db, gs_db_info *info)
 {
   if(!db || !info) return set_err(GS_ERR_USAGE, "null argument");
   info->graphs = db->d.host.n_graphs;
-  info->vertices = db->d.host.n_vertices();
-  info->adjacency_entries = db->d.host.n_adj();
+  info->vertices = db->d.n_vertices();
+  info->adjacency_entries = db->d.n_adj();
   info->vertex_labels = db->d.VL;
   info->edge_labels = db->d.EL;
   info->device_bytes = db->d.resident ? (int64_t)db->d.d_bytes : 0;

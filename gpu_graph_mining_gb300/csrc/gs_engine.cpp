@@ -168,6 +168,29 @@ void Database::upload()
   resident = true;
 }
 
+void Database::ensure_host()
+{
+  if(!device_only || (int64_t)host.vlabel.size() == dev_vertices) return;
+  const int64_t V = dev_vertices, E2 = dev_adj;
+  const int32_t G = host.n_graphs;
+  std::vector<unsigned long long> adj(E2 + 1);
+  std::vector<int32_t> off(V + 1), vl(V + 1), vb(G + 1);
+  CK(cudaMemcpy(adj.data(), dev.adj, sizeof(unsigned long long) * E2, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(off.data(), dev.adj_off, sizeof(int32_t) * (V + 1), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(vl.data(), dev.vlabel, sizeof(int32_t) * V, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(vb.data(), dev.vbase, sizeof(int32_t) * (G + 1), cudaMemcpyDeviceToHost));
+  host.vbase.assign(vb.begin(), vb.end());
+  host.aoff.assign(off.begin(), off.end());
+  host.vlabel.resize(V);
+  for(int64_t v = 0; v < V; v++) host.vlabel[v] = labels.vlabel_of[vl[v]];
+  host.adj_to.resize(E2);
+  host.adj_el.resize(E2);
+  for(int64_t k = 0; k < E2; k++) {
+    host.adj_to[k] = (int32_t)(adj[k] & 0xffffffffull);
+    host.adj_el[k] = labels.elabel_of[(uint32_t)(adj[k] >> 48)];
+  }
+}
+
 void Database::release()
 {
   if(d_block) cudaFree(d_block);

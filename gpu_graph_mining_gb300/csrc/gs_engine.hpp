@@ -56,12 +56,27 @@ struct Database {
   DevDB dev{};
   int32_t *d_root_off = nullptr;
   bool resident = false;
+  // built on the device from cudabin arrays (ingest_cudabin_device): the host
+  // arrays stay empty until ensure_host() downloads them
+  bool device_only = false;
+  int64_t dev_vertices = 0, dev_adj = 0;
 
   void prepare();   // label compaction and pair tables (host only)
   void upload();    // device copy (idempotent)
   void release();   // frees the device copy
+  void ensure_host();  // host arrays of a device-built database (original labels)
+  int64_t n_vertices() const { return device_only ? dev_vertices : host.n_vertices(); }
+  int64_t n_adj() const { return device_only ? dev_adj : host.n_adj(); }
   ~Database();
 };
+
+// Builds db's device copy directly from the reference's cudabin arrays (host
+// memory) on the GPU: the checks and the result of db_from_cudabin_arrays +
+// validate_simple + Database::prepare/upload, without the host conversion
+// (gs_ingest.cu).  Throws Error.
+void ingest_cudabin_device(Database &db, int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
+                           const int32_t *edges, const int32_t *edges_labels, const int32_t *vertex_labels,
+                           const int32_t *vertex_offsets);
 
 using EmitFn = void (*)(const int32_t *dfs5xN, int32_t n_edges, int64_t support, void *user);
 

@@ -235,7 +235,7 @@ private:
   {
     auto it = hist_.find(HistKey{ r.db_id, r.minsup, r.max_edges });
     if(it != hist_.end()) return it->second;
-    return 20 * dbs_[r.db_id]->host.n_adj();
+    return 20 * dbs_[r.db_id]->n_adj();
   }
 
   // under m_: end a request

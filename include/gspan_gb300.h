@@ -81,6 +81,19 @@ GS_API gs_db *gs_db_from_arrays(int32_t db_size, int32_t edges_sizes, int32_t ma
                                 int32_t vertex_count, const int32_t *edges, const int32_t *edges_labels,
                                 const int32_t *vertex_labels, const int32_t *vertex_offsets, gs_status *status);
 
+/* gs_db_from_arrays built on the GPU: the arrays are copied to the device
+ * (as graph_database_cuda::copy_to_device, cuda_graph_types.cpp:166-196,
+ * does) and converted, checked, label-compacted and indexed there, so no
+ * host conversion runs.  Same arguments, checks and mining results as
+ * gs_db_from_arrays; the database is resident when the call returns.  The
+ * host arrays are built only if the database is written (gs_db_write).
+ * Vertex label values must span at most 2^22 and the label alphabet must
+ * keep |VL|*|EL|*|VL| <= 2^25, else GS_ERR_LIMIT (use gs_db_from_arrays). */
+GS_API gs_db *gs_db_from_arrays_device(int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
+                                       int32_t vertex_count, const int32_t *edges, const int32_t *edges_labels,
+                                       const int32_t *vertex_labels, const int32_t *vertex_offsets,
+                                       gs_status *status);
+
 /* Seeded synthetic database of benchmark configuration 1..5 with `scale`
  * times its graph count.  No counterpart in the reference: it stands in for
  * the PAFI graph generator the reference's experiments used
