@@ -35,7 +35,7 @@ EXPORTS = [
     "gs_support_count_noalloc",
     "gs_dfs_code_is_min", "gs_engine_reset", "gs_engine_set_pool_bytes",
     "gs_server_opts_default", "gs_server_create", "gs_server_add_db", "gs_server_submit", "gs_server_poll",
-    "gs_server_cancel", "gs_server_get_stats", "gs_server_destroy",
+    "gs_server_cancel", "gs_server_get_stats", "gs_server_destroy", "gs_autotune",
 ]
 
 
@@ -50,7 +50,17 @@ class MineOpts(ctypes.Structure):
                 ("wave_nodes", ctypes.c_int32), ("threads", ctypes.c_int32),
                 ("wave_rows", ctypes.c_int64), ("wave_words", ctypes.c_int64),
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
-                ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32)]
+                ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
+                ("count_grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("trials", ctypes.c_int32), ("wave_nodes", ctypes.c_int32), ("wave_rows", ctypes.c_int64),
+                ("count_grid", ctypes.c_int32), ("reserved", ctypes.c_int32), ("base_ms", ctypes.c_double),
+                ("best_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
 class MineStats(ctypes.Structure):
@@ -185,6 +195,8 @@ def lib():
     L.gs_server_get_stats.restype = i32
     L.gs_server_destroy.argtypes = [vp]
     L.gs_server_destroy.restype = None
+    L.gs_autotune.argtypes = [ctypes.POINTER(vp), i32, pi32, ctypes.POINTER(MineOpts), ctypes.POINTER(TuneReport)]
+    L.gs_autotune.restype = i32
     _lib = L
     return L
 
@@ -281,7 +293,7 @@ def code_to_string(code):
 
 
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
-          root_part=0, root_parts=1, min_check=0, launch_mode=0):
+          root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0):
     o = MineOpts()
     lib().gs_mine_opts_default(ctypes.byref(o))
     o.max_edges = int(max_edges)
@@ -298,11 +310,12 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
     o.root_parts = int(root_parts)
     o.min_check = int(min_check)
     o.launch_mode = int(launch_mode)
+    o.count_grid = int(count_grid)
     return o
 
 
 def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
-         wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0):
+         wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0):
     """Mines db at absolute support minsup.
 
     Returns (patterns, stats): patterns is a list of (code, support) with code a
@@ -320,7 +333,7 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
 
     fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
     o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check,
-              launch_mode)
+              launch_mode, count_grid)
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()
@@ -356,7 +369,19 @@ def _take_patterns(p, decode=True):
         lib().gs_patterns_free(p)
 
 
-def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True):
+def autotune(dbs, minsups, **kw):
+    """Picks wave options for mining these databases together (gs_autotune).
+    Returns (options for mine / mine_batch / mine_collect, report)."""
+    o = _opts(**kw)
+    hs = (ctypes.c_void_p * len(dbs))(*[d.handle for d in dbs])
+    ms = (ctypes.c_int32 * len(dbs))(*[int(m) for m in minsups])
+    r = TuneReport()
+    _check(lib().gs_autotune(hs, len(dbs), ms, ctypes.byref(o), ctypes.byref(r)))
+    return {"wave_nodes": o.wave_nodes, "wave_rows": o.wave_rows, "count_grid": o.count_grid}, r.as_dict()
+
+
+def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True,
+               **kw):
     """Mines several databases in shared launches; returns ([patterns per db], stats)."""
     out = [[] for _ in dbs]
 
@@ -367,7 +392,7 @@ def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=No
     fn = BATCH_EMIT_FN(cb) if collect else ctypes.cast(None, BATCH_EMIT_FN)
     hs = (ctypes.c_void_p * len(dbs))(*[d.handle for d in dbs])
     ms = (ctypes.c_int32 * len(dbs))(*[int(m) for m in minsups])
-    o = _opts(max_edges, label_style, wave_nodes, threads)
+    o = _opts(max_edges, label_style, wave_nodes, threads, **kw)
     st = MineStats()
     _check(lib().gs_mine_batch(hs, len(dbs), ms, ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()

@@ -49,6 +49,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   if(o->wave_words > 0) m.wave_words = o->wave_words;
   m.min_check = o->min_check == 1 ? 1 : 0;
   m.launch_mode = o->launch_mode == 1 ? 1 : 0;
+  if(o->count_grid > 0 && o->count_grid <= 1024) m.count_grid = o->count_grid;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -226,6 +227,8 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->root_parts = 1;
   o->min_check = m.min_check;
   o->launch_mode = m.launch_mode;
+  o->count_grid = m.count_grid;
+  o->reserved = 0;
 }
 
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,
@@ -301,6 +304,45 @@ gs_status gs_mine_batch(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups
   int rc = gsgb::run_jobs(jobs, mo, &st, err);
   fill_stats(st, stats);
   if(rc != 0) return set_err(rc, err);
+  t_err.clear();
+  return GS_OK;
+}
+
+gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, gs_mine_opts *opts,
+                      gs_tune_report *report)
+{
+  if(n <= 0 || !dbs || !abs_minsups || !opts) return set_err(GS_ERR_USAGE, "invalid autotune arguments");
+  gsgb::MineOptions mo;
+  fill_opts(opts, mo);
+  std::vector<gsgb::MineJob> jobs(n);
+  for(int32_t i = 0; i < n; i++) {
+    if(!dbs[i]) return set_err(GS_ERR_USAGE, "null database");
+    jobs[i].db = &dbs[i]->d;
+    jobs[i].minsup = abs_minsups[i];
+    jobs[i].opt = mo;
+    jobs[i].tag = i;
+  }
+  gsgb::MineOptions best;
+  std::vector<gsgb::TuneTrial> trials;
+  std::string err;
+  const int rc = gsgb::autotune_jobs(jobs, mo, best, trials, err);
+  if(rc != 0) return set_err(rc, err);
+  opts->wave_nodes = best.wave_nodes;
+  opts->wave_rows = best.wave_rows;
+  opts->count_grid = best.count_grid;
+  if(report) {
+    report->trials = (int32_t)trials.size();
+    report->wave_nodes = best.wave_nodes;
+    report->wave_rows = best.wave_rows;
+    report->count_grid = best.count_grid;
+    report->reserved = 0;
+    report->base_ms = trials.front().ms;
+    double b = trials.front().ms;
+    for(const auto &t : trials)
+      if(t.wave_nodes == best.wave_nodes && t.wave_rows == best.wave_rows && t.count_grid == best.count_grid)
+        b = t.ms;
+    report->best_ms = b;
+  }
   t_err.clear();
   return GS_OK;
 }

@@ -1511,7 +1511,8 @@ private:
     q.head_host = X.h_head.p;
     q.d2h_bytes = kHeadBytes + sizeof(int4) * (size_t)f.sel_copied;
     q.count = wave_count_call(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, cnt, E.d_bytes.p + 0,
-                              err_flag(), f.rec, f.rec_cap, f.rec ? head + kHeadRecords : nullptr);
+                              err_flag(), f.rec, f.rec_cap, f.rec ? head + kHeadRecords : nullptr,
+                              wo_.count_grid);
     q.screen = screen_keys_call(f.dn, W, kb, cnt, X.d_childmap.p, X.d_listed.p, head + kHeadSelected, err_flag(),
                                 head + kHeadFlags);
     q.listed = count_listed_call(f.dn, X.d_listed.p, f.bm, cnt, X.d_bmx.p, X.d_keyword.p, sel, kb,
@@ -1896,6 +1897,68 @@ bool Scheduler::job_info(int32_t id, JobInfo &out)
   out.done = S->done;
   out.cancelled = S->cancelled;
   return true;
+}
+
+int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptions &best,
+                  std::vector<TuneTrial> &trials, std::string &err)
+{
+  // trials count patterns without emitting them
+  std::vector<MineJob> quiet = jobs;
+  for(auto &j : quiet) {
+    j.emit = nullptr;
+    j.user = nullptr;
+  }
+  auto trial = [&](const MineOptions &o, double &ms) -> int {
+    double b = 1e300;
+    for(int r = 0; r < 2; r++) {
+      MineStats st;
+      std::string e;
+      const int rc = run_jobs(quiet, o, &st, e);
+      if(rc) {
+        err = e;
+        return rc;
+      }
+      b = std::min(b, st.wall_ms);
+    }
+    ms = b;
+    trials.push_back(TuneTrial{ o.wave_nodes, o.wave_rows, o.count_grid, ms });
+    return ST_OK;
+  };
+  MineOptions cur = base;
+  double cur_ms = 0;
+  int rc = trial(cur, cur_ms);
+  if(rc) return rc;
+  // a value replaces the current one only when it is at least 2% faster
+  auto consider = [&](MineOptions o) -> int {
+    double ms = 0;
+    const int r = trial(o, ms);
+    if(r) return r;
+    if(ms < 0.98 * cur_ms) {
+      cur = o;
+      cur_ms = ms;
+    }
+    return ST_OK;
+  };
+  for(int32_t wn : { 1024, 2048, 4096, 8192, 16384 }) {
+    if(wn == cur.wave_nodes) continue;
+    MineOptions o = cur;
+    o.wave_nodes = wn;
+    if((rc = consider(o))) return rc;
+  }
+  for(int64_t wr : { (int64_t)1 << 22, (int64_t)1 << 23, (int64_t)1 << 24, (int64_t)1 << 25 }) {
+    if(wr == cur.wave_rows) continue;
+    MineOptions o = cur;
+    o.wave_rows = wr;
+    if((rc = consider(o))) return rc;
+  }
+  for(int32_t cg : { 16, 32, 48, 64 }) {
+    if(cg == cur.count_grid || (cur.count_grid == 0 && cg == 32)) continue;
+    MineOptions o = cur;
+    o.count_grid = cg;
+    if((rc = consider(o))) return rc;
+  }
+  best = cur;
+  return ST_OK;
 }
 
 int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,

@@ -91,6 +91,7 @@ struct MineOptions {
   int32_t root_parts = 1;
   int32_t min_check = 0;      // canonicality: 0 on the GPU (host for oversized patterns), 1 on the host
   int32_t launch_mode = 0;    // a wave's device work: 0 replayed from a CUDA graph, 1 launched directly
+  int32_t count_grid = 0;     // count-kernel grid cap in blocks per SM (0 = the built-in default)
 };
 
 struct MineStats {
@@ -175,6 +176,21 @@ private:
 // (host arrays; records must satisfy 0 <= key < n_keys, 0 <= graph < n_graphs).
 int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,
                        int32_t *support, std::string &err);
+
+// Autotuning of the wave options for a workload (the jobs, mined as one
+// batch): coordinate descent over the work chunk (wave_nodes), the row budget
+// per wave (wave_rows) and the count kernel's grid cap (count_grid); each
+// trial is a complete mining pass (patterns counted, not emitted), timed on
+// the host clock, best of two.  best receives the fastest options; trials
+// lists (wave_nodes, wave_rows, count_grid, ms) of every trial.
+struct TuneTrial {
+  int32_t wave_nodes;
+  int64_t wave_rows;
+  int32_t count_grid;
+  double ms;
+};
+int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptions &best,
+                  std::vector<TuneTrial> &trials, std::string &err);
 
 // Releases the engine's device pool and scratch (the next call re-creates them).
 void engine_reset();

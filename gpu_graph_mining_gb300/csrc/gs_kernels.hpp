@@ -61,7 +61,7 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
-                           unsigned long long *rec_n);
+                           unsigned long long *rec_n, int32_t grid_per_sm = 0);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,

@@ -369,7 +369,22 @@ template <bool MAT> void dispatch(int kmax, bool small_graphs, const WaveArgs &a
   else dispatch_k<MAT, false>(kmax, a, s);
 }
 
-template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a)
+// SMs of device 0 (the grid caps below are per SM)
+int sm_count()
+{
+  static int n = 0;
+  if(n == 0) {
+    int v = 0;
+    if(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 152;
+    }
+    n = v;
+  }
+  return n;
+}
+
+template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a, int grid_per_sm)
 {
   const size_t smem = sizeof(Smem<KMAX>) * kWarps;
   static bool configured = false;
@@ -378,7 +393,7 @@ template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a)
     configured = true;
   }
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
-  const long long cap = 152LL * GS_WAVE_GRID;
+  const long long cap = (long long)sm_count() * (grid_per_sm > 0 ? grid_per_sm : GS_WAVE_GRID);
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
   KernelCall c;
@@ -390,12 +405,12 @@ template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a)
   return c;
 }
 
-template <bool MASK> KernelCall count_call(int kmax, const WaveArgs &a)
+template <bool MASK> KernelCall count_call(int kmax, const WaveArgs &a, int grid_per_sm)
 {
-  if(kmax <= 8) return count_call_k<8, MASK>(a);
-  if(kmax <= 16) return count_call_k<16, MASK>(a);
-  if(kmax <= 32) return count_call_k<32, MASK>(a);
-  return count_call_k<64, MASK>(a);
+  if(kmax <= 8) return count_call_k<8, MASK>(a, grid_per_sm);
+  if(kmax <= 16) return count_call_k<16, MASK>(a, grid_per_sm);
+  if(kmax <= 32) return count_call_k<32, MASK>(a, grid_per_sm);
+  return count_call_k<64, MASK>(a, grid_per_sm);
 }
 
 }  // namespace
@@ -404,11 +419,11 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
-                           unsigned long long *rec_n)
+                           unsigned long long *rec_n, int32_t grid_per_sm)
 {
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
               nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n };
-  return small_graphs ? count_call<true>(kmax, a) : count_call<false>(kmax, a);
+  return small_graphs ? count_call<true>(kmax, a, grid_per_sm) : count_call<false>(kmax, a, grid_per_sm);
 }
 
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,

@@ -145,6 +145,8 @@ typedef struct gs_mine_opts {
                           or with too many self-embeddings, on the host), 1 = on the host */
   int32_t launch_mode; /* a wave's device work (uploads, clears, count, selection, check, results
                           copy): 0 = replayed from a per-variant CUDA graph, 1 = launched directly */
+  int32_t count_grid;  /* count-kernel grid cap in blocks per SM; 0 = built-in default (32) */
+  int32_t reserved;
 } gs_mine_opts;
 
 typedef struct gs_mine_stats {
@@ -274,6 +276,26 @@ GS_API gs_status gs_server_cancel(gs_server *srv, int64_t request_id);
 GS_API gs_status gs_server_get_stats(gs_server *srv, gs_server_stats *stats);
 /* Cancels what is left, stops the thread, frees the server's device memory. */
 GS_API void gs_server_destroy(gs_server *srv);
+
+/* Autotuner: picks the wave options for a workload (the databases mined
+ * together at their minsups, as gs_mine_batch would).  Coordinate descent
+ * over wave_nodes (1024..16384), wave_rows (2^22..2^25) and count_grid
+ * (16..64 blocks per SM); every trial is a complete mining pass with the
+ * patterns counted, not emitted, best of two on the host clock, and a value
+ * is taken only when it is 2% faster.  opts: in, the starting options (other
+ * fields are kept); out, the tuned ones.  No counterpart in the reference,
+ * whose launch shapes come from a fixed cuda_configurator. */
+typedef struct gs_tune_report {
+  int32_t trials;
+  int32_t wave_nodes;
+  int64_t wave_rows;
+  int32_t count_grid;
+  int32_t reserved;
+  double base_ms;  /* the starting options */
+  double best_ms;  /* the tuned options */
+} gs_tune_report;
+GS_API gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, gs_mine_opts *opts,
+                             gs_tune_report *report);
 
 /* Support of candidate DFS edges from extension records: support[k] = the
  * number of distinct graph ids among the records whose key is k, computed on

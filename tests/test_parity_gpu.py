@@ -243,3 +243,14 @@ def test_direct_launches_equal_graph_replay(gs):
     a, sa = gs.mine(db, s, launch_mode=0)
     b, sb = gs.mine(db, s, launch_mode=1)
     assert a == b and sa["waves"] == sb["waves"]
+
+
+def test_autotune_keeps_results(gs):
+    dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.05) for i in range(3)]
+    sups = [max(2, int(0.05 * len(d))) for d in dbs]
+    opts, rep = gs.autotune(dbs, sups)
+    assert rep["trials"] >= 10 and rep["best_ms"] <= rep["base_ms"] * 1.05
+    assert opts["wave_nodes"] in (1024, 2048, 4096, 8192, 16384)
+    a, _ = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ)
+    b, _ = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, **opts)
+    assert a == b
