@@ -1152,7 +1152,9 @@ private:
     const size_t nw = (size_t)R * words;
     X.d_bm.ensure(nw);
     X.d_bmx.ensure(nw);
-    X.d_cnt.ensure(R);
+    // copies of the root counters: every vertex adds into a few hundred counters
+    const int32_t rcopies = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)1 << 20) / R));
+    X.d_cnt.ensure((size_t)R * rcopies);
     X.d_sup.ensure(R);
     X.d_childmap.ensure(R);
     // pseudo node spanning the root keys, for the support kernel
@@ -1164,9 +1166,9 @@ private:
     std::memcpy(X.h_desc.p, &nd, sizeof(nd));
     h2d(X.d_desc.p, X.h_desc.p, sizeof(nd));
     CK(cudaMemsetAsync(X.d_bm.p, 0, nw * 4, E.stream));
-    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)R * 4, E.stream));
+    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)R * rcopies * 4, E.stream));
     CK(cudaEventRecord(X.ev[0], E.stream));
-    launch_root_count(db.dev, db.d_root_off, X.d_bm.p, X.d_cnt.p, words, E.d_bytes.p + 2, E.stream);
+    launch_root_count(db.dev, db.d_root_off, X.d_bm.p, X.d_cnt.p, words, R, rcopies, E.d_bytes.p + 2, E.stream);
     launch_support((const NodeDesc *)X.d_desc.p, 1, R, X.d_bm.p, X.d_bmx.p, X.d_sup.p, E.stream);
     CK(cudaEventRecord(X.ev[1], E.stream));
     st_.launches += 2;
@@ -1463,7 +1465,11 @@ private:
     f.kmax = kmax;
     f.small = small;
     f.tb = tb;
-    const size_t cnt_bytes = Carver::round(sizeof(int32_t) * (size_t)std::max(kb, 1));
+    // copies of the wave's counters: the warps of a large node all add into that
+    // node's few counters; copies spread them over L2 slices (summed by screening)
+    const int32_t ccopies = (int32_t)std::max<int64_t>(1, std::min<int64_t>(16, ((int64_t)1 << 22) / std::max(kb, 1)));
+    const long long cstride = (long long)Carver::round(sizeof(int32_t) * (size_t)std::max(kb, 1)) / 4;
+    const size_t cnt_bytes = sizeof(int32_t) * (size_t)cstride * ccopies;
     const size_t zero_bytes = cnt_bytes + sizeof(uint32_t) * (size_t)std::max<int64_t>(bb, 1);
     X.d_zero.ensure(zero_bytes);
     X.d_head.ensure(kHeadBytes + sizeof(int4) * (size_t)std::max(kb, 1));
@@ -1512,9 +1518,9 @@ private:
     q.d2h_bytes = kHeadBytes + sizeof(int4) * (size_t)f.sel_copied;
     q.count = wave_count_call(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, cnt, E.d_bytes.p + 0,
                               err_flag(), f.rec, f.rec_cap, f.rec ? head + kHeadRecords : nullptr,
-                              wo_.count_grid);
-    q.screen = screen_keys_call(f.dn, W, kb, cnt, X.d_childmap.p, X.d_listed.p, head + kHeadSelected, err_flag(),
-                                head + kHeadFlags);
+                              wo_.count_grid, ccopies, cstride);
+    q.screen = screen_keys_call(f.dn, W, kb, cnt, ccopies, cstride, X.d_childmap.p, X.d_listed.p,
+                                head + kHeadSelected, err_flag(), head + kHeadFlags);
     q.listed = count_listed_call(f.dn, X.d_listed.p, f.bm, cnt, X.d_bmx.p, X.d_keyword.p, sel, kb,
                                  head + kHeadSelected);
     q.with_min = wo_.min_check == 0;

@@ -47,6 +47,7 @@ __device__ __forceinline__ unsigned lanemask_lt()
 template <bool MAT>
 __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__restrict__ root_off, uint32_t *bm,
                                            const int32_t *__restrict__ bmx, int32_t *cnt, int32_t words,
+                                           int32_t R, int32_t cnt_copies,
                                            const int32_t *__restrict__ childmap, int32_t *cursor,
                                            const ChildOut *__restrict__ outs, unsigned long long *bytes,
                                            unsigned int *err)
@@ -56,7 +57,10 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
   const long long tiles = ((long long)db.n_vertices + 31) / 32;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   unsigned long long mine = 0;
-  for(long long tile = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < tiles; tile += nwarps) {
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // this warp's copy of the root counters (copies spread the hot counters over L2 slices)
+  int32_t *const cnt_copy = MAT ? nullptr : cnt + (gw % (cnt_copies > 0 ? cnt_copies : 1)) * (long long)R;
+  for(long long tile = gw; tile < tiles; tile += nwarps) {
     const long long v = tile * 32 + lane;
     const bool valid = v < db.n_vertices;
     const int a0 = valid ? __ldg(&db.adj_off[v]) : 0;
@@ -86,13 +90,15 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
       const int g_o = __shfl_sync(full, g, o);
       int key = -1, w = 0;
       if(has) {
+        // entry, pair index and the label's first key: independent loads, in flight together
         const unsigned long long ent = __ldg(&db.adj[e]);
+        const int pr = __ldg(&db.adj_pair[e]);
+        const int ro = __ldg(&root_off[fl_o]);
         w = (int)(unsigned)(ent & 0xffffffffull);
         const unsigned hi = (unsigned)(ent >> 32);
-        const int el = (int)(hi >> 16), wl = (int)(hi & 0xffffu);
+        const int wl = (int)(hi & 0xffffu);
         mine += 8;
-        (void)el;
-        if(fl_o <= wl) key = root_off[fl_o] + __ldg(&db.adj_pair[e]);
+        if(fl_o <= wl) key = ro + pr;
       }
       if(!MAT) {
         if(key >= 0) {
@@ -100,7 +106,7 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
           mine += 8;
         }
         const unsigned peers = __match_any_sync(full, key);
-        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[key], __popc(peers));
+        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt_copy[key], __popc(peers));
       } else {
         const int c = key >= 0 ? childmap[key] : -1;
         const unsigned peers = __match_any_sync(full, c);
@@ -127,9 +133,20 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
 }
 
 __global__ void __launch_bounds__(kBlock) k_root_count(DevDB db, const int32_t *__restrict__ root_off, uint32_t *bm,
-                                                        int32_t *cnt, int32_t words, unsigned long long *bytes)
+                                                        int32_t *cnt, int32_t words, int32_t R, int32_t cnt_copies,
+                                                        unsigned long long *bytes)
 {
-  root_tiles<false>(db, root_off, bm, nullptr, cnt, words, nullptr, nullptr, nullptr, bytes, nullptr);
+  root_tiles<false>(db, root_off, bm, nullptr, cnt, words, R, cnt_copies, nullptr, nullptr, nullptr, bytes, nullptr);
+}
+
+// cnt[k] += cnt[q * n + k] for the other copies q
+__global__ void __launch_bounds__(kBlock) k_sum_copies(int32_t *cnt, int32_t n, int32_t copies)
+{
+  for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int c = cnt[k];
+    for(int q = 1; q < copies; q++) c += cnt[(long long)q * n + k];
+    cnt[k] = c;
+  }
 }
 
 __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int32_t *__restrict__ root_off,
@@ -138,8 +155,8 @@ __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int
                                                               const int32_t *__restrict__ childmap, int32_t *cursor,
                                                               const ChildOut *__restrict__ outs, unsigned int *err)
 {
-  root_tiles<true>(db, root_off, const_cast<uint32_t *>(bm), bmx, nullptr, words, childmap, cursor, outs, nullptr,
-                   err);
+  root_tiles<true>(db, root_off, const_cast<uint32_t *>(bm), bmx, nullptr, words, 0, 0, childmap, cursor, outs,
+                   nullptr, err);
 }
 
 __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__ nodes, int nnodes, int total_keys,
@@ -178,8 +195,8 @@ __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__
 // first bitmap word.  counters: [0] selected, [1] embeddings of all keys,
 // [2] listed keys.
 __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restrict__ nodes, int nnodes,
-                                                         int total_keys, const int32_t *__restrict__ cnt,
-                                                         int32_t *childmap, int2 *listed,
+                                                         int total_keys, int32_t *cnt, int cnt_copies,
+                                                         long long cnt_stride, int32_t *childmap, int2 *listed,
                                                          unsigned long long *counters,
                                                          const unsigned int *err, unsigned long long *err_copy)
 {
@@ -194,7 +211,13 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
   const long long n32 = ((long long)total_keys + 31) & ~31ll;
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n32; i += stride) {
     const int key = (int)i;
-    const int c = key < total_keys ? cnt[key] : 0;
+    int c = 0;
+    if(key < total_keys) {
+      // the count pass spread its adds over copies: their sum, kept in copy 0
+      c = cnt[key];
+      for(int q = 1; q < cnt_copies; q++) c += cnt[q * cnt_stride + key];
+      if(cnt_copies > 1) cnt[key] = c;
+    }
     int n = 0;
     bool cand = false;
     if(c > 0) {
@@ -287,9 +310,11 @@ inline int grid_for(long long n)
 }  // namespace
 
 void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
-                       unsigned long long *bytes, cudaStream_t s)
+                       int32_t R, int32_t cnt_copies, unsigned long long *bytes, cudaStream_t s)
 {
-  k_root_count<<<grid_for((long long)db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, cnt, words, bytes);
+  k_root_count<<<grid_for((long long)db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, cnt, words, R, cnt_copies,
+                                                                      bytes);
+  if(cnt_copies > 1) k_sum_copies<<<grid_for(R), kBlock, 0, s>>>(cnt, R, cnt_copies);
 }
 
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
@@ -307,9 +332,9 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
   k_records_bitmap<<<grid_for(n), kBlock, 0, s>>>(keys, gids, n, words, bm);
 }
 
-KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const int32_t *cnt,
-                            int32_t *childmap, int2 *listed, unsigned long long *counters, const unsigned int *err,
-                            unsigned long long *err_copy)
+KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
+                            int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
+                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy)
 {
   KernelCall c;
   c.func = (const void *)k_screen_keys;
@@ -319,6 +344,8 @@ KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total
   c.arg(nnodes);
   c.arg(total_keys);
   c.arg(cnt);
+  c.arg(cnt_copies);
+  c.arg(cnt_stride);
   c.arg(childmap);
   c.arg(listed);
   c.arg(counters);

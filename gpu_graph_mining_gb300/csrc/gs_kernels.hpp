@@ -45,8 +45,10 @@ private:
 // entry (v -> w) with label(v) <= label(w) is a 1-edge embedding
 // (get_forward_root, src/globals/graph_types.cpp:365-375).
 // Sets support-bitmap bit [key][graph] and counts embeddings per key.
+// cnt holds cnt_copies copies of the R root counters, R apart (summed into the
+// first copy before the call returns on the stream).
 void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
-                       unsigned long long *bytes, cudaStream_t s);
+                       int32_t R, int32_t cnt_copies, unsigned long long *bytes, cudaStream_t s);
 // Writes the two columns and graph ranks of every selected root key.
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
                              int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
@@ -61,7 +63,8 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
-                           unsigned long long *rec_n, int32_t grid_per_sm = 0);
+                           unsigned long long *rec_n, int32_t grid_per_sm, int32_t cnt_copies,
+                           long long cnt_stride);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
@@ -87,9 +90,9 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 // counters: [0] selected keys, [1] embeddings of all keys, [2] keys listed for
 // counting; listed and sel hold total_keys entries.  *err_copy = *err (the
 // consistency flags after the count pass).
-KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const int32_t *cnt,
-                            int32_t *childmap, int2 *listed, unsigned long long *counters, const unsigned int *err,
-                            unsigned long long *err_copy);
+KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
+                            int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
+                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy);
 KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, const int32_t *cnt,
                              int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
                              unsigned long long *counters);

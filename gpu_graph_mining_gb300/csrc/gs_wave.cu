@@ -70,6 +70,10 @@ struct WaveArgs {
   int4 *rec;
   long long rec_cap;
   unsigned long long *rec_n;  // records produced (may exceed rec_cap: then none past it are written)
+  // count pass: cnt holds cnt_copies copies of the wave's counters, cnt_stride
+  // apart; warp w adds into copy w % cnt_copies (summed by the screening pass)
+  int cnt_copies;
+  long long cnt_stride;
 };
 
 template <int KMAX> struct Smem {
@@ -111,6 +115,7 @@ k_wave(const WaveArgs a)
   // starts "full" so the first batch reserves a chunk
   long long chunk_base = -1;
   int chunk_fill = kRecChunk;
+  int32_t *const cnt_copy = MAT ? nullptr : a.cnt + (gwarp % (a.cnt_copies > 0 ? a.cnt_copies : 1)) * a.cnt_stride;
 
   for(long long tile = gwarp; tile < a.total_tiles; tile += nwarps) {
     // ---- the tile's node (warp-uniform: tiles never span nodes)
@@ -274,8 +279,10 @@ k_wave(const WaveArgs a)
         if(key >= 0) atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
         const unsigned ext = __ballot_sync(kFull, key >= 0);  // every lane takes part
         if(lane == 0) mine += 8ull * __popc(ext);
+        // one counter add per distinct key of the step, into this warp's copy
+        // of the counters (copies spread a node's hot counters over L2 slices)
         const unsigned peers = __match_any_sync(kFull, key);
-        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&a.cnt[key_base + key], __popc(peers));
+        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt_copy[key_base + key], __popc(peers));
         if(a.rec && ext) {
           // append this step's extensions to the warp's current chunk of
           // kRecChunk records; a batch that does not fit is split across a
@@ -419,10 +426,11 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
-                           unsigned long long *rec_n, int32_t grid_per_sm)
+                           unsigned long long *rec_n, int32_t grid_per_sm, int32_t cnt_copies,
+                           long long cnt_stride)
 {
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
-              nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n };
+              nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n, cnt_copies, cnt_stride };
   return small_graphs ? count_call<true>(kmax, a, grid_per_sm) : count_call<false>(kmax, a, grid_per_sm);
 }
 
