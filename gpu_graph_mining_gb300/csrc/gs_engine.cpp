@@ -954,6 +954,8 @@ struct Flight {
   long long rec_cap = 0;
   int64_t sel_copied = 0;    // selected entries copied back with the results
   uint32_t *bm = nullptr;    // the wave's support bitmaps (in the zeroed region)
+  int32_t *cnt = nullptr;    // its counter copies, cstride apart (cursors of the records materialise)
+  long long cstride = 0;
 };
 
 // The wave scheduler.  Jobs join at any time (add) and leave when their last
@@ -1251,8 +1253,10 @@ private:
       std::memcpy(X.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
       h2d(X.d_outs.p, X.h_outs.p, sizeof(ChildOut) * outs.size());
       h2d(X.d_childmap.p, X.h_childmap.p, (size_t)R * 4);
-      CK(cudaMemsetAsync(X.d_cursor.p, 0, outs.size() * 4, E.stream));
-      launch_root_materialize(db.dev, db.d_root_off, X.d_bm.p, X.d_bmx.p, words, X.d_childmap.p, X.d_cursor.p,
+      // cursors: the root counter copies hold each copy's offset; copy 0 (the
+      // totals, already copied back) starts at 0
+      CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)R * 4, E.stream));
+      launch_root_materialize(db.dev, db.d_root_off, X.d_bm.p, X.d_bmx.p, words, X.d_childmap.p, X.d_cnt.p, R, rcopies,
                               X.d_outs.p, err_flag(), E.stream);
       st_.launches++;
     }
@@ -1345,7 +1349,7 @@ private:
     std::vector<PNode> &nodes = f.nodes;
     std::vector<NodeLayout> &lays = f.lays;  // kept between waves: layouts reuse their vectors
     nodes.clear();
-    int64_t rows = 0, words = 0;
+    int64_t rows = 0, words = 0, wkeys = 0;
     bool full = false;
     for(size_t oi = 0; oi < order_.size() && !full; oi++) {
       JobState &S = *jobs_[order_[oi]];
@@ -1357,12 +1361,15 @@ private:
         layout_node(top, db, L);
         const int32_t nk = layout_nkeys(L, db);
         const int64_t w = (int64_t)nk * words_for(top.support);
-        if(!nodes.empty() && (rows + top.nrows > wo_.wave_rows || words + w > wo_.wave_words)) {
+        // (keys per wave stay below 2^26: records carry a wave key in 27 bits)
+        if(!nodes.empty() && (rows + top.nrows > wo_.wave_rows || words + w > wo_.wave_words ||
+                              wkeys + nk >= ((int64_t)1 << 26))) {
           full = true;
           break;
         }
         rows += top.nrows;
         words += w;
+        wkeys += nk;
         nodes.push_back(std::move(top));
         S.stack.pop_back();
         stacked_--;
@@ -1467,7 +1474,9 @@ private:
     f.tb = tb;
     // copies of the wave's counters: the warps of a large node all add into that
     // node's few counters; copies spread them over L2 slices (summed by screening)
-    const int32_t ccopies = (int32_t)std::max<int64_t>(1, std::min<int64_t>(16, ((int64_t)1 << 22) / std::max(kb, 1)));
+    // (records hold a key in 27 bits next to the copy: one copy beyond that)
+    const int32_t ccopies =
+        kb >= (1 << 27) ? 1 : (int32_t)std::max<int64_t>(1, std::min<int64_t>(16, ((int64_t)1 << 22) / std::max(kb, 1)));
     const long long cstride = (long long)Carver::round(sizeof(int32_t) * (size_t)std::max(kb, 1)) / 4;
     const size_t cnt_bytes = sizeof(int32_t) * (size_t)cstride * ccopies;
     const size_t zero_bytes = cnt_bytes + sizeof(uint32_t) * (size_t)std::max<int64_t>(bb, 1);
@@ -1478,6 +1487,8 @@ private:
     X.d_keyword.ensure(std::max(kb, 1));
     X.d_listed.ensure(std::max(kb, 1));
     int32_t *cnt = (int32_t *)X.d_zero.p;
+    f.cnt = cnt;
+    f.cstride = cstride;
     f.bm = (uint32_t *)(X.d_zero.p + cnt_bytes);
     unsigned long long *head = (unsigned long long *)X.d_head.p;
     int4 *sel = (int4 *)(X.d_head.p + kHeadBytes);
@@ -1719,8 +1730,8 @@ private:
                               X.d_cursor.p, (int32_t)outs.size(), E.stream);
       if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
-        launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, f.bm, X.d_bmx.p, X.d_cursor.p, douts,
-                                   E.d_bytes.p + 1, err_flag(), E.stream);
+        launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, f.bm, X.d_bmx.p, f.cnt, f.cstride,
+                                   douts, E.d_bytes.p + 1, err_flag(), E.stream);
       } else {
         // records overflowed (or are disabled): enumerate again
         launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, X.d_bmx.p,

@@ -59,7 +59,8 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
   unsigned long long mine = 0;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   // this warp's copy of the root counters (copies spread the hot counters over L2 slices)
-  int32_t *const cnt_copy = MAT ? nullptr : cnt + (gw % (cnt_copies > 0 ? cnt_copies : 1)) * (long long)R;
+  const int cnt_copy_idx = (int)(gw % (cnt_copies > 0 ? cnt_copies : 1));
+  int32_t *const cnt_copy = MAT ? nullptr : cnt + cnt_copy_idx * (long long)R;
   for(long long tile = gw; tile < tiles; tile += nwarps) {
     const long long v = tile * 32 + lane;
     const bool valid = v < db.n_vertices;
@@ -112,7 +113,9 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
         const unsigned peers = __match_any_sync(full, c);
         const int leader = __ffs(peers) - 1;
         int pos = 0;
-        if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[c], __popc(peers));
+        // the cursor of this warp's counter copy of the key: the same warp
+        // counted the same entries in the count pass (same grid, same tiles)
+        if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[cnt_copy_idx * (long long)R + key], __popc(peers));
         pos = __shfl_sync(full, pos, leader) + __popc(peers & lanemask_lt());
         if(c >= 0) {
           const long long wi = (long long)key * words + (g_o >> 5);
@@ -139,12 +142,16 @@ __global__ void __launch_bounds__(kBlock) k_root_count(DevDB db, const int32_t *
   root_tiles<false>(db, root_off, bm, nullptr, cnt, words, R, cnt_copies, nullptr, nullptr, nullptr, bytes, nullptr);
 }
 
-// cnt[k] += cnt[q * n + k] for the other copies q
+// copies -> copy 0 the total, copy q >= 1 the count of copies 0..q-1
 __global__ void __launch_bounds__(kBlock) k_sum_copies(int32_t *cnt, int32_t n, int32_t copies)
 {
   for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     int c = cnt[k];
-    for(int q = 1; q < copies; q++) c += cnt[(long long)q * n + k];
+    for(int q = 1; q < copies; q++) {
+      const int x = cnt[(long long)q * n + k];
+      cnt[(long long)q * n + k] = c;
+      c += x;
+    }
     cnt[k] = c;
   }
 }
@@ -153,10 +160,11 @@ __global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int
                                                               const uint32_t *__restrict__ bm,
                                                               const int32_t *__restrict__ bmx, int32_t words,
                                                               const int32_t *__restrict__ childmap, int32_t *cursor,
+                                                              int32_t R, int32_t cnt_copies,
                                                               const ChildOut *__restrict__ outs, unsigned int *err)
 {
-  root_tiles<true>(db, root_off, const_cast<uint32_t *>(bm), bmx, nullptr, words, 0, 0, childmap, cursor, outs,
-                   nullptr, err);
+  root_tiles<true>(db, root_off, const_cast<uint32_t *>(bm), bmx, nullptr, words, R, cnt_copies, childmap, cursor,
+                   outs, nullptr, err);
 }
 
 __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__ nodes, int nnodes, int total_keys,
@@ -213,10 +221,9 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
     const int key = (int)i;
     int c = 0;
     if(key < total_keys) {
-      // the count pass spread its adds over copies: their sum, kept in copy 0
+      // the count pass spread its adds over copies: their total
       c = cnt[key];
       for(int q = 1; q < cnt_copies; q++) c += cnt[q * cnt_stride + key];
-      if(cnt_copies > 1) cnt[key] = c;
     }
     int n = 0;
     bool cand = false;
@@ -225,6 +232,17 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
       ext += (unsigned long long)c;
       n = find_node_by_key(nodes, nnodes, key);
       cand = c >= nodes[n].minsup;
+    }
+    if(cand && cnt_copies > 1) {
+      // a key that may be materialised: copy 0 keeps the total, copy q >= 1
+      // becomes the count of copies 0..q-1 (the offset of its share)
+      int run = cnt[key];
+      for(int q = 1; q < cnt_copies; q++) {
+        const int x = cnt[q * cnt_stride + key];
+        cnt[q * cnt_stride + key] = run;
+        run += x;
+      }
+      cnt[key] = c;
     }
     const unsigned m = __ballot_sync(full, cand);
     if(m) {
@@ -241,7 +259,7 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
 __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restrict__ nodes,
                                                           const int2 *__restrict__ listed,
                                                           const uint32_t *__restrict__ bm,
-                                                          const int32_t *__restrict__ cnt, int32_t *bmx,
+                                                          int32_t *cnt, int32_t *bmx,
                                                           long long *keyword, int4 *sel, int sel_cap,
                                                           unsigned long long *counters)
 {
@@ -269,6 +287,8 @@ __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restr
       keyword[kn.x] = wbase;
       const unsigned long long at = atomicAdd(&counters[0], 1ull);
       if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], 0);
+      // the total has been read: copy 0 turns into the cursor of copy 0's share
+      cnt[kn.x] = 0;
     }
   }
 }
@@ -318,11 +338,13 @@ void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, i
 }
 
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
-                             int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned int *err, cudaStream_t s)
+                             int32_t words, const int32_t *childmap, int32_t *cursor, int32_t R, int32_t cnt_copies,
+                             const ChildOut *outs, unsigned int *err, cudaStream_t s)
 {
-  k_root_materialize<<<grid_for(db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, bmx, words, childmap, cursor, outs,
-                                                                 err);
+  // the same grid as the count pass: warp w processes the same tiles and uses
+  // the same counter copy
+  k_root_materialize<<<grid_for(db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, bmx, words, childmap, cursor, R,
+                                                                 cnt_copies, outs, err);
 }
 
 void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n, int32_t words, uint32_t *bm,
@@ -354,7 +376,7 @@ KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total
   return c;
 }
 
-KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, const int32_t *cnt,
+KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, int32_t *cnt,
                              int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
                              unsigned long long *counters)
 {

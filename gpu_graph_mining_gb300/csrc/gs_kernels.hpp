@@ -49,10 +49,12 @@ private:
 // first copy before the call returns on the stream).
 void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
                        int32_t R, int32_t cnt_copies, unsigned long long *bytes, cudaStream_t s);
-// Writes the two columns and graph ranks of every selected root key.
+// Writes the two columns and graph ranks of every selected root key.  cursor
+// holds cnt_copies copies of R cursors: copy q of a key starts at the count
+// of copies 0..q-1 (as the root count leaves them, with copy 0 reset to 0).
 void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
-                             int32_t words, const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned int *err, cudaStream_t s);
+                             int32_t words, const int32_t *childmap, int32_t *cursor, int32_t R, int32_t cnt_copies,
+                             const ChildOut *outs, unsigned int *err, cudaStream_t s);
 
 // Wave level (gs_wave.cu): a warp per 32 embedding rows of the wave's nodes.
 // kmax = the largest column count of the wave's nodes (selects the instance
@@ -75,9 +77,12 @@ void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long to
 // Materialise from the count pass's records {wave key, x, y, graph rank}:
 // children whose key is selected get column element (x, y) and their graph
 // rank.  keyword[key] = the key's first support-bitmap word.
+// cursor: the wave's counter copies after selection (copy q of a key starts
+// at the count of copies 0..q-1), cursor_stride apart; a record's copy is in
+// bits 27-30 of its key field.
 void launch_materialize_records(const int4 *rec, long long n, const int32_t *childmap, const long long *keyword,
-                                const uint32_t *bm, const int32_t *bmx, int32_t *cursor, const ChildOut *outs,
-                                unsigned long long *bytes, unsigned int *err, cudaStream_t s);
+                                const uint32_t *bm, const int32_t *bmx, int32_t *cursor, long long cursor_stride,
+                                const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s);
 
 // Extension records given as (key, graph id) pairs: sets bit [key][graph].
 // Keys and graph ids must be in range (checked by the caller).
@@ -93,7 +98,7 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
                             int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
                             unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy);
-KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, const int32_t *cnt,
+KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, int32_t *cnt,
                              int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
                              unsigned long long *counters);
 // Canonicality of the selected candidates (gs_ismin.cu): sel[i].w = 1 minimal,

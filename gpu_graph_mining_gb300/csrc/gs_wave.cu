@@ -47,6 +47,8 @@ namespace {
 constexpr int kWarps = GS_WAVE_WARPS;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kRecChunk = 128;  // records a warp reserves at a time
+constexpr int kRecCopyShift = 27;  // record key field: wave key (bits 0-26) | counter copy (27-30)
+constexpr int kRecKeyMask = (1 << kRecCopyShift) - 1;
 
 struct WaveArgs {
   const NodeDesc *nodes;
@@ -115,7 +117,12 @@ k_wave(const WaveArgs a)
   // starts "full" so the first batch reserves a chunk
   long long chunk_base = -1;
   int chunk_fill = kRecChunk;
-  int32_t *const cnt_copy = MAT ? nullptr : a.cnt + (gwarp % (a.cnt_copies > 0 ? a.cnt_copies : 1)) * a.cnt_stride;
+  const int copy = (int)(gwarp % (a.cnt_copies > 0 ? a.cnt_copies : 1));
+  int32_t *const cnt_copy = MAT ? nullptr : a.cnt + copy * a.cnt_stride;
+  // records carry the copy their embedding was counted in (bits 27-30 of the
+  // key field): the materialise pass places it in that copy's share of the
+  // child column
+  const int rec_tag = copy << kRecCopyShift;
 
   for(long long tile = gwarp; tile < a.total_tiles; tile += nwarps) {
     // ---- the tile's node (warp-uniform: tiles never span nodes)
@@ -304,8 +311,8 @@ k_wave(const WaveArgs a)
           }
           if(key >= 0 && dst >= 0 && dst < a.rec_cap) {
             const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
-            a.rec[dst] = bwd ? make_int4(key_base + key, S.phi[k - 1][o], lp_o, g_o)
-                             : make_int4(key_base + key, w, i_o, g_o);
+            a.rec[dst] = bwd ? make_int4((key_base + key) | rec_tag, S.phi[k - 1][o], lp_o, g_o)
+                             : make_int4((key_base + key) | rec_tag, w, i_o, g_o);
           }
           if(lane == 0) mine += 16ull * cntx;
         }
@@ -455,8 +462,9 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
                                                      const int32_t *__restrict__ childmap,
                                                      const long long *__restrict__ keyword,
                                                      const uint32_t *__restrict__ bm, const int32_t *__restrict__ bmx,
-                                                     int32_t *cursor, const ChildOut *__restrict__ outs,
-                                                     unsigned long long *bytes, unsigned int *err)
+                                                     int32_t *cursor, long long cursor_stride,
+                                                     const ChildOut *__restrict__ outs, unsigned long long *bytes,
+                                                     unsigned int *err)
 {
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -464,20 +472,26 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
   // the loop runs a warp-uniform number of times: lanes past n carry no record
   const long long n32 = (n + 31) & ~31ll;
   for(long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n32; r += stride) {
-    int c = -1;
+    int c = -1, key = 0, cp = 0;
     int4 x = make_int4(0, 0, 0, 0);
     if(r < n) {
       x = __ldg(&rec[r]);
-      if(x.x >= 0) c = childmap[x.x];  // key -1: an unused slot of a reserved chunk
+      if(x.x >= 0) {  // key -1: an unused slot of a reserved chunk
+        key = x.x & kRecKeyMask;
+        cp = x.x >> kRecCopyShift;
+        c = childmap[key];
+      }
       mine += 20;
     }
-    const unsigned peers = __match_any_sync(kFull, c);
+    // one cursor per (key, counter copy): copy q of a key starts where the
+    // counts of copies 0..q-1 end, so the adds spread over many addresses
+    const unsigned peers = __match_any_sync(kFull, c >= 0 ? x.x : -1);
     const int leader = __ffs(peers) - 1;
     int pos = 0;
-    if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[c], __popc(peers));
+    if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[cp * cursor_stride + key], __popc(peers));
     pos = __shfl_sync(kFull, pos, leader) + __popc(peers & lanemask_lt());
     if(c >= 0) {
-      const long long wi = keyword[x.x] + (x.w >> 5);
+      const long long wi = keyword[key] + (x.w >> 5);
       const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (x.w & 31)) - 1u));
       const ChildOut out = outs[c];
       if(pos < out.cap) {
@@ -498,13 +512,14 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
 }  // namespace
 
 void launch_materialize_records(const int4 *rec, long long n, const int32_t *childmap, const long long *keyword,
-                                const uint32_t *bm, const int32_t *bmx, int32_t *cursor, const ChildOut *outs,
-                                unsigned long long *bytes, unsigned int *err, cudaStream_t s)
+                                const uint32_t *bm, const int32_t *bmx, int32_t *cursor, long long cursor_stride,
+                                const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s)
 {
   if(n <= 0) return;
   long long blocks = ((n + 31) / 32 * 32 + 255) / 256;
   if(blocks > 152LL * 16) blocks = 152LL * 16;
-  k_mat_records<<<(int)blocks, 256, 0, s>>>(rec, n, childmap, keyword, bm, bmx, cursor, outs, bytes, err);
+  k_mat_records<<<(int)blocks, 256, 0, s>>>(rec, n, childmap, keyword, bm, bmx, cursor, cursor_stride, outs, bytes,
+                                            err);
 }
 
 }  // namespace gsgb
