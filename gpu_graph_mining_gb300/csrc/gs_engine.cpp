@@ -1968,8 +1968,8 @@ int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptio
     o.wave_rows = wr;
     if((rc = consider(o))) return rc;
   }
-  for(int32_t cg : { 16, 32, 48, 64 }) {
-    if(cg == cur.count_grid || (cur.count_grid == 0 && cg == 32)) continue;
+  for(int32_t cg : { 16, 32, 64, 96 }) {
+    if(cg == cur.count_grid || (cur.count_grid == 0 && cg == 64)) continue;
     MineOptions o = cur;
     o.count_grid = cg;
     if((rc = consider(o))) return rc;

@@ -42,11 +42,14 @@ namespace {
 #define GS_WAVE_MINB 0
 #endif
 #ifndef GS_WAVE_GRID
-#define GS_WAVE_GRID 32
+#define GS_WAVE_GRID 64
 #endif
 constexpr int kWarps = GS_WAVE_WARPS;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kRecChunk = 128;  // records a warp reserves at a time
+#ifndef GS_REC_CHUNK
+#define GS_REC_CHUNK 128
+#endif
+constexpr int kRecChunk = GS_REC_CHUNK;  // records a warp reserves at a time
 constexpr int kRecCopyShift = 27;  // record key field: wave key (bits 0-26) | counter copy (27-30)
 constexpr int kRecKeyMask = (1 << kRecCopyShift) - 1;
 

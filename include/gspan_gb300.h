@@ -145,7 +145,7 @@ typedef struct gs_mine_opts {
                           or with too many self-embeddings, on the host), 1 = on the host */
   int32_t launch_mode; /* a wave's device work (uploads, clears, count, selection, check, results
                           copy): 0 = replayed from a per-variant CUDA graph, 1 = launched directly */
-  int32_t count_grid;  /* count-kernel grid cap in blocks per SM; 0 = built-in default (32) */
+  int32_t count_grid;  /* count-kernel grid cap in blocks per SM; 0 = built-in default (64) */
   int32_t reserved;
 } gs_mine_opts;
 
@@ -280,7 +280,7 @@ GS_API void gs_server_destroy(gs_server *srv);
 /* Autotuner: picks the wave options for a workload (the databases mined
  * together at their minsups, as gs_mine_batch would).  Coordinate descent
  * over wave_nodes (1024..16384), wave_rows (2^22..2^25) and count_grid
- * (16..64 blocks per SM); every trial is a complete mining pass with the
+ * (16..96 blocks per SM); every trial is a complete mining pass with the
  * patterns counted, not emitted, best of two on the host clock, and a value
  * is taken only when it is 2% faster.  opts: in, the starting options (other
  * fields are kept); out, the tuned ones.  No counterpart in the reference,
