@@ -29,7 +29,7 @@ STATUS_NAMES = {
 # every symbol include/gspan_gb300.h declares
 EXPORTS = [
     "gs_last_error", "gs_filetype_from_name", "gs_db_load", "gs_db_from_arrays", "gs_db_from_arrays_device",
-    "gs_db_generate",
+    "gs_db_generate", "gs_db_convert",
     "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
     "gs_mine", "gs_mine_ex", "gs_mine_collect", "gs_patterns_free", "gs_mine_batch", "gs_support_count",
     "gs_support_count_noalloc",
@@ -52,6 +52,11 @@ class MineOpts(ctypes.Structure):
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
                 ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
                 ("count_grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ConvertInfo(ctypes.Structure):
+    _fields_ = [("graphs", ctypes.c_int64), ("graphs_fixed", ctypes.c_int64), ("graphs_renumbered", ctypes.c_int64),
+                ("vertex_labels", ctypes.c_int32), ("edge_labels", ctypes.c_int32)]
 
 
 class TuneReport(ctypes.Structure):
@@ -197,6 +202,8 @@ def lib():
     L.gs_server_destroy.restype = None
     L.gs_autotune.argtypes = [ctypes.POINTER(vp), i32, pi32, ctypes.POINTER(MineOpts), ctypes.POINTER(TuneReport)]
     L.gs_autotune.restype = i32
+    L.gs_db_convert.argtypes = [ctypes.c_char_p, i32, ctypes.c_char_p, i32, ctypes.POINTER(ConvertInfo)]
+    L.gs_db_convert.restype = i32
     _lib = L
     return L
 
@@ -367,6 +374,16 @@ def _take_patterns(p, decode=True):
                 for i in range(P.count)]
     finally:
         lib().gs_patterns_free(p)
+
+
+def convert_database(in_path, in_type, out_path, out_type):
+    """The reference's convertdb (gs_db_convert): read, apply the fix_database
+    repairs, write.  Returns the counts of graphs written, repaired and
+    renumbered, and of labels."""
+    info = ConvertInfo()
+    _check(lib().gs_db_convert(os.fsencode(in_path), filetype(in_type), os.fsencode(out_path), filetype(out_type),
+                               ctypes.byref(info)))
+    return {f: getattr(info, f) for f, _ in info._fields_}
 
 
 def autotune(dbs, minsups, **kw):

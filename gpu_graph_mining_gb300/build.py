@@ -16,6 +16,7 @@ OUT = os.path.join(HERE, "_lib")
 OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libgspan_gb300.so")
 CLI = os.path.join(OUT, "gspan_gb300")
+CONVERT = os.path.join(OUT, "gspan_gb300_convertdb")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
@@ -66,10 +67,9 @@ def build(verbose=False, force=False):
     if force or jobs or not os.path.exists(LIB):
         _run([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs +
              ["-Xlinker", "--exclude-libs,ALL", "-lpthread"])
-    cli_src = os.path.join(CSRC, "gs_cli.cpp")
-    if force or not _newer(CLI, [cli_src, LIB]):
-        _run(["g++", "-O2", "-std=c++17", cli_src, "-o", CLI, "-L" + OUT, "-lgspan_gb300",
-              "-Wl,-rpath,$ORIGIN"])
+    for src, exe in ((os.path.join(CSRC, "gs_cli.cpp"), CLI), (os.path.join(CSRC, "gs_convertdb.cpp"), CONVERT)):
+        if force or not _newer(exe, [src, LIB]):
+            _run(["g++", "-O2", "-std=c++17", src, "-o", exe, "-L" + OUT, "-lgspan_gb300", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

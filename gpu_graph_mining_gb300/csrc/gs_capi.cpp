@@ -2,6 +2,7 @@
 #include "../../include/gspan_gb300.h"
 
 #include <cstring>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -187,6 +188,32 @@ gs_status gs_db_write(const gs_db *db, const char *path, int32_t filetype)
 }
 
 int32_t gs_db_size(const gs_db *db) { return db ? db->d.host.n_graphs : -1; }
+
+gs_status gs_db_convert(const char *in_path, int32_t in_type, const char *out_path, int32_t out_type,
+                        gs_convert_info *info)
+{
+  if(!in_path || !out_path) return set_err(GS_ERR_USAGE, "null path");
+  gsgb::HostDB db;
+  gsgb::LoadResult r = gsgb::load_database(in_path, in_type, db, false);
+  if(!r.error.empty()) return set_err(r.code ? r.code : GS_ERR_FORMAT, r.error);
+  int64_t fixed = 0, renumbered = 0;
+  r = gsgb::fix_database(db, &fixed, &renumbered);
+  if(!r.error.empty()) return set_err(r.code ? r.code : GS_ERR_FORMAT, r.error);
+  if(out_type == GS_BIN && db.n_graphs == 0)
+    return set_err(GS_ERR_FORMAT, "Cannot save empty database.");  // write_database_bin, dbio.cpp:211
+  r = gsgb::write_database(db, out_path, out_type);
+  if(!r.error.empty()) return set_err(r.code ? r.code : GS_ERR_IO, r.error);
+  if(info) {
+    std::set<int32_t> vl(db.vlabel.begin(), db.vlabel.end()), el(db.adj_el.begin(), db.adj_el.end());
+    info->graphs = db.n_graphs;
+    info->graphs_fixed = fixed;
+    info->graphs_renumbered = renumbered;
+    info->vertex_labels = (int32_t)vl.size();
+    info->edge_labels = (int32_t)el.size();
+  }
+  t_err.clear();
+  return GS_OK;
+}
 
 gs_status gs_db_get_info(const gs_db *db, gs_db_info *info)
 {

@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -371,7 +372,7 @@ LoadResult read_cudabin(const char *path, HostDB &db)
 
 }  // namespace
 
-LoadResult load_database(const char *path, int filetype, HostDB &db)
+LoadResult load_database(const char *path, int filetype, HostDB &db, bool validate)
 {
   db = HostDB();
   LoadResult r;
@@ -387,7 +388,78 @@ LoadResult load_database(const char *path, int filetype, HostDB &db)
   if(db.aoff.empty()) db.aoff.push_back(0);
   if(db.n_vertices() >= (int64_t)INT32_MAX || db.n_adj() >= (int64_t)INT32_MAX)
     return fail(ST_ERR_FORMAT, "database too large for 32-bit vertex/adjacency indices");
-  return validate_simple(db);
+  return validate ? validate_simple(db) : LoadResult();
+}
+
+LoadResult fix_database(HostDB &db, int64_t *fixed, int64_t *renumbered)
+{
+  int64_t nfix = 0, nren = 0;
+  HostDB out;
+  out.vbase.push_back(0);
+  out.aoff.push_back(0);
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> lists;
+  for(int32_t g = 0; g < db.n_graphs; g++) {
+    const int64_t base = db.vbase[g];
+    const int32_t nv = db.graph_nv(g);
+    lists.assign(nv, {});
+    // check_graph: a self loop, or a neighbour listed twice at one vertex
+    bool bad = false;
+    for(int32_t v = 0; v < nv && !bad; v++) {
+      std::set<int32_t> seen;
+      for(int64_t k = db.aoff[base + v]; k < db.aoff[base + v + 1]; k++) {
+        const int32_t t = (int32_t)(db.adj_to[k] - base);
+        if(t == v || !seen.insert(t).second) {
+          bad = true;
+          break;
+        }
+      }
+    }
+    for(int32_t v = 0; v < nv; v++) {
+      if(!bad) {
+        for(int64_t k = db.aoff[base + v]; k < db.aoff[base + v + 1]; k++)
+          lists[v].push_back({ (int32_t)(db.adj_to[k] - base), db.adj_el[k] });
+        continue;
+      }
+      // fix_graph: one edge per neighbour, neighbours ascending, no self loops
+      std::map<int32_t, int32_t> to_label;
+      for(int64_t k = db.aoff[base + v]; k < db.aoff[base + v + 1]; k++) {
+        const int32_t t = (int32_t)(db.adj_to[k] - base);
+        if(t == v) continue;
+        auto it = to_label.find(t);
+        if(it == to_label.end()) to_label.emplace(t, db.adj_el[k]);
+        else if(it->second != db.adj_el[k])
+          return fail(ST_ERR_FORMAT, "error: unable to fix graph, parallel edge has different label (graph " +
+                                         std::to_string(g) + ")");
+      }
+      for(const auto &e : to_label) lists[v].push_back(e);
+    }
+    if(bad) nfix++;
+    // vertex 0 goes when no other vertex has it as a neighbour
+    bool drop0 = nv > 0;
+    for(int32_t v = 1; v < nv && drop0; v++)
+      for(const auto &e : lists[v])
+        if(e.first == 0) {
+          drop0 = false;
+          break;
+        }
+    const int32_t first = drop0 ? 1 : 0;
+    if(drop0) nren++;
+    const int64_t obase = out.vbase.back();
+    for(int32_t v = first; v < nv; v++) {
+      out.vlabel.push_back(db.vlabel[base + v]);
+      for(const auto &e : lists[v]) {
+        out.adj_to.push_back((int32_t)(obase + e.first - first));
+        out.adj_el.push_back(e.second);
+      }
+      out.aoff.push_back((int64_t)out.adj_to.size());
+    }
+    out.vbase.push_back(obase + (nv - first));
+    out.n_graphs++;
+  }
+  db = std::move(out);
+  if(fixed) *fixed = nfix;
+  if(renumbered) *renumbered = nren;
+  return LoadResult();
 }
 
 LoadResult validate_simple(const HostDB &db)

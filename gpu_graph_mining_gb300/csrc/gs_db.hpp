@@ -50,7 +50,8 @@ struct LoadResult {
   int code = 0;  // gs_status value on failure
 };
 
-LoadResult load_database(const char *path, int filetype, HostDB &db);
+// validate = false keeps self loops and parallel edges (for fix_database).
+LoadResult load_database(const char *path, int filetype, HostDB &db, bool validate = true);
 LoadResult db_from_cudabin_arrays(int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
                                   const int32_t *edges, const int32_t *edges_labels,
                                   const int32_t *vertex_labels, const int32_t *vertex_offsets, HostDB &db);
@@ -60,6 +61,19 @@ LoadResult write_database(const HostDB &db, const char *path, int filetype);
 // graphs, as the reference's cudabin layout does: cuda_graph_types.cpp:65-127
 // sizes its edge arrays from distinct edge ids).
 LoadResult validate_simple(const HostDB &db);
+
+// The repairs of the reference's convertdb tool (fix_database,
+// src/globals/fix_database.cpp:10-85, with check_graph,
+// check_database.cpp:10-30), graph by graph:
+//  - a graph with a self loop or a repeated neighbour at some vertex is
+//    rebuilt: self loops dropped, each neighbour kept once (its first edge
+//    label; a differing label on a parallel edge is an error), every
+//    vertex's neighbours in ascending order;
+//  - a graph in which no vertex other than 0 has vertex 0 as a neighbour
+//    loses vertex 0 and its other vertices move down by one (inputs written
+//    with ids from 1).
+// Counts the graphs rebuilt and renumbered.
+LoadResult fix_database(HostDB &db, int64_t *fixed, int64_t *renumbered);
 
 // Builds the dense label arrays (vertex and edge) and the label maps.
 void compact_labels(const HostDB &db, std::vector<int32_t> &vl_dense, std::vector<int32_t> &el_dense, LabelMap &map);

@@ -104,6 +104,29 @@ GS_API gs_db *gs_db_generate(int32_t config, uint64_t seed, double scale, gs_sta
  * write_database_cudabin, src/globals/dbio.cpp:209-260, 354-370). */
 GS_API gs_status gs_db_write(const gs_db *db, const char *path, int32_t filetype);
 
+/* The reference's convertdb tool (src/globals/convertdb.cpp:28-66): reads a
+ * database (self loops and parallel edges allowed), applies its
+ * fix_database repairs (src/globals/fix_database.cpp:10-85) graph by graph,
+ * and writes it out:
+ *  - a graph with a self loop or a neighbour listed twice at a vertex is
+ *    rebuilt with self loops dropped, each neighbour once (a parallel edge
+ *    with a different label is an error, GS_ERR_FORMAT) and every vertex's
+ *    neighbours in ascending order;
+ *  - a graph in which no vertex but 0 has vertex 0 as a neighbour loses
+ *    vertex 0 and its other vertices move down by one (files numbered from 1).
+ * bin and cudabin output are byte-identical to the reference tool's; txt
+ * output (which the reference's writer refuses) is also accepted.  info may
+ * be NULL. */
+typedef struct gs_convert_info {
+  int64_t graphs;
+  int64_t graphs_fixed;       /* rebuilt: self loops dropped, parallel edges merged */
+  int64_t graphs_renumbered;  /* vertex 0 dropped */
+  int32_t vertex_labels;      /* distinct labels written */
+  int32_t edge_labels;
+} gs_convert_info;
+GS_API gs_status gs_db_convert(const char *in_path, int32_t in_type, const char *out_path, int32_t out_type,
+                               gs_convert_info *info);
+
 /* Number of graphs (graph_database_cuda::size, cuda_graph_types.hpp:67). */
 GS_API int32_t gs_db_size(const gs_db *db);
 

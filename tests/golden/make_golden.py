@@ -14,7 +14,10 @@ or REF=...).  It
   * writes the synthetic configuration-1 database (seed 1) with this
     package's generator, and
   * runs the reference miner on every fixture database at several supports,
-    writing "<code>\\t<support>" lines in the reference's traversal order.
+    writing "<code>\\t<support>" lines in the reference's traversal order,
+  * builds the reference's convertdb tool (src/globals/convertdb.cpp with its
+    fix_database repairs) the same way and runs it on the inputs under
+    convert/, keeping its bin and cudabin outputs.
 
 Nothing at test time reads the reference; the tests use only these files.
 """
@@ -28,6 +31,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
 REF = os.environ.get("REF", "/root/reference")
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "gspan_ref")
+REF_CONVERT = os.path.join(REPO, "oracle", "_ref", "convertdb_ref")
 
 
 def build_ref():
@@ -105,6 +109,64 @@ def run_ref(ftype, db, minsup, out):
     return r.stderr.strip()
 
 
+def convert_inputs():
+    """Inputs for the convertdb runs: graphs needing the fix_database repairs
+    (parallel edges, self loops, files numbered from 1), one it cannot repair
+    (a parallel edge with another label), and the same repairs in fsg form."""
+    d = {}
+    d["in_repair.txt"] = ("t # 0\nv 0 1\nv 1 2\nv 2 3\ne 0 1 5\ne 1 0 5\ne 1 2 6\ne 2 2 7\n"
+                          "t # 1\nv 0 9\nv 1 1\nv 2 2\ne 1 2 3\n"
+                          "t # 2\nv 0 4\nv 1 4\ne 0 1 1\n"
+                          "t # 3\nv 0 0\nv 1 5\nv 2 6\nv 3 5\ne 1 2 1\ne 2 3 1\ne 3 1 2\ne 3 2 1\n")
+    d["in_conflict.txt"] = "t # 0\nv 0 1\nv 1 2\ne 0 1 5\ne 0 1 6\n"
+    d["in_repair.fsg"] = ("t # 0\nv 0 C\nv 1 O\nv 2 N\nu 0 1 s\nu 1 0 s\nu 1 2 d\nu 2 2 s\n"
+                          "t # 1\nv 0 H\nv 1 C\nv 2 C\nu 1 2 s\n")
+    # the first 40 graphs of the configuration-1 database, made dirty: every
+    # 7th graph repeats its first edge and gets a self loop on vertex 1
+    lines, g, first = [], -1, None
+    with open(os.path.join(HERE, "cfg1_seed1.txt")) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            if line.startswith("t"):
+                if g >= 0 and g % 7 == 0 and first:
+                    lines += [first, "e 1 1 0"]
+                g += 1
+                if g == 40:
+                    break
+                first = None
+            elif line.startswith("e") and first is None:
+                first = line
+            lines.append(line)
+    d["in_cfg1_dirty.txt"] = "\n".join(lines) + "\n"
+    return d
+
+
+def convert_runs():
+    os.makedirs(os.path.join(HERE, "convert"), exist_ok=True)
+    runs = []
+    for name, text in convert_inputs().items():
+        with open(os.path.join(HERE, "convert", name), "w") as f:
+            f.write(text)
+        ft = "fsg" if name.endswith(".fsg") else "txt"
+        for out_ft in ("bin", "cudabin"):
+            out = "out_%s.%s" % (os.path.splitext(name)[0] + ("_fsg" if ft == "fsg" else ""), out_ft)
+            path = os.path.join(HERE, "convert", out)
+            if os.path.exists(path):
+                os.remove(path)
+            r = subprocess.run([REF_CONVERT, ft, os.path.join(HERE, "convert", name), out_ft, path],
+                               stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+            if r.returncode != 0:
+                if os.path.exists(path):
+                    os.remove(path)
+                out = "error"
+            runs.append((ft, name, out_ft, out))
+    with open(os.path.join(HERE, "convert", "convert_runs.tsv"), "w") as idx:
+        idx.write("# input filetype\tinput\toutput filetype\treference convertdb output ('error': it aborted)\n")
+        for r in runs:
+            idx.write("\t".join(r) + "\n")
+            print("convert", *r)
+
+
 def main():
     build_ref()
     with open(os.path.join(HERE, "ismin_kats.tsv"), "w") as f:
@@ -160,6 +222,7 @@ def main():
             log = run_ref(ft, os.path.join(HERE, db), s, os.path.join(HERE, out))
             idx.write("%s\t%s\t%d\t%s\t%s\n" % (ft, db, s, out, log))
             print(ft, db, s, log)
+    convert_runs()
 
 
 if __name__ == "__main__":

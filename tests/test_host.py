@@ -208,3 +208,85 @@ def test_server_validates_requests_on_the_host(gs):
         assert e.value.status == 1
         s = srv.stats()
         assert s["submitted"] == 0 and s["running"] == 0
+
+
+def _convert_runs():
+    rows = []
+    for line in read_lines(os.path.join(GOLDEN, "convert", "convert_runs.tsv")):
+        if not line.startswith("#"):
+            rows.append(tuple(line.split("\t")))
+    return rows
+
+
+@pytest.mark.parametrize("run", _convert_runs(), ids=lambda r: "%s-%s" % (r[1], r[2]))
+def test_convert_matches_reference_tool(gs, tmp_path, run):
+    # outputs of the reference's convertdb (with fix_database), byte for byte
+    ft, name, out_ft, out = run
+    dst = str(tmp_path / ("x." + out_ft))
+    src = os.path.join(GOLDEN, "convert", name)
+    if out == "error":
+        with pytest.raises(gs.GSpanError) as e:
+            gs.convert_database(src, ft, dst, out_ft)
+        assert e.value.status == 3 and "different label" in str(e.value)
+        return
+    info = gs.convert_database(src, ft, dst, out_ft)
+    with open(dst, "rb") as a, open(os.path.join(GOLDEN, "convert", out), "rb") as b:
+        assert a.read() == b.read()
+    assert info["graphs"] >= 1
+    # the repaired database is simple: it loads and mines
+    d = gs.Database.load(dst, out_ft)
+    assert len(d) == info["graphs"]
+
+
+def test_convertdb_cli(gs, tmp_path):
+    exe = os.path.join(os.path.dirname(gs.LIB_PATH), "gspan_gb300_convertdb")
+    r = subprocess.run([exe, "txt"], stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    assert r.returncode == 1
+    dst = str(tmp_path / "o.cudabin")
+    src = os.path.join(GOLDEN, "convert", "in_repair.txt")
+    r = subprocess.run([exe, "txt", src, "cudabin", dst], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 0 and "repaired 2" in r.stdout
+    with open(dst, "rb") as a, open(os.path.join(GOLDEN, "convert", "out_in_repair.cudabin"), "rb") as b:
+        assert a.read() == b.read()
+    r = subprocess.run([exe, "txt", os.path.join(GOLDEN, "convert", "in_conflict.txt"), "bin", dst],
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 2
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REPO, "oracle", "_ref", "convertdb_ref")),
+                    reason="the reference's convertdb is built only where the reference tree is")
+def test_convert_live_against_reference_tool(gs, tmp_path):
+    # a larger dirty database: every 3rd graph of configuration 1 gets a repeated
+    # edge, every 5th a self loop, and every 4th is shifted to ids from 1
+    import random
+    rnd = random.Random(5)
+    src = gs.Database.generate(1, seed=9, scale=0.5)
+    p = str(tmp_path / "clean.txt")
+    src.write(p, "txt")
+    out, g, edges = [], -1, []
+    for line in read_lines(p):
+        if line.startswith("t"):
+            g += 1
+            out.append(line)
+            continue
+        parts = line.split()
+        if g % 4 == 0:
+            parts[1] = str(int(parts[1]) + 1)
+            if parts[0] == "e":
+                parts[2] = str(int(parts[2]) + 1)
+            if parts[0] == "v" and parts[1] == "1":
+                out.append("v 0 %d" % rnd.randint(0, 3))
+        out.append(" ".join(parts))
+        if parts[0] == "e" and g % 3 == 0 and rnd.random() < 0.3:
+            out.append("e %s %s %s" % (parts[2], parts[1], parts[3]))
+        if parts[0] == "e" and g % 5 == 0 and rnd.random() < 0.1:
+            out.append("e %s %s 1" % (parts[1], parts[1]))
+    dirty = str(tmp_path / "dirty.txt")
+    with open(dirty, "w") as f:
+        f.write("\n".join(out) + "\n")
+    ref = os.path.join(REPO, "oracle", "_ref", "convertdb_ref")
+    for ft in ("bin", "cudabin"):
+        a, b = str(tmp_path / ("a." + ft)), str(tmp_path / ("b." + ft))
+        subprocess.run([ref, "txt", dirty, ft, a], check=True, stdout=subprocess.DEVNULL)
+        gs.convert_database(dirty, "txt", b, ft)
+        assert open(a, "rb").read() == open(b, "rb").read(), ft
