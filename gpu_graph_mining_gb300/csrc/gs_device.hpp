@@ -28,6 +28,7 @@ struct DevDB {
   const int32_t *adj_off;
   const int32_t *vlabel;
   const int32_t *vgraph;
+  const int32_t *vgbase;    // [V] first global vertex of each vertex's graph
   const int32_t *vbase;     // [G+1] first global vertex of each graph
   const int32_t *adj_pair;  // [E2] pair index of each directed entry: pair_idx(label(source), el, label(nbr))
   const int32_t *pair_idx;

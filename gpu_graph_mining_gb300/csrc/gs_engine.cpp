@@ -92,7 +92,8 @@ void Database::upload()
   size_t o_off = o_adj + al(sizeof(unsigned long long) * (E2 + 1));
   size_t o_vl = o_off + al(sizeof(int32_t) * (V + 1));
   size_t o_vg = o_vl + al(sizeof(int32_t) * (V + 1));
-  size_t o_pi = o_vg + al(sizeof(int32_t) * (V + 1));
+  size_t o_gb = o_vg + al(sizeof(int32_t) * (V + 1));
+  size_t o_pi = o_gb + al(sizeof(int32_t) * (V + 1));
   size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
   size_t o_vb = o_ro + al(sizeof(int32_t) * (VL + 1));
   size_t o_ap = o_vb + al(sizeof(int32_t) * (host.n_graphs + 1));
@@ -106,13 +107,16 @@ void Database::upload()
       adj[k] = ((unsigned long long)hi << 32) | w;
     }
   }, 1 << 16);
-  std::vector<int32_t> off(V + 1), vg(V + 1, 0), pidx(tab, -1);
+  std::vector<int32_t> off(V + 1), vg(V + 1, 0), vgb(V + 1, 0), pidx(tab, -1);
   parallel_ranges(V + 1, [&](int64_t b, int64_t e, int) {
     for(int64_t v = b; v < e; v++) off[v] = (int32_t)host.aoff[v];
   }, 1 << 16);
   parallel_ranges(host.n_graphs, [&](int64_t g0, int64_t g1, int) {
     for(int64_t g = g0; g < g1; g++)
-      for(int64_t v = host.vbase[g]; v < host.vbase[g + 1]; v++) vg[v] = (int32_t)g;
+      for(int64_t v = host.vbase[g]; v < host.vbase[g + 1]; v++) {
+        vg[v] = (int32_t)g;
+        vgb[v] = (int32_t)host.vbase[g];
+      }
   });
   for(int32_t a = 0; a < VL; a++)
     for(size_t i = 0; i < pairs[a].size(); i++)
@@ -139,6 +143,7 @@ void Database::upload()
   CK(cudaMemcpy(b + o_off, off.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
   if(V) CK(cudaMemcpy(b + o_vl, vl_dense.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_vg, vg.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b + o_gb, vgb.data(), sizeof(int32_t) * (V + 1), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(b + o_pi, pidx.data(), sizeof(int32_t) * tab, cudaMemcpyHostToDevice));
   std::vector<int32_t> ro(root_off);
   ro.push_back(root_keys);
@@ -154,6 +159,7 @@ void Database::upload()
   dev.adj_off = (const int32_t *)(b + o_off);
   dev.vlabel = (const int32_t *)(b + o_vl);
   dev.vgraph = (const int32_t *)(b + o_vg);
+  dev.vgbase = (const int32_t *)(b + o_gb);
   dev.pair_idx = (const int32_t *)(b + o_pi);
   dev.vbase = (const int32_t *)(b + o_vb);
   dev.adj_pair = (const int32_t *)(b + o_ap);

@@ -126,7 +126,7 @@ __global__ void k_graphs(int G, int maxv, long long slots, long long esz, const 
 __global__ void k_vertices(int G, int maxv, long long slots, long long esz, const int32_t *voff,
                            const int32_t *vlab, const int32_t *edges, const int32_t *elab, const long long *gnv,
                            const long long *vbase, const long long *gpos, int32_t *off, int32_t *vgraph,
-                           int32_t *vl_raw, int32_t *adj_to, int32_t *el_raw, unsigned *flags)
+                           int32_t *vgbase, int32_t *vl_raw, int32_t *adj_to, int32_t *el_raw, unsigned *flags)
 {
   for(long long slot = (long long)blockIdx.x * blockDim.x + threadIdx.x; slot < slots;
       slot += (long long)gridDim.x * blockDim.x) {
@@ -144,6 +144,7 @@ __global__ void k_vertices(int G, int maxv, long long slots, long long esz, cons
     }
     off[gv] = (int32_t)pos;
     vgraph[gv] = (int32_t)g;
+    vgbase[gv] = (int32_t)vbase[g];
     vl_raw[gv] = vlab[slot];
     const bool small = nv <= 64;
     unsigned long long seen = 0;
@@ -364,13 +365,14 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
 
   // 2. vertices and adjacency, raw labels, checks
   int32_t *off = fr.add(dalloc<int32_t>(V + 1)), *vgraph = fr.add(dalloc<int32_t>(V + 1));
+  int32_t *vgbase = fr.add(dalloc<int32_t>(V + 1));
   int32_t *vl = fr.add(dalloc<int32_t>(V)), *adj_to = fr.add(dalloc<int32_t>(E2)), *el = fr.add(dalloc<int32_t>(E2));
   {
     const int32_t e2 = (int32_t)E2;
     CK(cudaMemcpyAsync(off + V, &e2, sizeof(int32_t), cudaMemcpyHostToDevice, s));
   }
   k_vertices<<<blocks_for(slots), kThreads, 0, s>>>(G, maxv, slots, esz, d_voff, d_vlab, d_edges, d_elab, gnv,
-                                                      vbase, gpos, off, vgraph, vl, adj_to, el, flags);
+                                                      vbase, gpos, off, vgraph, vgbase, vl, adj_to, el, flags);
   CK(cudaMemcpyAsync(&hflags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if(hflags & kBadLeave) throw Error(ST_ERR_FORMAT, "cudabin: edge leaves its graph");
@@ -409,7 +411,8 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   const size_t o_off = o_adj + al(sizeof(unsigned long long) * (E2 + 1));
   const size_t o_vl = o_off + al(sizeof(int32_t) * (V + 1));
   const size_t o_vg = o_vl + al(sizeof(int32_t) * (V + 1));
-  const size_t o_pi = o_vg + al(sizeof(int32_t) * (V + 1));
+  const size_t o_gb = o_vg + al(sizeof(int32_t) * (V + 1));
+  const size_t o_pi = o_gb + al(sizeof(int32_t) * (V + 1));
   const size_t o_ro = o_pi + al(sizeof(int32_t) * tab);
   const size_t o_vb = o_ro + al(sizeof(int32_t) * (VL + 1));
   const size_t o_ap = o_vb + al(sizeof(int32_t) * (G + 1));
@@ -433,6 +436,7 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     CK(cudaMemcpyAsync(b + o_off, off, sizeof(int32_t) * (V + 1), cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(b + o_vl, vl, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(b + o_vg, vgraph, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(b + o_gb, vgbase, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
     {
       // vertex bases as int32
       std::vector<long long> hv(G + 1);
@@ -470,6 +474,7 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     db.dev.adj_off = (const int32_t *)(b + o_off);
     db.dev.vlabel = (const int32_t *)(b + o_vl);
     db.dev.vgraph = (const int32_t *)(b + o_vg);
+    db.dev.vgbase = (const int32_t *)(b + o_gb);
     db.dev.pair_idx = pidx;
     db.dev.vbase = (const int32_t *)(b + o_vb);
     db.dev.adj_pair = (const int32_t *)(b + o_ap);

@@ -89,6 +89,8 @@ template <int KMAX> struct Smem {
   int pre[KMAX + 1][32];    // degree prefix over slots
   SlotDesc slot[KMAX];      // the tile's node: right-most-path slots
   int vtab[KMAX];           // the tile's node: pattern vertex -> backward slot
+  const int2 *col[KMAX];    // the tile's node: its columns and their lengths,
+  int clen[KMAX];           // loaded once so the walk's chain is one load per column
 };
 
 __device__ __forceinline__ unsigned lanemask_lt()
@@ -128,17 +130,17 @@ k_wave(const WaveArgs a)
   const int rec_tag = copy << kRecCopyShift;
 
   for(long long tile = gwarp; tile < a.total_tiles; tile += nwarps) {
-    // ---- the tile's node (warp-uniform: tiles never span nodes)
-    int n = 0;
-    if(lane == 0) {
-      int lo = 0, hi = a.nnodes - 1;
-      while(lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if(a.nodes[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
-      }
-      n = lo;
+    // ---- the tile's node (warp-uniform: tiles never span nodes): a 32-way
+    // search, the lanes probing 32 nodes per round (3 rounds for 4096 nodes)
+    int lo = 0, hi = a.nnodes;  // the node is the last in [lo, hi) with tile_begin <= tile
+    while(hi - lo > 1) {
+      const int step = (hi - lo + 31) >> 5;
+      const int probe = lo + lane * step;
+      const unsigned ok = __ballot_sync(kFull, probe < hi && a.nodes[probe].tile_begin <= tile);
+      lo += (31 - __clz(ok | 1u)) * step;
+      hi = min(hi, lo + step);
     }
-    n = __shfl_sync(kFull, n, 0);
+    const int n = lo;
     const NodeDesc &nd = a.nodes[n];
     const int k = nd.k, nslot = nd.nslot, minlabel = nd.minlabel, words = nd.words, key_base = nd.key_base;
     const long long bm_base = nd.bm_base;
@@ -147,33 +149,29 @@ k_wave(const WaveArgs a)
     const int32_t *__restrict__ adj_off = dbr.adj_off;
     const int32_t *__restrict__ adj_pair = dbr.adj_pair;
     const int nv = dbr.n_vertices;
-    const int32_t *__restrict__ vbase = dbr.vbase;
-    const int32_t *__restrict__ vgraph = dbr.vgraph;
     if(k > KMAX || nslot > KMAX || k < 1 || nslot < 1) {
       if(lane == 0) atomicOr(a.err, 2u);
       continue;
     }
     if(lane < nslot) S.slot[lane] = a.slots[nd.slot_off + lane];
-    if(lane < k) S.vtab[lane] = a.vtab[nd.vtab_off + lane];
+    if(lane < k) {
+      S.vtab[lane] = a.vtab[nd.vtab_off + lane];
+      S.col[lane] = a.coltab[nd.col_off + lane];
+      S.clen[lane] = a.collen[nd.col_off + lane];
+    }
     // ---- phase 1: this lane's row
     const int i = (int)((tile - nd.tile_begin) * 32) + lane;
     bool valid = i < nd.nrows;
     int W = 0, g = 0, last_prev = 0;
+    // the graph rank is loaded now and checked after the walk, so that the
+    // walk's loads do not wait for it
+    if(valid) g = __ldg(&nd.gord[i]);
     __syncwarp();
     if(valid) {
-      g = nd.gord[i];
-      if((unsigned)g >= (unsigned)words * 32u) {
-        atomicOr(a.err, 1u);
-        valid = false;
-      }
-    }
-    if(valid) {
-      const int2 *const *cols = a.coltab + nd.col_off;
-      const int32_t *clen = a.collen + nd.col_off;
       int idx = i;
       for(int c = k - 1; c >= 0; --c) {
-        if((unsigned)idx >= (unsigned)clen[c]) { valid = false; break; }
-        const int2 e = __ldg(&cols[c][idx]);
+        if((unsigned)idx >= (unsigned)S.clen[c]) { valid = false; break; }
+        const int2 e = __ldg(&S.col[c][idx]);
         if((unsigned)e.x >= (unsigned)nv) { valid = false; break; }
         S.phi[c][lane] = e.x;
         if(c == k - 1) last_prev = e.y;
@@ -181,8 +179,12 @@ k_wave(const WaveArgs a)
       }
       if(!valid) atomicOr(a.err, 2u);
     }
+    if(valid && (unsigned)g >= (unsigned)words * 32u) {
+      atomicOr(a.err, 1u);
+      valid = false;
+    }
     if(MASK && valid) {
-      const int gb = __ldg(&vbase[__ldg(&vgraph[S.phi[0][lane]])]);
+      const int gb = __ldg(&dbr.vgbase[S.phi[0][lane]]);
       unsigned long long m = 0;
       for(int c = 0; c < k; ++c) {
         const unsigned lv = (unsigned)(S.phi[c][lane] - gb);
