@@ -39,7 +39,7 @@ namespace {
 #define GS_WAVE_WARPS 4
 #endif
 #ifndef GS_WAVE_MINB
-#define GS_WAVE_MINB 0
+#define GS_WAVE_MINB 9
 #endif
 #ifndef GS_WAVE_GRID
 #define GS_WAVE_GRID 64
