@@ -199,8 +199,12 @@ void Database::ensure_host()
 
 void Database::release()
 {
-  if(d_block) cudaFree(d_block);
+  if(d_block) {
+    if(pooled) ingest_free_block(d_block);
+    else cudaFree(d_block);
+  }
   d_block = nullptr;
+  pooled = false;
   resident = false;
 }
 
@@ -2040,8 +2044,11 @@ int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int3
 
 void engine_reset()
 {
-  std::lock_guard<std::mutex> g(g_mu);
-  g_engine.destroy();
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    g_engine.destroy();
+  }
+  ingest_release();
 }
 
 void engine_set_pool_bytes(int64_t bytes)

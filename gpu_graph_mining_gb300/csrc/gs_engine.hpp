@@ -59,6 +59,7 @@ struct Database {
   // built on the device from cudabin arrays (ingest_cudabin_device): the host
   // arrays stay empty until ensure_host() downloads them
   bool device_only = false;
+  bool pooled = false;   // d_block is from the ingest's pool (ingest_free_block)
   int64_t dev_vertices = 0, dev_adj = 0;
 
   void prepare();   // label compaction and pair tables (host only)
@@ -77,6 +78,13 @@ struct Database {
 void ingest_cudabin_device(Database &db, int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
                            const int32_t *edges, const int32_t *edges_labels, const int32_t *vertex_labels,
                            const int32_t *vertex_offsets);
+
+// Returns the device ingest's pooled scratch to the driver.
+void ingest_release();
+
+// Frees a database block taken from the ingest's pool (after the device is idle,
+// as cudaFree would be).
+void ingest_free_block(void *block);
 
 using EmitFn = void (*)(const int32_t *dfs5xN, int32_t n_edges, int64_t support, void *user);
 

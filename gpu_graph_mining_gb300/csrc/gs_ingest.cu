@@ -19,6 +19,7 @@
 // Accepts exactly what gs_db_from_arrays accepts (same checks), and the
 // device database is identical to the one the host path uploads.
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -77,30 +78,53 @@ __global__ void k_scan_add(long long *out, long long n, const long long *block_o
   if(i < n) out[i] += block_off[blockIdx.x];
 }
 
+// Scratch of one ingest: stream-ordered allocations from a pool that keeps
+// its memory between ingests (up to kKeepBytes), so that repeated ingests of
+// similar databases allocate and free without driver calls.  Freed in stream
+// order when the ingest returns.
+struct Scratch {
+  cudaStream_t s;
+  cudaMemPool_t pool;
+  std::vector<void *> ptrs;
+  cudaEvent_t after = nullptr;  // work of another stream on the scratch, ordered before the frees
+  ~Scratch()
+  {
+    if(after) cudaStreamWaitEvent(s, after, 0);
+    for(void *p : ptrs) cudaFreeAsync(p, s);
+  }
+  template <class T> T *get(size_t n)
+  {
+    void *p = nullptr;
+    if(cudaMallocFromPoolAsync(&p, sizeof(T) * std::max<size_t>(n, 1), pool, s) != cudaSuccess) {
+      cudaGetLastError();
+      throw Error(ST_ERR_NOMEM, "device ingest: out of device memory");
+    }
+    ptrs.push_back(p);
+    return (T *)p;
+  }
+};
+
 // out[i] = sum of in[0..i) for i in [0, n]; out must hold n + 1 values
-void scan_exclusive(const long long *in, long long *out, long long n, cudaStream_t s)
+void scan_exclusive(const long long *in, long long *out, long long n, Scratch &sc)
 {
+  cudaStream_t s = sc.s;
   const long long nb = (n + kThreads - 1) / kThreads;
   if(nb <= 0) {
     CK(cudaMemsetAsync(out, 0, sizeof(long long), s));
     return;
   }
-  long long *sums = nullptr;
-  CK(cudaMallocAsync(&sums, sizeof(long long) * (nb + 1), s));
+  long long *sums = sc.get<long long>(nb + 1);
   k_scan_blocks<<<(unsigned)nb, kThreads, 0, s>>>(in, out, n, sums);
   if(nb == 1) {
     // one block: its sum is the total
     CK(cudaMemcpyAsync(out + n, sums, sizeof(long long), cudaMemcpyDeviceToDevice, s));
   } else {
-    long long *offs = nullptr;
-    CK(cudaMallocAsync(&offs, sizeof(long long) * (nb + 1), s));
-    scan_exclusive(sums, offs, nb, s);
+    long long *offs = sc.get<long long>(nb + 1);
+    scan_exclusive(sums, offs, nb, sc);
     k_scan_add<<<(unsigned)nb, kThreads, 0, s>>>(out, n, offs);
     // the total, after the last element
     CK(cudaMemcpyAsync(out + n, offs + nb, sizeof(long long), cudaMemcpyDeviceToDevice, s));
-    CK(cudaFreeAsync(offs, s));
   }
-  CK(cudaFreeAsync(sums, s));
 }
 
 // ---- 1. per graph: valid slots and adjacency entries
@@ -172,8 +196,10 @@ __global__ void k_vertices(int G, int maxv, long long slots, long long esz, cons
 }
 
 // ---- 3. labels
+// block-reduced: one pair of atomics per block (the range is one address)
 __global__ void k_minmax(const int32_t *x, long long n, int *mn, int *mx)
 {
+  __shared__ int slo[kThreads / 32], shi[kThreads / 32];
   int lo = INT32_MAX, hi = INT32_MIN;
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     lo = min(lo, x[i]);
@@ -183,7 +209,17 @@ __global__ void k_minmax(const int32_t *x, long long n, int *mn, int *mx)
     lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
     hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
   }
-  if((threadIdx.x & 31) == 0) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if(lane == 0) {
+    slo[w] = lo;
+    shi[w] = hi;
+  }
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    for(int k = 1; k < kThreads / 32; k++) {
+      lo = min(lo, slo[k]);
+      hi = max(hi, shi[k]);
+    }
     atomicMin(mn, lo);
     atomicMax(mx, hi);
   }
@@ -192,7 +228,11 @@ __global__ void k_minmax(const int32_t *x, long long n, int *mn, int *mx)
 __global__ void k_mark(const int32_t *x, long long n, int lo, long long *present)
 {
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    present[(long long)x[i] - lo] = 1;
+  {
+    // a label alphabet is small: most elements find their flag already set
+    long long *f = present + ((long long)x[i] - lo);
+    if(!*f) *f = 1;
+  }
 }
 
 // dense[i] = rank of x[i] among the distinct values; of[rank] = value
@@ -214,7 +254,10 @@ __global__ void k_pairs_seen(const int32_t *off, long long V, const int32_t *vl,
 {
   for(long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
     const long long a = vl[v];
-    for(long long k = off[v]; k < off[v + 1]; k++) seen[(a * EL + el[k]) * VL + vl[adj_to[k]]] = 1;
+    for(long long k = off[v]; k < off[v + 1]; k++) {
+      long long *f = seen + (a * EL + el[k]) * VL + vl[adj_to[k]];
+      if(!*f) *f = 1;
+    }
   }
 }
 
@@ -253,157 +296,234 @@ __global__ void k_pack(const int32_t *off, long long V, const int32_t *vl, const
 
 __global__ void k_max_ll(const long long *x, long long n, int *mx)
 {
+  __shared__ int shi[kThreads / 32];
   int hi = 0;
   for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     hi = max(hi, (int)x[i]);
   for(int o = 16; o > 0; o >>= 1) hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  if((threadIdx.x & 31) == 0) atomicMax(mx, hi);
+  if((threadIdx.x & 31) == 0) shi[threadIdx.x >> 5] = hi;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    for(int k = 1; k < kThreads / 32; k++) hi = max(hi, shi[k]);
+    atomicMax(mx, hi);
+  }
 }
 
-template <class T> T *dalloc(size_t n)
+__global__ void k_narrow(const long long *x, long long n, int32_t *out)
 {
-  T *p = nullptr;
-  if(cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
-    cudaGetLastError();
-    throw Error(ST_ERR_NOMEM, "device ingest: out of device memory");
-  }
-  return p;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (int32_t)x[i];
 }
 
-struct Frees {
-  std::vector<void *> ptrs;
-  ~Frees()
+constexpr unsigned long long kKeepBytes = 4ull << 30;
+
+// Values read back to the host at the ingest's synchronisation points
+// (pinned, so the copies are asynchronous).
+struct ReadBack {
+  long long v_total, e_total;
+  unsigned flags, pad;
+  int minmax[4];        // vertex labels min, max; edge labels min, max
+  long long label_cnt[2];
+  long long nkeys;
+  int max_vertices, pad2;
+};
+
+// Process-wide ingest state: the ingest stream and a copy stream, the
+// scratch pool and the pinned read-back area.  Ingests are serialised by mu.
+struct IngestCtx {
+  std::mutex mu;
+  cudaStream_t s = nullptr, s_copy = nullptr;
+  cudaEvent_t ev_alloc = nullptr, ev_copied = nullptr;
+  cudaMemPool_t pool = nullptr;
+  ReadBack *rb = nullptr;
+  int32_t *meta = nullptr;   // pinned: label values, root offsets and pair codes read back
+  size_t meta_cap = 0;
+
+  void init()
   {
-    for(void *p : ptrs) cudaFree(p);
+    if(s) return;
+    CK(cudaSetDevice(0));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = 0;
+    CK(cudaMemPoolCreate(&pool, &props));
+    unsigned long long keep = kKeepBytes;
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    CK(cudaMallocHost(&rb, sizeof(ReadBack)));
+    CK(cudaEventCreateWithFlags(&ev_alloc, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_copied, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   }
-  template <class T> T *add(T *p)
+  int32_t *meta_buf(size_t n)
   {
-    ptrs.push_back(p);
-    return p;
+    if(n > meta_cap) {
+      if(meta) CK(cudaFreeHost(meta));
+      meta = nullptr;
+      meta_cap = 0;
+      CK(cudaMallocHost(&meta, sizeof(int32_t) * n));
+      meta_cap = n;
+    }
+    return meta;
   }
 };
 
-// dense labels of x[0..n) in place; returns the distinct values in order
-std::vector<int32_t> compact_device(int32_t *x, long long n, Frees &fr, cudaStream_t s)
+IngestCtx &ingest_ctx()
 {
-  std::vector<int32_t> of;
-  if(n == 0) return of;
-  int *mm = fr.add(dalloc<int>(2));
-  const int init[2] = { INT32_MAX, INT32_MIN };
-  CK(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, s));
-  k_minmax<<<blocks_for(n), kThreads, 0, s>>>(x, n, mm, mm + 1);
-  int h[2];
-  CK(cudaMemcpyAsync(h, mm, sizeof(h), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  const long long range = (long long)h[1] - (long long)h[0] + 1;
+  static IngestCtx c;
+  return c;
+}
+
+// Dense ids for the labels x[0..n) in place, order-preserving, given the
+// value range [lo, hi]; *cnt receives the number of distinct values (read
+// back later) and the returned device array of.  of[rank] = value.
+int32_t *compact_labels(int32_t *x, long long n, int lo, int hi, long long *cnt, Scratch &sc)
+{
+  cudaStream_t s = sc.s;
+  const long long range = (long long)hi - (long long)lo + 1;
   if(range > (1ll << 22))
     throw Error(ST_ERR_LIMIT, "device ingest: label values span more than 2^22; use gs_db_from_arrays");
-  long long *present = fr.add(dalloc<long long>(range));
-  long long *rank = fr.add(dalloc<long long>(range + 1));
+  long long *present = sc.get<long long>(range);
+  long long *rank = sc.get<long long>(range + 1);
+  int32_t *of = sc.get<int32_t>(range);
   CK(cudaMemsetAsync(present, 0, sizeof(long long) * range, s));
-  k_mark<<<blocks_for(n), kThreads, 0, s>>>(x, n, h[0], present);
-  scan_exclusive(present, rank, range, s);
-  long long cnt = 0;
-  CK(cudaMemcpyAsync(&cnt, rank + range, sizeof(cnt), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  int32_t *ofd = fr.add(dalloc<int32_t>(cnt));
-  k_label_values<<<blocks_for(range), kThreads, 0, s>>>(present, rank, range, h[0], ofd);
-  k_relabel<<<blocks_for(n), kThreads, 0, s>>>(x, n, h[0], rank);
-  of.resize(cnt);
-  CK(cudaMemcpyAsync(of.data(), ofd, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  k_mark<<<blocks_for(n), kThreads, 0, s>>>(x, n, lo, present);
+  scan_exclusive(present, rank, range, sc);
+  k_label_values<<<blocks_for(range), kThreads, 0, s>>>(present, rank, range, lo, of);
+  k_relabel<<<blocks_for(n), kThreads, 0, s>>>(x, n, lo, rank);
+  CK(cudaMemcpyAsync(cnt, rank + range, sizeof(long long), cudaMemcpyDeviceToHost, s));
   return of;
 }
 
 }  // namespace
 
+void ingest_release()
+{
+  IngestCtx &cx = ingest_ctx();
+  std::lock_guard<std::mutex> lk(cx.mu);
+  if(cx.pool) cudaMemPoolTrimTo(cx.pool, 0);
+}
+
+void ingest_free_block(void *block)
+{
+  IngestCtx &cx = ingest_ctx();
+  std::lock_guard<std::mutex> lk(cx.mu);
+  // every kernel that may still read the block has finished
+  cudaDeviceSynchronize();
+  cudaFreeAsync(block, cx.s);
+  cudaStreamSynchronize(cx.s);
+}
+
 void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, const int32_t *edges,
                            const int32_t *elab, const int32_t *vlab, const int32_t *voff)
 {
   if(G < 0 || esz < 0 || maxv < 0) throw Error(ST_ERR_FORMAT, "cudabin: negative sizes");
+  IngestCtx &cx = ingest_ctx();
+  std::lock_guard<std::mutex> lk(cx.mu);
+  cx.init();
   CK(cudaSetDevice(0));
-  cudaStream_t s;
-  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct StreamGuard {
-    cudaStream_t s;
-    ~StreamGuard()
+  cudaStream_t s = cx.s;
+  ReadBack &rb = *cx.rb;
+  // drains the streams when the ingest returns or throws (after the
+  // scratch's frees are queued), so that nothing of this ingest is in flight
+  // afterwards
+  struct Drain {
+    cudaStream_t s, s_copy;
+    ~Drain()
     {
+      cudaStreamSynchronize(s_copy);
       cudaStreamSynchronize(s);
-      cudaStreamDestroy(s);
     }
-  } sg{ s };
-  Frees fr;
+  } drain{ s, cx.s_copy };
+  Scratch sc{ s, cx.pool, {} };
   const long long slots = (long long)G * maxv;
-  // raw arrays up (the reference's copy_to_device)
-  int32_t *d_edges = fr.add(dalloc<int32_t>(esz)), *d_elab = fr.add(dalloc<int32_t>(esz));
-  int32_t *d_vlab = fr.add(dalloc<int32_t>(slots)), *d_voff = fr.add(dalloc<int32_t>(slots + 1));
-  if(esz) {
-    CK(cudaMemcpyAsync(d_edges, edges, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(d_elab, elab, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, s));
-  }
-  if(slots) CK(cudaMemcpyAsync(d_vlab, vlab, sizeof(int32_t) * slots, cudaMemcpyHostToDevice, s));
+  // raw arrays up (the reference's copy_to_device): the vertex offsets on the
+  // ingest stream, which needs them first; the rest on the copy stream,
+  // overlapping the per-graph pass
+  int32_t *d_edges = sc.get<int32_t>(esz), *d_elab = sc.get<int32_t>(esz);
+  int32_t *d_vlab = sc.get<int32_t>(slots), *d_voff = sc.get<int32_t>(slots + 1);
+  CK(cudaEventRecord(cx.ev_alloc, s));
   CK(cudaMemcpyAsync(d_voff, voff, sizeof(int32_t) * (slots + 1), cudaMemcpyHostToDevice, s));
-  unsigned *flags = fr.add(dalloc<unsigned>(1));
+  CK(cudaStreamWaitEvent(cx.s_copy, cx.ev_alloc, 0));
+  if(esz) {
+    CK(cudaMemcpyAsync(d_edges, edges, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
+    CK(cudaMemcpyAsync(d_elab, elab, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
+  }
+  if(slots) CK(cudaMemcpyAsync(d_vlab, vlab, sizeof(int32_t) * slots, cudaMemcpyHostToDevice, cx.s_copy));
+  CK(cudaEventRecord(cx.ev_copied, cx.s_copy));
+  sc.after = cx.ev_copied;
+  unsigned *flags = sc.get<unsigned>(1);
   CK(cudaMemsetAsync(flags, 0, sizeof(unsigned), s));
 
-  // 1. graphs
-  long long *gnv = fr.add(dalloc<long long>(G + 1)), *gadj = fr.add(dalloc<long long>(G + 1));
-  long long *vbase = fr.add(dalloc<long long>(G + 1)), *gpos = fr.add(dalloc<long long>(G + 1));
+  // 1. graphs (read back: vertex and entry totals, the tiling check)
+  long long *gnv = sc.get<long long>(G + 1), *gadj = sc.get<long long>(G + 1);
+  long long *vbase = sc.get<long long>(G + 1), *gpos = sc.get<long long>(G + 1);
   k_graphs<<<blocks_for(G), kThreads, 0, s>>>(G, maxv, slots, esz, d_voff, gnv, gadj, flags);
-  scan_exclusive(gnv, vbase, G, s);
-  scan_exclusive(gadj, gpos, G, s);
-  long long tot[2];
-  unsigned hflags = 0;
-  CK(cudaMemcpyAsync(&tot[0], vbase + G, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&tot[1], gpos + G, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&hflags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  scan_exclusive(gnv, vbase, G, sc);
+  scan_exclusive(gadj, gpos, G, sc);
+  CK(cudaMemcpyAsync(&rb.v_total, vbase + G, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rb.e_total, gpos + G, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rb.flags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  if(hflags & kBadTile) throw Error(ST_ERR_FORMAT, "cudabin: bad vertex offsets");
-  const long long V = tot[0], E2 = tot[1];
+  if(rb.flags & kBadTile) throw Error(ST_ERR_FORMAT, "cudabin: bad vertex offsets");
+  const long long V = rb.v_total, E2 = rb.e_total;
   if(V >= (long long)INT32_MAX || E2 >= (long long)INT32_MAX)
     throw Error(ST_ERR_FORMAT, "database too large for 32-bit vertex/adjacency indices");
 
-  // 2. vertices and adjacency, raw labels, checks
-  int32_t *off = fr.add(dalloc<int32_t>(V + 1)), *vgraph = fr.add(dalloc<int32_t>(V + 1));
-  int32_t *vgbase = fr.add(dalloc<int32_t>(V + 1));
-  int32_t *vl = fr.add(dalloc<int32_t>(V)), *adj_to = fr.add(dalloc<int32_t>(E2)), *el = fr.add(dalloc<int32_t>(E2));
+  // 2. vertices and adjacency, raw labels, checks (read back with the label ranges)
+  int32_t *off = sc.get<int32_t>(V + 1), *vgraph = sc.get<int32_t>(V + 1);
+  int32_t *vgbase = sc.get<int32_t>(V + 1);
+  int32_t *vl = sc.get<int32_t>(V), *adj_to = sc.get<int32_t>(E2), *el = sc.get<int32_t>(E2);
   {
     const int32_t e2 = (int32_t)E2;
     CK(cudaMemcpyAsync(off + V, &e2, sizeof(int32_t), cudaMemcpyHostToDevice, s));
   }
+  CK(cudaStreamWaitEvent(s, cx.ev_copied, 0));
   k_vertices<<<blocks_for(slots), kThreads, 0, s>>>(G, maxv, slots, esz, d_voff, d_vlab, d_edges, d_elab, gnv,
                                                       vbase, gpos, off, vgraph, vgbase, vl, adj_to, el, flags);
-  CK(cudaMemcpyAsync(&hflags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  int *mm = sc.get<int>(4);
+  {
+    static const int init[4] = { INT32_MAX, INT32_MIN, INT32_MAX, INT32_MIN };
+    CK(cudaMemcpyAsync(mm, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  }
+  if(V) k_minmax<<<blocks_for(V), kThreads, 0, s>>>(vl, V, mm, mm + 1);
+  if(E2) k_minmax<<<blocks_for(E2), kThreads, 0, s>>>(el, E2, mm + 2, mm + 3);
+  CK(cudaMemcpyAsync(&rb.flags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(rb.minmax, mm, sizeof(rb.minmax), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  if(hflags & kBadLeave) throw Error(ST_ERR_FORMAT, "cudabin: edge leaves its graph");
-  if(hflags & kBadTile) throw Error(ST_ERR_FORMAT, "cudabin: vertex offsets do not tile the edge array");
-  if(hflags & kSelfLoop) throw Error(ST_ERR_FORMAT, "self loop (only simple graphs are supported)");
-  if(hflags & kParallel) throw Error(ST_ERR_FORMAT, "parallel edges (only simple graphs are supported)");
+  if(rb.flags & kBadLeave) throw Error(ST_ERR_FORMAT, "cudabin: edge leaves its graph");
+  if(rb.flags & kBadTile) throw Error(ST_ERR_FORMAT, "cudabin: vertex offsets do not tile the edge array");
+  if(rb.flags & kSelfLoop) throw Error(ST_ERR_FORMAT, "self loop (only simple graphs are supported)");
+  if(rb.flags & kParallel) throw Error(ST_ERR_FORMAT, "parallel edges (only simple graphs are supported)");
 
-  // 3. labels
-  LabelMap labels;
-  labels.vlabel_of = compact_device(vl, V, fr, s);
-  labels.elabel_of = compact_device(el, E2, fr, s);
-  const int32_t VL = std::max<int32_t>(1, (int32_t)labels.vlabel_of.size());
-  const int32_t EL = std::max<int32_t>(1, (int32_t)labels.elabel_of.size());
+  // 3. labels, both alphabets compacted before one read-back of their sizes
+  const int vmin = rb.minmax[0], vmax = rb.minmax[1], emin = rb.minmax[2], emax = rb.minmax[3];
+  rb.label_cnt[0] = rb.label_cnt[1] = 0;
+  int32_t *vof = V ? compact_labels(vl, V, vmin, vmax, &rb.label_cnt[0], sc) : nullptr;
+  int32_t *eof = E2 ? compact_labels(el, E2, emin, emax, &rb.label_cnt[1], sc) : nullptr;
+  CK(cudaStreamSynchronize(s));
+  const long long nvl = rb.label_cnt[0], nel = rb.label_cnt[1];
+  const int32_t VL = std::max<int32_t>(1, (int32_t)nvl);
+  const int32_t EL = std::max<int32_t>(1, (int32_t)nel);
   if(VL > 65535 || EL > 65535) throw Error(ST_ERR_LIMIT, "more than 65535 distinct vertex or edge labels");
   const long long tab = (long long)VL * EL * VL;
   if(tab > (1ll << 25))
     throw Error(ST_ERR_LIMIT, "device ingest: label alphabet too large for its pair table; use gs_db_from_arrays");
 
-  // 4. pair table
-  long long *seen = fr.add(dalloc<long long>(tab)), *prank = fr.add(dalloc<long long>(tab + 1));
+  // 4. pair table (read back: the number of pairs and the largest graph)
+  long long *seen = sc.get<long long>(tab), *prank = sc.get<long long>(tab + 1);
   CK(cudaMemsetAsync(seen, 0, sizeof(long long) * tab, s));
   k_pairs_seen<<<blocks_for(V), kThreads, 0, s>>>(off, V, vl, adj_to, el, EL, VL, seen);
-  scan_exclusive(seen, prank, tab, s);
-  long long nkeys = 0;
-  CK(cudaMemcpyAsync(&nkeys, prank + tab, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  int mxv = 0;
-  int *d_mx = fr.add(dalloc<int>(1));
+  scan_exclusive(seen, prank, tab, sc);
+  int *d_mx = sc.get<int>(1);
   CK(cudaMemsetAsync(d_mx, 0, sizeof(int), s));
   k_max_ll<<<blocks_for(G), kThreads, 0, s>>>(gnv, G, d_mx);
-  CK(cudaMemcpyAsync(&mxv, d_mx, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rb.nkeys, prank + tab, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rb.max_vertices, d_mx, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  const long long nkeys = rb.nkeys;
+  const int mxv = rb.max_vertices;
 
   // the database block, laid out as Database::upload lays it out
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -419,7 +539,7 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   const size_t o_pc = o_ap + al(sizeof(int32_t) * (E2 + 1));
   const size_t total = o_pc + al(sizeof(int32_t) * (nkeys + 1));
   char *b = nullptr;
-  if(cudaMalloc(&b, total) != cudaSuccess) {
+  if(cudaMallocFromPoolAsync((void **)&b, total, cx.pool, s) != cudaSuccess) {
     cudaGetLastError();
     throw Error(ST_ERR_NOMEM, "device ingest: out of device memory");
   }
@@ -437,22 +557,26 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     CK(cudaMemcpyAsync(b + o_vl, vl, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(b + o_vg, vgraph, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(b + o_gb, vgbase, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
-    {
-      // vertex bases as int32
-      std::vector<long long> hv(G + 1);
-      CK(cudaMemcpyAsync(hv.data(), vbase, sizeof(long long) * (G + 1), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      std::vector<int32_t> v32(hv.begin(), hv.end());
-      CK(cudaMemcpyAsync(b + o_vb, v32.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice, s));
-      CK(cudaStreamSynchronize(s));
-    }
-    // host metadata: each label's pairs, in pair-index order
-    std::vector<int32_t> hro(VL + 1), hpc(std::max<long long>(nkeys, 1));
-    CK(cudaMemcpyAsync(hro.data(), ro, sizeof(int32_t) * VL, cudaMemcpyDeviceToHost, s));
-    if(nkeys) CK(cudaMemcpyAsync(hpc.data(), pc, sizeof(int32_t) * nkeys, cudaMemcpyDeviceToHost, s));
+    k_narrow<<<blocks_for(G + 1), kThreads, 0, s>>>(vbase, G + 1, (int32_t *)(b + o_vb));
+    // host metadata (label values, each label's first pair, the pair codes), one read-back
+    int32_t *hm = cx.meta_buf((size_t)(nvl + nel + VL + nkeys + 1));
+    int32_t *h_vof = hm, *h_eof = hm + nvl, *hro = hm + nvl + nel, *hpc = hro + VL;
+    if(nvl) CK(cudaMemcpyAsync(h_vof, vof, sizeof(int32_t) * nvl, cudaMemcpyDeviceToHost, s));
+    if(nel) CK(cudaMemcpyAsync(h_eof, eof, sizeof(int32_t) * nel, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hro, ro, sizeof(int32_t) * VL, cudaMemcpyDeviceToHost, s));
+    if(nkeys) CK(cudaMemcpyAsync(hpc, pc, sizeof(int32_t) * nkeys, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     CK(cudaGetLastError());
-    hro[VL] = (int32_t)nkeys;
+    LabelMap labels;
+    labels.vlabel_of.assign(h_vof, h_vof + nvl);
+    labels.elabel_of.assign(h_eof, h_eof + nel);
+    if(db.d_block && db.pooled) {
+      // a block of an earlier ingest into this database (the lock is held here)
+      cudaDeviceSynchronize();
+      cudaFreeAsync(db.d_block, s);
+      db.d_block = nullptr;
+      db.pooled = false;
+    }
     db.release();
     db.host = HostDB();
     db.host.n_graphs = G;
@@ -461,13 +585,15 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     db.EL = EL;
     db.pairs.assign(VL, {});
     db.pair_cnt.assign(VL, 0);
-    db.root_off.assign(hro.begin(), hro.begin() + VL);
+    db.root_off.assign(hro, hro + VL);
     for(int32_t a = 0; a < VL; a++) {
-      for(int32_t i = hro[a]; i < hro[a + 1]; i++) db.pairs[a].push_back({ hpc[i] >> 16, hpc[i] & 0xffff });
-      db.pair_cnt[a] = hro[a + 1] - hro[a];
+      const int32_t end = a + 1 < VL ? hro[a + 1] : (int32_t)nkeys;
+      for(int32_t i = hro[a]; i < end; i++) db.pairs[a].push_back({ hpc[i] >> 16, hpc[i] & 0xffff });
+      db.pair_cnt[a] = end - hro[a];
     }
     db.root_keys = (int32_t)nkeys;
     db.d_block = b;
+    db.pooled = true;
     db.d_bytes = total;
     db.dev = DevDB{};
     db.dev.adj = (const unsigned long long *)(b + o_adj);
@@ -491,8 +617,7 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     db.dev_vertices = V;
     db.dev_adj = E2;
   } catch(...) {
-    cudaStreamSynchronize(s);
-    cudaFree(b);
+    cudaFreeAsync(b, s);
     throw;
   }
 }

@@ -78,3 +78,38 @@ def test_device_ingest_rejects_what_host_rejects(gs, tmp_path):
             with pytest.raises(gs.GSpanError) as e:
                 gs.Database.from_arrays(n, maxv, *arrs, vc, device=device)
             assert e.value.status == 3, (device, str(e.value))
+
+
+def test_device_ingest_repeated_pooled(gs, tmp_path):
+    # the ingest's scratch and database blocks come from a pool that is kept
+    # between ingests: databases of different sizes built, failed, kept alive
+    # together and freed out of order all mine as their host conversions do
+    srcs = [gs.Database.generate(2, seed=11, scale=0.01),
+            gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt"),
+            gs.Database.generate(5, seed=12, scale=0.004)]
+    arrs = [_cudabin(db, tmp_path) for db in srcs]
+    want = []
+    for n, maxv, edges, elab, vlab, voff, vc in arrs:
+        h = gs.Database.from_arrays(n, maxv, edges, elab, vlab, voff, vc)
+        want.append(gs.mine_collect(h, max(2, int(0.05 * n)))[0])
+        h.free()
+    live = {}
+    order = [0, 1, 2, 2, 0, 1, 0, 2, 1, 1]
+    for step, i in enumerate(order):
+        n, maxv, edges, elab, vlab, voff, vc = arrs[i]
+        if step % 3 == 1:
+            # a failed ingest (self loop) between good ones
+            bad = edges.copy()
+            bad[voff[0]] = 0
+            with pytest.raises(gs.GSpanError):
+                gs.Database.from_arrays(n, maxv, bad, elab, vlab, voff, vc, device=True)
+        d = gs.Database.from_arrays(n, maxv, edges, elab, vlab, voff, vc, device=True)
+        assert gs.mine_collect(d, max(2, int(0.05 * n)))[0] == want[i], (step, i)
+        if i in live:
+            live.pop(i).free()
+        live[i] = d
+        if step == 5:
+            gs.engine_reset()   # also returns the ingest's pooled memory
+    for i, d in live.items():
+        assert gs.mine_collect(d, max(2, int(0.05 * arrs[i][0])))[0] == want[i]
+        d.free()
