@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--minsup-frac", type=float, default=0.01)
     p.add_argument("--wave-nodes", type=int, default=None)
     p.add_argument("--launch-mode", type=int, default=0, help="0: per-wave CUDA graphs, 1: direct launches")
+    p.add_argument("--extension", default="rmpath", choices=["rmpath", "lists"],
+                   help="extension strategy: rmpath scans every right-most-path vertex (default); lists joins "
+                        "the parent's per-row lists (the reference's gspan_cuda_lists)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", default="mine", choices=["mine", "batch", "serving"],
@@ -413,6 +416,9 @@ def main():
         kw["wave_nodes"] = a.wave_nodes
     if a.launch_mode:
         kw["launch_mode"] = a.launch_mode
+    if a.extension != "rmpath":
+        kw["extension"] = a.extension
+        config["extension"] = a.extension
     # warm-up (also creates the engine's pool and scratch)
     for _ in range(max(3, a.warmup)):
         g.mine_collect(db, minsup, decode=False, **kw)

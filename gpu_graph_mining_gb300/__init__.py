@@ -51,7 +51,12 @@ class MineOpts(ctypes.Structure):
                 ("wave_rows", ctypes.c_int64), ("wave_words", ctypes.c_int64),
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
                 ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
-                ("count_grid", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("count_grid", ctypes.c_int32), ("extension", ctypes.c_int32)]
+
+
+# extension strategies (gs_mine_opts.extension)
+EXTENSION_RMPATH = 0
+EXTENSION_LISTS = 1
 
 
 class ConvertInfo(ctypes.Structure):
@@ -77,7 +82,8 @@ class MineStats(ctypes.Structure):
                 ("peak_pool_bytes", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
                 ("host_build_ms", ctypes.c_double), ("host_wait_ms", ctypes.c_double),
                 ("host_select_ms", ctypes.c_double), ("host_emit_ms", ctypes.c_double),
-                ("min_host_checks", ctypes.c_int64)]
+                ("min_host_checks", ctypes.c_int64), ("list_entries", ctypes.c_int64),
+                ("join_nodes", ctypes.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -299,8 +305,16 @@ def code_to_string(code):
     return ";".join("(%d %d %d %d %d)" % tuple(d) for d in code)
 
 
+def _extension(x):
+    if x in (EXTENSION_RMPATH, "rmpath", None):
+        return EXTENSION_RMPATH
+    if x in (EXTENSION_LISTS, "lists"):
+        return EXTENSION_LISTS
+    raise ValueError("extension must be 'rmpath' or 'lists'")
+
+
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
-          root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0):
+          root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0, extension=EXTENSION_RMPATH):
     o = MineOpts()
     lib().gs_mine_opts_default(ctypes.byref(o))
     o.max_edges = int(max_edges)
@@ -318,16 +332,19 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
     o.min_check = int(min_check)
     o.launch_mode = int(launch_mode)
     o.count_grid = int(count_grid)
+    o.extension = _extension(extension)
     return o
 
 
 def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
-         wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0):
+         wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0,
+         extension=EXTENSION_RMPATH):
     """Mines db at absolute support minsup.
 
     Returns (patterns, stats): patterns is a list of (code, support) with code a
     tuple of 5-tuples, in the reference's traversal order (empty when
     collect=False); sink(code, support) is called per pattern if given.
+    extension="lists" selects the reference's lists (intersection) strategy.
     """
     out = []
 
@@ -340,7 +357,7 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
 
     fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
     o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check,
-              launch_mode, count_grid)
+              launch_mode, count_grid, extension)
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()

@@ -51,6 +51,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   m.min_check = o->min_check == 1 ? 1 : 0;
   m.launch_mode = o->launch_mode == 1 ? 1 : 0;
   if(o->count_grid > 0 && o->count_grid <= 1024) m.count_grid = o->count_grid;
+  m.extension = o->extension == GS_EXTENSION_LISTS ? 1 : 0;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -83,6 +84,8 @@ void fill_stats(const gsgb::MineStats &s, gs_mine_stats *o)
   o->host_select_ms = s.host_select_ms;
   o->host_emit_ms = s.host_emit_ms;
   o->min_host_checks = s.min_host;
+  o->list_entries = s.list_entries;
+  o->join_nodes = s.join_nodes;
 }
 
 struct BatchCtx {
@@ -255,7 +258,7 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->min_check = m.min_check;
   o->launch_mode = m.launch_mode;
   o->count_grid = m.count_grid;
-  o->reserved = 0;
+  o->extension = m.extension;
 }
 
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,

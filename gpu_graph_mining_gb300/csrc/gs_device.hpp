@@ -62,7 +62,22 @@ struct NodeDesc {
   int32_t code_off;      // the node's DFS code: edges code_off.. of the wave's code table
   int32_t code_len;      //   (5 int32 per edge: from, to, fromlabel, elabel, tolabel)
   int32_t nfwd;          // keys below nfwd are forward extensions
-  int32_t pad2;
+  // Lists strategy (extension by intersection): a forward child's extensions
+  // from right-most-path vertices other than its new right-most vertex are
+  // its parent's frequent forward extensions at the same parent row (minus
+  // the child's new vertex), read from the parent's per-row lists instead of
+  // the database; only the right-most vertex's adjacency is scanned.  The
+  // child's right-most path up to the new edge's source u is the parent's, so
+  // those slots have the parent's forward keys: a list entry's parent key lk
+  // is the child's key when lk < join_hi (slots up to u) and, from u itself,
+  // lk >= join_key (pairs at or after the new edge's).  csr_off == nullptr:
+  // no join, every right-most-path vertex is scanned.
+  const int32_t *csr_off;  // [csr_rows + 1] the parent rows' list offsets into csr_ent
+  const int2 *csr_ent;     // list entries {neighbour, parent's forward key}
+  int32_t csr_rows;        // parent rows
+  int32_t join_lo;         // first forward key of u
+  int32_t join_key;        // the new edge's key (in the parent)
+  int32_t join_hi;         // one past u's forward keys
 };
 
 // One right-most-path vertex of a node.

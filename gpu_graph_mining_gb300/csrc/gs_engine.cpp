@@ -547,6 +547,14 @@ struct PNode {
   int32_t gord_blk;
   int64_t nrows;
   int64_t support;
+  // lists strategy (forward children whose parent kept its per-row lists):
+  // the parent's lists (a pool block shared by the parent's wave) and the
+  // join rule (NodeDesc::join_lo / join_key / join_hi)
+  int32_t list_blk = -1;
+  const int32_t *list_off = nullptr;
+  const int2 *list_ent = nullptr;
+  int64_t list_rows = 0;
+  int32_t join_lo = 0, join_key = 0, join_hi = 0;
 };
 
 // One mining job inside a scheduler.
@@ -651,6 +659,7 @@ struct WaveCtx {
   DBuf<int4> d_rec;
   DBuf<unsigned long long> d_recn;
   DBuf<long long> d_keyword;
+  DBuf<int32_t> d_lnode;   // lists strategy: the node of each frequent forward key
   // A wave's results, copied back in one piece: a 64-byte header (kHead*
   // slots) followed by the selected candidates {key, support, embeddings,
   // verdict}.  The zeroed region holds the embedding counts and the support
@@ -684,7 +693,7 @@ struct WaveCtx {
   void free()
   {
     d_desc.free(); d_bm.free(); d_bmx.free(); d_cnt.free(); d_sup.free(); d_childmap.free(); d_cursor.free();
-    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free(); d_listed.free();
+    d_outs.free(); d_rec.free(); d_recn.free(); d_keyword.free(); d_listed.free(); d_lnode.free();
     d_head.free(); d_zero.free(); d_mat.free(); h_head.free(); h_mat.free();
     h_desc.free(); h_sup.free(); h_cnt.free(); h_childmap.free(); h_outs.free(); h_keyword.free(); h_misc.free();
     sel_hint = 4096;
@@ -957,6 +966,7 @@ struct Flight {
   const int2 *const *dc = nullptr;
   const SlotDesc *ds = nullptr;
   const int32_t *dv = nullptr, *dl = nullptr;
+  bool join = false;         // some node joins its parent's lists (lists strategy)
   int32_t W = 0, kb = 0, kmax = 1;
   bool small = true;
   int64_t tb = 0;
@@ -1130,6 +1140,8 @@ private:
     for(int32_t id : p.cols) S.live_bytes -= E.unref(id);
     S.live_bytes -= p.nrows * (int64_t)sizeof(int32_t);
     E.block_unref(p.gord_blk);
+    if(p.list_blk >= 0) E.block_unref(p.list_blk);
+    p.list_blk = -1;
     S.pending--;
   }
 
@@ -1394,10 +1406,12 @@ private:
 
     // descriptors
     int32_t tot_cols = 0, tot_slots = 0, tot_edges = 0;
+    bool any_join = false;
     for(int32_t n = 0; n < W; n++) {
       tot_cols += (int32_t)nodes[n].cols.size();
       tot_slots += (int32_t)lays[n].slots.size();
       tot_edges += (int32_t)nodes[n].code.size();
+      any_join = any_join || nodes[n].list_off != nullptr;
     }
     size_t off = 0;
     size_t need = 256 * 7 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
@@ -1443,6 +1457,16 @@ private:
       d.code_off = eo;
       d.code_len = (int32_t)p.code.size();
       d.nfwd = L.nfwd;
+      if(p.list_off) {
+        // lists strategy: join the parent's per-row lists
+        d.csr_off = p.list_off;
+        d.csr_ent = p.list_ent;
+        d.csr_rows = (int32_t)p.list_rows;
+        d.join_lo = p.join_lo;
+        d.join_key = p.join_key;
+        d.join_hi = p.join_hi;
+        st_.join_nodes++;
+      }
       for(const DFS &e : p.code) {
         int32_t *c = hcode + 5 * (size_t)eo++;
         c[0] = e.from;
@@ -1477,6 +1501,7 @@ private:
     f.dv = (const int32_t *)(db_ + ((char *)hv - hb));
     f.dl = (const int32_t *)(db_ + ((char *)hl - hb));
     const int32_t *dcode = (const int32_t *)(db_ + ((char *)hcode - hb));
+    f.join = any_join;
     f.W = W;
     f.kb = kb;
     f.kmax = kmax;
@@ -1539,11 +1564,16 @@ private:
     q.d2h_bytes = kHeadBytes + sizeof(int4) * (size_t)f.sel_copied;
     q.count = wave_count_call(f.dn, W, tb, kmax, small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, cnt, E.d_bytes.p + 0,
                               err_flag(), f.rec, f.rec_cap, f.rec ? head + kHeadRecords : nullptr,
-                              wo_.count_grid, ccopies, cstride);
+                              wo_.count_grid, ccopies, cstride, f.join);
+    int32_t *lnode = nullptr;
+    if(wo_.extension == 1) {
+      X.d_lnode.ensure(std::max(kb, 1));
+      lnode = X.d_lnode.p;
+    }
     q.screen = screen_keys_call(f.dn, W, kb, cnt, ccopies, cstride, X.d_childmap.p, X.d_listed.p,
-                                head + kHeadSelected, err_flag(), head + kHeadFlags);
+                                head + kHeadSelected, err_flag(), head + kHeadFlags, lnode);
     q.listed = count_listed_call(f.dn, X.d_listed.p, f.bm, cnt, X.d_bmx.p, X.d_keyword.p, sel, kb,
-                                 head + kHeadSelected);
+                                 head + kHeadSelected, lnode);
     q.with_min = wo_.min_check == 0;
     if(q.with_min) q.ismin = is_min_call(f.dn, W, f.ds, E.d_dbs.p, dcode, sel, kb, head + kHeadSelected);
     issue(X, q);
@@ -1644,6 +1674,14 @@ private:
     // children in node order (a node's children are contiguous, from made_at[n])
     std::vector<PNode> made;
     std::vector<int32_t> made_at(W + 1, 0);
+    // lists strategy: every node with a forward child to materialise keeps
+    // per-row lists of its frequent forward extensions (built from this
+    // wave's records) for those children's joins
+    int32_t list_blk = -1;
+    int32_t *list_off = nullptr, *list_scr = nullptr;
+    int2 *list_ent = nullptr;
+    int64_t list_rows = 0, list_n = 0;
+    std::vector<int32_t> list_rb;  // per node: its first list row, or -1
     {
       // accepted candidates; cands is in key order, so each node's are contiguous
       std::vector<int32_t> acc;
@@ -1682,6 +1720,31 @@ private:
         }
         a0 = a1;
       }
+      if(wo_.extension == 1 && f.rec && nrec >= 0 && nrec <= f.rec_cap) {
+        list_rb.assign(W, -1);
+        std::vector<char> need(W, 0);
+        for(const Mat &m : mats)
+          if(cands[m.cand].dfs.is_forward()) need[m.node] = 1;
+        for(int32_t n = 0; n < W; n++)
+          if(need[n]) {
+            list_rb[n] = (int32_t)list_rows;
+            list_rows += nodes[n].nrows;
+          }
+        for(const Candidate &cd : cands)
+          if(need[cd.node] && cd.key < lays[cd.node].nfwd) list_n += cd.cnt;
+        if(list_rows > 0 && list_rows + 1 < INT32_MAX && list_n < INT32_MAX) {
+          const size_t lb = Carver::round(sizeof(int32_t) * (size_t)(list_rows + 1)) +
+                            Carver::round(sizeof(int2) * (size_t)std::max<int64_t>(list_n, 1)) +
+                            Carver::round(sizeof(int32_t) * (size_t)list_scan_scratch(list_rows));
+          list_blk = E.new_block(lb);
+          Carver lc{ (char *)E.blocks[list_blk].base };
+          list_off = lc.take<int32_t>((size_t)(list_rows + 1));
+          list_ent = lc.take<int2>((size_t)std::max<int64_t>(list_n, 1));
+          list_scr = lc.take<int32_t>((size_t)list_scan_scratch(list_rows));
+        } else {
+          list_rb.clear();
+        }
+      }
       // pass 2: every child's new column and graph ranks carved from one block
       if(!mats.empty()) {
         const int32_t blk = E.new_block(bytes);
@@ -1717,6 +1780,28 @@ private:
           E.block_ref(blk);
           nn.nrows = rowsn;
           nn.support = cd.support;
+          if(list_blk >= 0 && cd.dfs.is_forward() && list_rb[m.node] >= 0) {
+            nn.list_blk = list_blk;
+            E.block_ref(list_blk);
+            nn.list_off = list_off + list_rb[m.node];
+            nn.list_ent = list_ent;
+            nn.list_rows = p.nrows;
+            // the child's right-most path up to the new edge's source u is
+            // the parent's, with the same forward keys: the parent's keys
+            // from u's slot and the slots before it stay keys of the child
+            // (from u only those at or after the new edge's pair)
+            // (gspan_cuda_lists.cpp:327-369 possible_extension, 372-443 the
+            // forward-forward joins)
+            const NodeLayout &Lp = lays[m.node];
+            for(const SlotDesc &sd : Lp.slots) {
+              const int32_t hi = sd.fkey_off + S.job.db->pair_cnt[sd.vlab];
+              if(cd.key >= sd.fkey_off && cd.key < hi) {
+                nn.join_lo = sd.fkey_off;
+                nn.join_key = cd.key;
+                nn.join_hi = hi;
+              }
+            }
+          }
           S.live_bytes += rowsn * (int64_t)(sizeof(int2) + sizeof(int32_t));
           S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
           made.push_back(std::move(nn));
@@ -1727,26 +1812,37 @@ private:
     if(!outs.empty()) {
       // one upload: children's outputs, then the (key, child) pairs
       const size_t outs_bytes = Carver::round(sizeof(ChildOut) * outs.size());
-      const size_t mat_bytes = outs_bytes + sizeof(int2) * pairs.size();
+      const size_t pairs_bytes = Carver::round(sizeof(int2) * pairs.size());
+      const size_t mat_bytes = outs_bytes + pairs_bytes + (list_blk >= 0 ? sizeof(int32_t) * (size_t)W : 0);
       X.d_mat.ensure(mat_bytes);
       X.h_mat.ensure(mat_bytes);
       std::memcpy(X.h_mat.p, outs.data(), sizeof(ChildOut) * outs.size());
       std::memcpy(X.h_mat.p + outs_bytes, pairs.data(), sizeof(int2) * pairs.size());
+      if(list_blk >= 0) std::memcpy(X.h_mat.p + outs_bytes + pairs_bytes, list_rb.data(), sizeof(int32_t) * W);
       h2d(X.d_mat.p, X.h_mat.p, mat_bytes);
       const ChildOut *douts = (const ChildOut *)X.d_mat.p;
       X.d_cursor.ensure(outs.size());
       CK(cudaEventRecord(X.ev[4], E.stream));
       launch_scatter_childmap((const int2 *)(X.d_mat.p + outs_bytes), (int32_t)pairs.size(), X.d_childmap.p,
                               X.d_cursor.p, (int32_t)outs.size(), E.stream);
+      // lists strategy: the records pass also counts the list rows
+      ListBuild lb{ X.d_lnode.p, f.dn, (const int32_t *)(X.d_mat.p + outs_bytes + pairs_bytes) };
+      if(list_blk >= 0) CK(cudaMemsetAsync(list_off, 0, sizeof(int32_t) * (size_t)(list_rows + 1), E.stream));
       if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
         launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, f.bm, X.d_bmx.p, f.cnt, f.cstride,
-                                   douts, E.d_bytes.p + 1, err_flag(), E.stream);
+                                   douts, E.d_bytes.p + 1, err_flag(), list_blk >= 0 ? &lb : nullptr,
+                                   list_off + 1, E.stream);
       } else {
         // records overflowed (or are disabled): enumerate again
         launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, X.d_bmx.p,
-                                X.d_childmap.p, X.d_cursor.p, douts, E.d_bytes.p + 1, err_flag(), E.stream);
+                                X.d_childmap.p, X.d_cursor.p, douts, E.d_bytes.p + 1, err_flag(), f.join, E.stream);
         if(f.rec) X.wanted_rec = std::max<long long>(X.wanted_rec, nrec + nrec / 4);
+      }
+      if(list_blk >= 0) {
+        launch_fill_lists(f.rec, nrec, lb, list_off, list_rows, list_ent, list_n, list_scr, err_flag(), E.stream);
+        st_.list_entries += list_n;
+        st_.launches += 2;
       }
       CK(cudaEventRecord(X.ev[5], E.stream));
       st_.launches += 2;

@@ -100,6 +100,10 @@ struct MineOptions {
   int32_t min_check = 0;      // canonicality: 0 on the GPU (host for oversized patterns), 1 on the host
   int32_t launch_mode = 0;    // a wave's device work: 0 replayed from a CUDA graph, 1 launched directly
   int32_t count_grid = 0;     // count-kernel grid cap in blocks per SM (0 = the built-in default)
+  int32_t extension = 0;      // extension strategy: 0 every right-most-path vertex's adjacency is
+                              // scanned; 1 lists: forward children join their parent's per-row
+                              // lists of frequent forward extensions and scan only their new
+                              // right-most vertex (the reference's gspan_cuda_lists)
 };
 
 struct MineStats {
@@ -126,6 +130,8 @@ struct MineStats {
   double host_select_ms = 0; // candidate decoding, child allocation, child tables
   double host_emit_ms = 0;   // pattern-tree traversal and output
   int64_t min_host = 0;      // candidates whose canonicality was checked on the host
+  int64_t list_entries = 0;  // lists strategy: per-row list entries built
+  int64_t join_nodes = 0;    // lists strategy: nodes extended through a join
 };
 
 struct MineJob {

@@ -7,6 +7,7 @@
 // flags 32-byte extension records per candidate (compute_support.cpp:146-257,
 // 805-960).
 #include "gs_kernels.hpp"
+#include "gs_lists.cuh"
 
 namespace gsgb {
 
@@ -206,7 +207,8 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
                                                          int total_keys, int32_t *cnt, int cnt_copies,
                                                          long long cnt_stride, int32_t *childmap, int2 *listed,
                                                          unsigned long long *counters,
-                                                         const unsigned int *err, unsigned long long *err_copy)
+                                                         const unsigned int *err, unsigned long long *err_copy,
+                                                         int32_t *lnode)
 {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -229,6 +231,7 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
     bool cand = false;
     if(c > 0) {
       childmap[key] = -1;
+      if(lnode) lnode[key] = -1;
       ext += (unsigned long long)c;
       n = find_node_by_key(nodes, nnodes, key);
       cand = c >= nodes[n].minsup;
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restr
                                                           const uint32_t *__restrict__ bm,
                                                           int32_t *cnt, int32_t *bmx,
                                                           long long *keyword, int4 *sel, int sel_cap,
-                                                          unsigned long long *counters)
+                                                          unsigned long long *counters, int32_t *lnode)
 {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -289,7 +292,98 @@ __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restr
       if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], 0);
       // the total has been read: copy 0 turns into the cursor of copy 0's share
       cnt[kn.x] = 0;
+      // lists strategy: a frequent forward key goes into its node's per-row lists
+      if(lnode && kn.x - nd.key_base < nd.nfwd) lnode[kn.x] = kn.y;
     }
+  }
+}
+
+// ---- lists strategy: per-row lists of the frequent forward extensions
+
+// cursor[r] starts at list row r's offset and ends at the next row's
+__global__ void __launch_bounds__(kBlock) k_list_fill(const int4 *__restrict__ rec, long long n, const ListBuild lb,
+                                                      int32_t *cursor, int2 *ent, long long ent_cap,
+                                                      unsigned int *err)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int4 x = __ldg(&rec[i]);
+    long long row;
+    int lk;
+    if(list_entry(x, lb, row, lk, err)) {
+      const int pos = atomicAdd(&cursor[row], 1);
+      if((unsigned)pos < (unsigned long long)ent_cap) ent[pos] = make_int2(x.y, lk);
+      else atomicOr(err, 4u);
+    }
+  }
+}
+
+// ---- exclusive scan of int32 counts in place, 1024 per block
+constexpr int kScanPer = 1024;
+
+__global__ void __launch_bounds__(kBlock) k_xscan_blocks(int32_t *x, long long n, int32_t *sums)
+{
+  __shared__ int32_t wsum[kBlock / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long base = (long long)blockIdx.x * kScanPer + (long long)threadIdx.x * 4;
+  int v[4], t = 0;
+#pragma unroll
+  for(int j = 0; j < 4; j++) {
+    v[j] = base + j < n ? x[base + j] : 0;
+    t += v[j];
+  }
+  int incl = t;
+  for(int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if(lane >= o) incl += u;
+  }
+  if(lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if(w == 0) {
+    int y = lane < kBlock / 32 ? wsum[lane] : 0;
+    for(int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, y, o);
+      if(lane >= o) y += u;
+    }
+    if(lane < kBlock / 32) wsum[lane] = y;
+  }
+  __syncthreads();
+  int run = (w > 0 ? wsum[w - 1] : 0) + incl - t;
+#pragma unroll
+  for(int j = 0; j < 4; j++) {
+    if(base + j < n) x[base + j] = run;
+    run += v[j];
+  }
+  if(threadIdx.x == kBlock - 1) sums[blockIdx.x] = run;
+}
+
+__global__ void __launch_bounds__(kBlock) k_xscan_add(int32_t *x, long long n, const int32_t *offs)
+{
+  const long long base = (long long)blockIdx.x * kScanPer;
+  const int add = offs[blockIdx.x];
+  for(int j = threadIdx.x; j < kScanPer; j += kBlock)
+    if(base + j < n) x[base + j] += add;
+}
+
+// x[0..n) -> exclusive prefix sums; scratch: xscan_scratch(n) ints
+long long xscan_scratch(long long n)
+{
+  long long tot = 0;
+  while(n > 1) {
+    n = (n + kScanPer - 1) / kScanPer;
+    tot += n;
+  }
+  return tot;
+}
+
+void xscan(int32_t *x, long long n, int32_t *scratch, cudaStream_t s)
+{
+  if(n <= 0) return;
+  const long long nb = (n + kScanPer - 1) / kScanPer;
+  k_xscan_blocks<<<(unsigned)nb, kBlock, 0, s>>>(x, n, scratch);
+  if(nb > 1) {
+    xscan(scratch, nb, scratch + nb, s);
+    k_xscan_add<<<(unsigned)nb, kBlock, 0, s>>>(x, n, scratch);
   }
 }
 
@@ -356,7 +450,8 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 
 KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
                             int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
-                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy)
+                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy,
+                            int32_t *lnode)
 {
   KernelCall c;
   c.func = (const void *)k_screen_keys;
@@ -373,12 +468,13 @@ KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total
   c.arg(counters);
   c.arg(err);
   c.arg(err_copy);
+  c.arg(lnode);
   return c;
 }
 
 KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, int32_t *cnt,
                              int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
-                             unsigned long long *counters)
+                             unsigned long long *counters, int32_t *lnode)
 {
   KernelCall c;
   c.func = (const void *)k_count_listed;
@@ -393,7 +489,22 @@ KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const ui
   c.arg(sel);
   c.arg(sel_cap);
   c.arg(counters);
+  c.arg(lnode);
   return c;
+}
+
+int64_t list_scan_scratch(int64_t n) { return xscan_scratch(n) + 1; }
+
+void launch_fill_lists(const int4 *rec, long long nrec, const ListBuild &lb, int32_t *off, int64_t nrows_total,
+                       int2 *ent, int64_t ent_cap, int32_t *scratch, unsigned int *err, cudaStream_t s)
+{
+  if(nrec <= 0 || nrows_total <= 0) return;
+  // the counts of row r are at off[r + 1]; their exclusive scan makes off[r + 1]
+  // the start of row r, which the fill's cursor adds carry to the start of
+  // row r + 1, with off[0] = 0
+  int32_t *cnt = off + 1;
+  xscan(cnt, nrows_total, scratch, s);
+  k_list_fill<<<grid_for(nrec), kBlock, 0, s>>>(rec, nrec, lb, cnt, ent, ent_cap, err);
 }
 
 void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, int32_t *cursor, int32_t ncursor,

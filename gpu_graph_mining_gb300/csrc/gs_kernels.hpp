@@ -12,6 +12,16 @@
 
 namespace gsgb {
 
+// Extension records of the count pass, int4 {key field, x, y, graph rank}: the
+// key field holds the wave key in bits 0-26 and the counter copy the
+// extension was counted in in bits 27-30 (-1: an unused slot).  A forward
+// extension has (x, y) = (new vertex, parent row), a backward one the copy of
+// the parent row's last column element.
+constexpr int kRecCopyShift = 27;
+constexpr int kRecKeyMask = (1 << kRecCopyShift) - 1;
+
+struct ListBuild;
+
 // A kernel launch as data: function, shape and argument values.  run()
 // launches it on a stream; params() gives the argument pointers a CUDA graph
 // kernel node takes (the graph copies the values when the node is set).
@@ -66,13 +76,13 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
                            unsigned long long *rec_n, int32_t grid_per_sm, int32_t cnt_copies,
-                           long long cnt_stride);
+                           long long cnt_stride, bool join);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned long long *bytes, unsigned int *err, cudaStream_t s);
+                             unsigned long long *bytes, unsigned int *err, bool join, cudaStream_t s);
 
 // Materialise from the count pass's records {wave key, x, y, graph rank}:
 // children whose key is selected get column element (x, y) and their graph
@@ -80,9 +90,12 @@ void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long to
 // cursor: the wave's counter copies after selection (copy q of a key starts
 // at the count of copies 0..q-1), cursor_stride apart; a record's copy is in
 // bits 27-30 of its key field.
+// lists (may be null): also counts each list row's entries at list_cnt[row]
+// (lists strategy, launch_fill_lists)
 void launch_materialize_records(const int4 *rec, long long n, const int32_t *childmap, const long long *keyword,
                                 const uint32_t *bm, const int32_t *bmx, int32_t *cursor, long long cursor_stride,
-                                const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s);
+                                const ChildOut *outs, unsigned long long *bytes, unsigned int *err,
+                                const ListBuild *lists, int32_t *list_cnt, cudaStream_t s);
 
 // Extension records given as (key, graph id) pairs: sets bit [key][graph].
 // Keys and graph ids must be in range (checked by the caller).
@@ -95,12 +108,16 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 // counters: [0] selected keys, [1] embeddings of all keys, [2] keys listed for
 // counting; listed and sel hold total_keys entries.  *err_copy = *err (the
 // consistency flags after the count pass).
+// lnode (lists strategy, may be null): reset to -1 for every key with extensions
 KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
                             int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
-                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy);
+                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy,
+                            int32_t *lnode);
+// lnode (lists strategy, may be null): lnode[key] = the key's node for every
+// frequent forward key
 KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, int32_t *cnt,
                              int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
-                             unsigned long long *counters);
+                             unsigned long long *counters, int32_t *lnode);
 // Canonicality of the selected candidates (gs_ismin.cu): sel[i].w = 1 minimal,
 // 0 not minimal, 2 left to the host.  codes = the wave's code table.
 KernelCall is_min_call(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
@@ -110,5 +127,24 @@ void launch_scatter_childmap(const int2 *pairs, int32_t n, int32_t *childmap, in
                              cudaStream_t s);
 void launch_support(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, const uint32_t *bm, int32_t *bmx,
                     int32_t *support, cudaStream_t s);
+
+// Lists strategy: the per-row lists of a wave's nodes' frequent forward
+// extensions, built from the count pass's records (ListBuild, gs_lists.cuh):
+// the records materialise pass adds each list row's entry count at off[r + 1]
+// (off zeroed before), then launch_fill_lists turns the counts into offsets
+// off[0..nrows_total] and writes ent[off[r] ..], the entries {neighbour, the
+// node's forward key} of list row r; entries past ent_cap set err bit 4 and
+// are dropped.  scratch holds list_scan_scratch(nrows_total) ints.
+// The lists of one wave: lnode[wave key] = the node of a frequent forward key
+// (else -1); node n's rows are list rows rowbase[n] .. (rowbase[n] < 0: the
+// node keeps no lists).
+struct ListBuild {
+  const int32_t *lnode;
+  const NodeDesc *nodes;
+  const int32_t *rowbase;
+};
+int64_t list_scan_scratch(int64_t n);
+void launch_fill_lists(const int4 *rec, long long nrec, const ListBuild &lb, int32_t *off, int64_t nrows_total,
+                       int2 *ent, int64_t ent_cap, int32_t *scratch, unsigned int *err, cudaStream_t s);
 
 }  // namespace gsgb

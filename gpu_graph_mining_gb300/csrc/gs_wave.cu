@@ -27,6 +27,7 @@
 // writes only bitmap bits and counters; the materialise pass writes only the
 // selected children's 8-byte column elements and 4-byte graph ranks.
 #include "gs_kernels.hpp"
+#include "gs_lists.cuh"
 
 namespace gsgb {
 
@@ -50,8 +51,6 @@ constexpr unsigned kFull = 0xffffffffu;
 #define GS_REC_CHUNK 128
 #endif
 constexpr int kRecChunk = GS_REC_CHUNK;  // records a warp reserves at a time
-constexpr int kRecCopyShift = 27;  // record key field: wave key (bits 0-26) | counter copy (27-30)
-constexpr int kRecKeyMask = (1 << kRecCopyShift) - 1;
 
 struct WaveArgs {
   const NodeDesc *nodes;
@@ -85,9 +84,10 @@ template <int KMAX> struct Smem {
   unsigned long long mask[32];  // small graphs: the row's graph-local vertex ids as a bit set
   int gb[32];                   // small graphs: first global vertex of the row's graph
   int phi[KMAX][32];        // graph vertex of pattern vertex t for lane l
-  int start[KMAX][32];      // adjacency start of right-most-path slot s
-  int pre[KMAX + 1][32];    // degree prefix over slots
+  int start[KMAX][32];      // scanned position p: adjacency (or parent list) start
+  int pre[KMAX + 1][32];    // item prefix over the scanned positions
   SlotDesc slot[KMAX];      // the tile's node: right-most-path slots
+  int join_lo, join_key, join_hi;  // the tile's node: join rule (lists strategy)
   int vtab[KMAX];           // the tile's node: pattern vertex -> backward slot
   const int2 *col[KMAX];    // the tile's node: its columns and their lengths,
   int clen[KMAX];           // loaded once so the walk's chain is one load per column
@@ -102,8 +102,10 @@ __device__ __forceinline__ unsigned lanemask_lt()
 
 // MASK: every graph of the wave's databases has at most 64 vertices, so
 // "is w already in the embedding" is one bit test of the row's vertex set
-// instead of a loop over its k vertices.
-template <int KMAX, bool MAT, bool MASK>
+// instead of a loop over its k vertices.  JOIN: some node of the wave joins
+// its parent's per-row lists (lists strategy); without it the join code is
+// compiled out.
+template <int KMAX, bool MAT, bool MASK, bool JOIN>
 __global__ void
 #if GS_WAVE_MINB > 0
 __launch_bounds__(kWarps * 32, GS_WAVE_MINB)
@@ -153,7 +155,21 @@ k_wave(const WaveArgs a)
       if(lane == 0) atomicOr(a.err, 2u);
       continue;
     }
+    // scanned positions: slots s0..nslot-1 (adjacency), then with a join the
+    // parent's list of the row (lists strategy: s0 = the right-most vertex)
+    const bool join = JOIN && nd.csr_off != nullptr;
+    if(join && nslot < 2) {
+      if(lane == 0) atomicOr(a.err, 2u);
+      continue;
+    }
+    const int s0 = join ? nslot - 1 : 0;
+    const int np = nslot - s0 + (join ? 1 : 0);
     if(lane < nslot) S.slot[lane] = a.slots[nd.slot_off + lane];
+    if(join && lane == 0) {
+      S.join_lo = nd.join_lo;
+      S.join_key = nd.join_key;
+      S.join_hi = nd.join_hi;
+    }
     if(lane < k) {
       S.vtab[lane] = a.vtab[nd.vtab_off + lane];
       S.col[lane] = a.coltab[nd.col_off + lane];
@@ -195,16 +211,27 @@ k_wave(const WaveArgs a)
       S.mask[lane] = m;
       S.gb[lane] = gb;
     }
+    if(valid && join && (unsigned)last_prev >= (unsigned)nd.csr_rows) {
+      atomicOr(a.err, 2u);
+      valid = false;
+    }
     if(valid) {
-      for(int s = 0; s < nslot; ++s) {
+      for(int s = s0; s < nslot; ++s) {
         const int v = S.phi[S.slot[s].vertex][lane];
         const int a0 = __ldg(&adj_off[v]), a1 = __ldg(&adj_off[v + 1]);
-        S.start[s][lane] = a0;
-        S.pre[s][lane] = W;
+        S.start[s - s0][lane] = a0;
+        S.pre[s - s0][lane] = W;
         W += a1 - a0;
       }
-      S.pre[nslot][lane] = W;
-      mine += 8ull * k + 4 + 8ull * nslot + (MASK ? 8 : 0);
+      if(join) {
+        // the parent row's list (the last column's back-link is the parent row)
+        const int c0 = __ldg(&nd.csr_off[last_prev]), c1 = __ldg(&nd.csr_off[last_prev + 1]);
+        S.start[np - 1][lane] = c0;
+        S.pre[np - 1][lane] = W;
+        W += c1 - c0;
+      }
+      S.pre[np][lane] = W;
+      mine += 8ull * k + 4 + 8ull * np + (MASK ? 8 : 0);
     }
     __syncwarp();
     // ---- phase 2: the tile's (row, slot, neighbour) items, 32 at a time
@@ -239,10 +266,17 @@ k_wave(const WaveArgs a)
       if(has_n) {
         int sl = 0;
         while(S.pre[sl + 1][o] <= q) sl++;
-        s_n = sl;
         const int e = S.start[sl][o] + (q - S.pre[sl][o]);
-        ent_n = __ldg(&adj[e]);
-        pr_n = __ldg(&adj_pair[e]);
+        if(join && sl == np - 1) {
+          // a parent list entry {neighbour, parent's forward key}
+          const int2 je = __ldg(&nd.csr_ent[e]);
+          s_n = -1;
+          ent_n = ((unsigned long long)(unsigned)je.y << 32) | (unsigned)je.x;
+        } else {
+          s_n = s0 + sl;
+          ent_n = __ldg(&adj[e]);
+          pr_n = __ldg(&adj_pair[e]);
+        }
       }
     };
     if(T > 0) locate(lane);
@@ -256,7 +290,16 @@ k_wave(const WaveArgs a)
       const int lp_o = __shfl_sync(kFull, last_prev, o);
       int key = -1, w = 0;
       bool bwd = false;
-      if(has) {
+      if(JOIN && has && s < 0) {
+        // lists strategy: the parent's frequent forward extension, still one
+        // of this node's if its source is on this node's right-most path
+        // (key below join_hi), its (edge label, target label) is allowed from
+        // there (from u: at or after the new edge's, keys follow that order),
+        // and its target is not the node's new vertex
+        w = (int)(unsigned)(ent & 0xffffffffull);
+        const int lk = (int)(ent >> 32);
+        if(lk < S.join_hi && (lk < S.join_lo || lk >= S.join_key) && w != S.phi[k - 1][o]) key = lk;
+      } else if(has) {
         const int frule = S.slot[s].frule, fko = S.slot[s].fkey_off;
         w = (int)(unsigned)(ent & 0xffffffffull);
         const int hi = (int)(ent >> 32);  // (edge label << 16) | neighbour label
@@ -359,33 +402,38 @@ k_wave(const WaveArgs a)
   }
 }
 
-template <int KMAX, bool MAT, bool MASK> void launch_k(const WaveArgs &a, cudaStream_t s)
+template <int KMAX, bool MAT, bool MASK, bool JOIN> void launch_k(const WaveArgs &a, cudaStream_t s)
 {
   const size_t smem = sizeof(Smem<KMAX>) * kWarps;
   static bool configured = false;
   if(!configured) {
-    cudaFuncSetAttribute(k_wave<KMAX, MAT, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_wave<KMAX, MAT, MASK, JOIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
   const long long cap = 152LL * GS_WAVE_GRID;
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
-  k_wave<KMAX, MAT, MASK><<<(int)blocks, kWarps * 32, smem, s>>>(a);
+  k_wave<KMAX, MAT, MASK, JOIN><<<(int)blocks, kWarps * 32, smem, s>>>(a);
 }
 
-template <bool MAT, bool MASK> void dispatch_k(int kmax, const WaveArgs &a, cudaStream_t s)
+template <bool MAT, bool MASK, bool JOIN> void dispatch_k(int kmax, const WaveArgs &a, cudaStream_t s)
 {
-  if(kmax <= 8) launch_k<8, MAT, MASK>(a, s);
-  else if(kmax <= 16) launch_k<16, MAT, MASK>(a, s);
-  else if(kmax <= 32) launch_k<32, MAT, MASK>(a, s);
-  else launch_k<64, MAT, MASK>(a, s);
+  if(kmax <= 8) launch_k<8, MAT, MASK, JOIN>(a, s);
+  else if(kmax <= 16) launch_k<16, MAT, MASK, JOIN>(a, s);
+  else if(kmax <= 32) launch_k<32, MAT, MASK, JOIN>(a, s);
+  else launch_k<64, MAT, MASK, JOIN>(a, s);
 }
 
-template <bool MAT> void dispatch(int kmax, bool small_graphs, const WaveArgs &a, cudaStream_t s)
+template <bool MAT> void dispatch(int kmax, bool small_graphs, bool join, const WaveArgs &a, cudaStream_t s)
 {
-  if(small_graphs) dispatch_k<MAT, true>(kmax, a, s);
-  else dispatch_k<MAT, false>(kmax, a, s);
+  if(small_graphs) {
+    if(join) dispatch_k<MAT, true, true>(kmax, a, s);
+    else dispatch_k<MAT, true, false>(kmax, a, s);
+  } else {
+    if(join) dispatch_k<MAT, false, true>(kmax, a, s);
+    else dispatch_k<MAT, false, false>(kmax, a, s);
+  }
 }
 
 // SMs of device 0 (the grid caps below are per SM)
@@ -403,12 +451,12 @@ int sm_count()
   return n;
 }
 
-template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a, int grid_per_sm)
+template <int KMAX, bool MASK, bool JOIN> KernelCall count_call_k(const WaveArgs &a, int grid_per_sm)
 {
   const size_t smem = sizeof(Smem<KMAX>) * kWarps;
   static bool configured = false;
   if(!configured) {
-    cudaFuncSetAttribute(k_wave<KMAX, false, MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_wave<KMAX, false, MASK, JOIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = true;
   }
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
@@ -416,7 +464,7 @@ template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a, int gr
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
   KernelCall c;
-  c.func = (const void *)k_wave<KMAX, false, MASK>;
+  c.func = (const void *)k_wave<KMAX, false, MASK, JOIN>;
   c.grid = dim3((unsigned)blocks);
   c.block = dim3(kWarps * 32);
   c.smem = (unsigned)smem;
@@ -424,12 +472,12 @@ template <int KMAX, bool MASK> KernelCall count_call_k(const WaveArgs &a, int gr
   return c;
 }
 
-template <bool MASK> KernelCall count_call(int kmax, const WaveArgs &a, int grid_per_sm)
+template <bool MASK, bool JOIN> KernelCall count_call(int kmax, const WaveArgs &a, int grid_per_sm)
 {
-  if(kmax <= 8) return count_call_k<8, MASK>(a, grid_per_sm);
-  if(kmax <= 16) return count_call_k<16, MASK>(a, grid_per_sm);
-  if(kmax <= 32) return count_call_k<32, MASK>(a, grid_per_sm);
-  return count_call_k<64, MASK>(a, grid_per_sm);
+  if(kmax <= 8) return count_call_k<8, MASK, JOIN>(a, grid_per_sm);
+  if(kmax <= 16) return count_call_k<16, MASK, JOIN>(a, grid_per_sm);
+  if(kmax <= 32) return count_call_k<32, MASK, JOIN>(a, grid_per_sm);
+  return count_call_k<64, MASK, JOIN>(a, grid_per_sm);
 }
 
 }  // namespace
@@ -439,11 +487,13 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
                            unsigned long long *rec_n, int32_t grid_per_sm, int32_t cnt_copies,
-                           long long cnt_stride)
+                           long long cnt_stride, bool join)
 {
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
               nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n, cnt_copies, cnt_stride };
-  return small_graphs ? count_call<true>(kmax, a, grid_per_sm) : count_call<false>(kmax, a, grid_per_sm);
+  if(small_graphs)
+    return join ? count_call<true, true>(kmax, a, grid_per_sm) : count_call<true, false>(kmax, a, grid_per_sm);
+  return join ? count_call<false, true>(kmax, a, grid_per_sm) : count_call<false, false>(kmax, a, grid_per_sm);
 }
 
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
@@ -451,12 +501,12 @@ void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long to
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned long long *bytes, unsigned int *err, cudaStream_t s)
+                             unsigned long long *bytes, unsigned int *err, bool join, cudaStream_t s)
 {
   if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, const_cast<uint32_t *>(bm), bmx,
-              nullptr, childmap, cursor, outs, bytes, err, nullptr, 0, nullptr };
-  dispatch<true>(kmax, small_graphs, a, s);
+              nullptr, childmap, cursor, outs, bytes, err, nullptr, 0, nullptr, 0, 0 };
+  dispatch<true>(kmax, small_graphs, join, a, s);
 }
 
 namespace {
@@ -469,7 +519,7 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
                                                      const uint32_t *__restrict__ bm, const int32_t *__restrict__ bmx,
                                                      int32_t *cursor, long long cursor_stride,
                                                      const ChildOut *__restrict__ outs, unsigned long long *bytes,
-                                                     unsigned int *err)
+                                                     unsigned int *err, const ListBuild lb, int32_t *list_cnt)
 {
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -487,6 +537,10 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
         c = childmap[key];
       }
       mine += 20;
+      long long lrow;
+      int lk;
+      // lists strategy: count the record's list row
+      if(list_cnt && list_entry(x, lb, lrow, lk, err)) atomicAdd(&list_cnt[lrow], 1);
     }
     // one cursor per (key, counter copy): copy q of a key starts where the
     // counts of copies 0..q-1 end, so the adds spread over many addresses
@@ -518,13 +572,15 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
 
 void launch_materialize_records(const int4 *rec, long long n, const int32_t *childmap, const long long *keyword,
                                 const uint32_t *bm, const int32_t *bmx, int32_t *cursor, long long cursor_stride,
-                                const ChildOut *outs, unsigned long long *bytes, unsigned int *err, cudaStream_t s)
+                                const ChildOut *outs, unsigned long long *bytes, unsigned int *err,
+                                const ListBuild *lists, int32_t *list_cnt, cudaStream_t s)
 {
   if(n <= 0) return;
   long long blocks = ((n + 31) / 32 * 32 + 255) / 256;
   if(blocks > 152LL * 16) blocks = 152LL * 16;
+  const ListBuild lb = lists ? *lists : ListBuild{ nullptr, nullptr, nullptr };
   k_mat_records<<<(int)blocks, 256, 0, s>>>(rec, n, childmap, keyword, bm, bmx, cursor, cursor_stride, outs, bytes,
-                                            err);
+                                            err, lb, lists ? list_cnt : nullptr);
 }
 
 }  // namespace gsgb

@@ -169,8 +169,17 @@ typedef struct gs_mine_opts {
   int32_t launch_mode; /* a wave's device work (uploads, clears, count, selection, check, results
                           copy): 0 = replayed from a per-variant CUDA graph, 1 = launched directly */
   int32_t count_grid;  /* count-kernel grid cap in blocks per SM; 0 = built-in default (64) */
-  int32_t reserved;
+  int32_t extension;   /* extension strategy: GS_EXTENSION_RMPATH (default) scans the adjacency of
+                          every right-most-path vertex of every embedding; GS_EXTENSION_LISTS is
+                          the reference's lists variant (gspan_cuda_lists, main_gspan_cuda_lists.cpp):
+                          a forward child takes its extensions from the right-most path's older
+                          vertices by joining its parent's frequent forward extensions at the same
+                          parent row (extend_embeddings.cpp:206-330, intersection_fwd_fwd) and
+                          scans only its new right-most vertex.  Same patterns and supports. */
 } gs_mine_opts;
+
+#define GS_EXTENSION_RMPATH 0
+#define GS_EXTENSION_LISTS 1
 
 typedef struct gs_mine_stats {
   int64_t patterns;
@@ -196,6 +205,8 @@ typedef struct gs_mine_stats {
   double host_select_ms;   /* host: candidate decoding and child allocation */
   double host_emit_ms;     /* host: output */
   int64_t min_host_checks; /* candidates whose canonicality was checked on the host */
+  int64_t list_entries;    /* GS_EXTENSION_LISTS: parent-row list entries built */
+  int64_t join_nodes;      /* GS_EXTENSION_LISTS: DFS-tree nodes extended through a join */
 } gs_mine_stats;
 
 GS_API void gs_mine_opts_default(gs_mine_opts *opts);

@@ -290,3 +290,23 @@ def test_convert_live_against_reference_tool(gs, tmp_path):
         subprocess.run([ref, "txt", dirty, ft, a], check=True, stdout=subprocess.DEVNULL)
         gs.convert_database(dirty, "txt", b, ft)
         assert open(a, "rb").read() == open(b, "rb").read(), ft
+
+
+def test_option_structs_match_the_header(gs):
+    # the ctypes mirrors of gs_mine_opts / gs_mine_stats against the header's
+    # field lists, and the extension option's defaults and spellings
+    import ctypes
+    import re
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "gspan_gb300.h")).read()
+    for cname, py in (("gs_mine_opts", gs.MineOpts), ("gs_mine_stats", gs.MineStats)):
+        body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), hdr, re.S).group(1)
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        names = re.findall(r"\b(?:int32_t|int64_t|double)\s+(\w+);", body)
+        assert names == [f for f, _ in py._fields_], cname
+    o = gs.MineOpts()
+    gs.lib().gs_mine_opts_default(ctypes.byref(o))
+    assert o.extension == gs.EXTENSION_RMPATH
+    assert gs._opts(extension="lists").extension == gs.EXTENSION_LISTS
+    assert gs._opts(extension="rmpath").extension == gs.EXTENSION_RMPATH
+    with pytest.raises(ValueError):
+        gs._opts(extension="bogus")
