@@ -1614,6 +1614,9 @@ private:
     const int64_t nsel = (int64_t)hh[kHeadSelected];
     const long long nrec = f.rec ? (long long)hh[kHeadRecords] : -1;
     st_.extensions += (int64_t)hh[kHeadExt];
+    // the count kernel's bytes per extension (bitmap word and counter, and the
+    // record when records are on), counted here rather than in its inner loop
+    st_.count_bytes += (int64_t)hh[kHeadExt] * (8 + (f.rec ? 16 : 0));
     if(nsel > kb) throw Error(ST_ERR_STATE, "candidate selection overflow");
     if(nsel > f.sel_copied) {
       // copies the whole list again (growing the pinned buffer drops its

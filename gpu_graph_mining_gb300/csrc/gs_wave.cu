@@ -83,6 +83,8 @@ struct WaveArgs {
 template <int KMAX> struct Smem {
   unsigned long long mask[32];  // small graphs: the row's graph-local vertex ids as a bit set
   int gb[32];                   // small graphs: first global vertex of the row's graph
+  int lp[32];                   // the row's last column back-link (a backward child's element)
+  unsigned long long bytes;     // the warp's algorithmic bytes (lane 0 adds, once per tile)
   int phi[KMAX][32];        // graph vertex of pattern vertex t for lane l
   int start[KMAX][32];      // scanned position p: adjacency (or parent list) start
   int pre[KMAX + 1][32];    // item prefix over the scanned positions
@@ -119,7 +121,7 @@ k_wave(const WaveArgs a)
   Smem<KMAX> &S = reinterpret_cast<Smem<KMAX> *>(smem_raw)[warp];
   const long long gwarp = (long long)blockIdx.x * kWarps + warp;
   const long long nwarps = (long long)gridDim.x * kWarps;
-  unsigned long long mine = 0;
+  if(lane == 0) S.bytes = 0;
   // count pass with records: the warp's current reserved chunk (warp-uniform);
   // starts "full" so the first batch reserves a chunk
   long long chunk_base = -1;
@@ -190,7 +192,10 @@ k_wave(const WaveArgs a)
         const int2 e = __ldg(&S.col[c][idx]);
         if((unsigned)e.x >= (unsigned)nv) { valid = false; break; }
         S.phi[c][lane] = e.x;
-        if(c == k - 1) last_prev = e.y;
+        if(c == k - 1) {
+          last_prev = e.y;
+          S.lp[lane] = e.y;
+        }
         idx = e.y;
       }
       if(!valid) atomicOr(a.err, 2u);
@@ -231,7 +236,6 @@ k_wave(const WaveArgs a)
         W += c1 - c0;
       }
       S.pre[np][lane] = W;
-      mine += 8ull * k + 4 + 8ull * np + (MASK ? 8 : 0);
     }
     __syncwarp();
     // ---- phase 2: the tile's (row, slot, neighbour) items, 32 at a time
@@ -242,7 +246,12 @@ k_wave(const WaveArgs a)
     }
     const int off = incl - W;
     const int T = __shfl_sync(kFull, incl, 31);
-    if(lane == 0) mine += 8ull * T;  // one packed adjacency entry per item
+    // per valid row: its k column elements, graph rank, scanned offsets and bit
+    // set; per item one packed adjacency entry (or list entry)
+    {
+      const unsigned nvalid = __popc(__ballot_sync(kFull, valid));
+      if(lane == 0) S.bytes += (8ull * k + 4 + 8ull * np + (MASK ? 8 : 0)) * nvalid + 8ull * T;
+    }
     // Items are located and their adjacency entries (and pair indices) loaded
     // one batch ahead: the next batch's loads are in flight while this batch
     // is decided and emitted.
@@ -287,7 +296,6 @@ k_wave(const WaveArgs a)
       const int pr = pr_n;
       if(base + 32 < T) locate(base + 32 + lane);  // warp-uniform condition
       const int g_o = __shfl_sync(kFull, g, o);
-      const int lp_o = __shfl_sync(kFull, last_prev, o);
       int key = -1, w = 0;
       bool bwd = false;
       if(JOIN && has && s < 0) {
@@ -331,13 +339,19 @@ k_wave(const WaveArgs a)
       }
       // ---- emission, warp converged
       if(!MAT) {
-        if(key >= 0) atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
-        const unsigned ext = __ballot_sync(kFull, key >= 0);  // every lane takes part
-        if(lane == 0) mine += 8ull * __popc(ext);
         // one counter add per distinct key of the step, into this warp's copy
-        // of the counters (copies spread a node's hot counters over L2 slices)
+        // of the counters (copies spread a node's hot counters over L2 slices);
+        // one bitmap OR per distinct key unless a lane's graph differs from its
+        // key group leader's (a tile's rows mostly share a graph).  The bytes of
+        // the bitmap word, the counter and the record per extension are added
+        // on the host from the wave's extension total.
         const unsigned peers = __match_any_sync(kFull, key);
-        if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt_copy[key_base + key], __popc(peers));
+        const int leader = __ffs(peers) - 1;
+        const int g_lead = __shfl_sync(kFull, g_o, leader);
+        if(key >= 0 && (lane == leader || g_o != g_lead))
+          atomicOr(&a.bm[bm_base + (long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
+        if(key >= 0 && lane == leader) atomicAdd(&cnt_copy[key_base + key], __popc(peers));
+        const unsigned ext = __ballot_sync(kFull, key >= 0);  // every lane takes part
         if(a.rec && ext) {
           // append this step's extensions to the warp's current chunk of
           // kRecChunk records; a batch that does not fit is split across a
@@ -359,15 +373,14 @@ k_wave(const WaveArgs a)
           }
           if(key >= 0 && dst >= 0 && dst < a.rec_cap) {
             const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
-            a.rec[dst] = bwd ? make_int4((key_base + key) | rec_tag, S.phi[k - 1][o], lp_o, g_o)
+            a.rec[dst] = bwd ? make_int4((key_base + key) | rec_tag, S.phi[k - 1][o], S.lp[o], g_o)
                              : make_int4((key_base + key) | rec_tag, w, i_o, g_o);
           }
-          if(lane == 0) mine += 16ull * cntx;
         }
       } else {
         const int c = key >= 0 ? a.childmap[key_base + key] : -1;
         const unsigned ext = __ballot_sync(kFull, key >= 0), sel = __ballot_sync(kFull, c >= 0);
-        if(lane == 0) mine += 4ull * __popc(ext) + 20ull * __popc(sel);
+        if(lane == 0) S.bytes += 4ull * __popc(ext) + 20ull * __popc(sel);
         const unsigned peers = __match_any_sync(kFull, c);
         const int leader = __ffs(peers) - 1;
         int pos = 0;
@@ -379,7 +392,7 @@ k_wave(const WaveArgs a)
           const ChildOut out = a.outs[c];
           if(pos < out.cap) {
             const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
-            out.col[pos] = bwd ? make_int2(S.phi[k - 1][o], lp_o) : make_int2(w, i_o);
+            out.col[pos] = bwd ? make_int2(S.phi[k - 1][o], S.lp[o]) : make_int2(w, i_o);
             out.gord[pos] = rank;
           } else {
             atomicOr(a.err, 4u);
@@ -396,10 +409,8 @@ k_wave(const WaveArgs a)
       if(dst < a.rec_cap) a.rec[dst] = make_int4(-1, 0, 0, 0);
     }
   }
-  if(a.bytes) {
-    for(int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(kFull, mine, o);
-    if(lane == 0 && mine) atomicAdd(a.bytes, mine);
-  }
+  __syncwarp();
+  if(a.bytes && lane == 0 && S.bytes) atomicAdd(a.bytes, S.bytes);
 }
 
 template <int KMAX, bool MAT, bool MASK, bool JOIN> void launch_k(const WaveArgs &a, cudaStream_t s)
