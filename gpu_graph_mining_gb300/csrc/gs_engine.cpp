@@ -710,7 +710,13 @@ struct WaveCtx {
   }
 };
 
-constexpr int kMaxDbSlots = 256;   // databases one scheduler keeps in its device table before it grows
+constexpr int kMaxDbSlots = 256;
+// Wave contexts in flight (compile-time tunable): while the GPU works through
+// the queued waves, the host completes the oldest and launches new ones.
+#ifndef GS_WAVE_CTX
+#define GS_WAVE_CTX 2
+#endif
+constexpr int kWaveCtx = GS_WAVE_CTX;   // databases one scheduler keeps in its device table before it grows
 
 struct Engine {
   cudaStream_t stream = nullptr;
@@ -725,7 +731,7 @@ struct Engine {
   int64_t pool_limit = 0;
   DBuf<DevDB> d_dbs;
   DBuf<unsigned long long> d_bytes;   // [0] count bytes, [1] materialise bytes, [2] root bytes, [3] flags
-  WaveCtx ctx[2];
+  WaveCtx ctx[kWaveCtx];
   WaveCtx rootc;
   bool ready = false;
 
@@ -990,7 +996,7 @@ class Sched {
 public:
   Sched(Engine &e, const MineOptions &wo, MineStats &st) : E(e), wo_(wo), st_(st)
   {
-    nctx_ = wo_.wave_nodes > 1 ? 2 : 1;
+    nctx_ = wo_.wave_nodes > 1 ? kWaveCtx : 1;
     E.pool.reset_peak();
     CK(cudaMemsetAsync(E.d_bytes.p, 0, sizeof(unsigned long long) * 4, E.stream));
   }
@@ -1043,7 +1049,11 @@ public:
   void step()
   {
     for(int c = 0; c < nctx_; c++)
-      if(!fl_[c].busy) launch(c, nctx_ > 1 && fl_[1 - c].busy);
+      if(!fl_[c].busy) {
+        int idle = 0;
+        for(int d = 0; d < nctx_; d++) idle += fl_[d].busy ? 0 : 1;
+        launch(c, idle);
+      }
     int pick = -1;
     for(int c = 0; c < nctx_; c++)
       if(fl_[c].busy && (pick < 0 || fl_[c].seq < fl_[pick].seq)) pick = c;
@@ -1105,8 +1115,8 @@ private:
   Engine &E;
   const MineOptions &wo_;
   MineStats &st_;
-  int nctx_ = 2;
-  Flight fl_[2];
+  int nctx_ = kWaveCtx;
+  Flight fl_[kWaveCtx];
   uint64_t seq_ = 0;
   std::vector<std::unique_ptr<JobState>> jobs_;
   std::vector<int32_t> order_;   // unfinished jobs, oldest first
@@ -1358,16 +1368,16 @@ private:
   }
 
   // ---- launch one wave into context c: descriptors, count, support, results copy
-  void launch(int c, bool other_busy)
+  void launch(int c, int idle)
   {
     const clk::time_point t_begin = clk::now();
     WaveCtx &X = E.ctx[c];
     Flight &f = fl_[c];
     if(stacked_ == 0) return;
-    // with the other context idle take half of what is queued, so that both
-    // contexts have work and the host's half overlaps the GPU's
+    // with other contexts idle take an equal share of what is queued, so that
+    // every context has work and the host's share overlaps the GPU's
     int64_t limit = std::max(1, wo_.wave_nodes);
-    if(nctx_ > 1 && !other_busy) limit = std::max<int64_t>(1, std::min<int64_t>(limit, (stacked_ + 1) / 2));
+    if(nctx_ > 1 && idle > 1) limit = std::max<int64_t>(1, std::min<int64_t>(limit, (stacked_ + idle - 1) / idle));
     std::vector<PNode> &nodes = f.nodes;
     std::vector<NodeLayout> &lays = f.lays;  // kept between waves: layouts reuse their vectors
     nodes.clear();

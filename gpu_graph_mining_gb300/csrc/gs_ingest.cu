@@ -249,15 +249,35 @@ __global__ void k_label_values(const long long *present, const long long *rank, 
 }
 
 // ---- 4. pair table
+// A label alphabet gives a small table that every thread hits: up to
+// kSmemTab entries each block marks its own copy in shared memory and merges
+// it once; larger tables are marked in place (read before write).
+constexpr long long kSmemTab = 32768;
+
 __global__ void k_pairs_seen(const int32_t *off, long long V, const int32_t *vl, const int32_t *adj_to,
-                             const int32_t *el, int EL, int VL, long long *seen)
+                             const int32_t *el, int EL, int VL, long long *seen, long long tab)
 {
+  extern __shared__ unsigned char flags[];
+  const bool local = tab <= kSmemTab;
+  if(local) {
+    for(long long i = threadIdx.x; i < tab; i += blockDim.x) flags[i] = 0;
+    __syncthreads();
+  }
   for(long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
     const long long a = vl[v];
     for(long long k = off[v]; k < off[v + 1]; k++) {
-      long long *f = seen + (a * EL + el[k]) * VL + vl[adj_to[k]];
-      if(!*f) *f = 1;
+      const long long x = (a * EL + el[k]) * VL + vl[adj_to[k]];
+      if(local) {
+        flags[x] = 1;
+      } else if(!seen[x]) {
+        seen[x] = 1;
+      }
     }
+  }
+  if(local) {
+    __syncthreads();
+    for(long long i = threadIdx.x; i < tab; i += blockDim.x)
+      if(flags[i] && !seen[i]) seen[i] = 1;
   }
 }
 
@@ -514,7 +534,12 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   // 4. pair table (read back: the number of pairs and the largest graph)
   long long *seen = sc.get<long long>(tab), *prank = sc.get<long long>(tab + 1);
   CK(cudaMemsetAsync(seen, 0, sizeof(long long) * tab, s));
-  k_pairs_seen<<<blocks_for(V), kThreads, 0, s>>>(off, V, vl, adj_to, el, EL, VL, seen);
+  {
+    // few blocks when the table is block-local: each merges the whole table once
+    const bool local = tab <= kSmemTab;
+    const unsigned nb = local ? std::min<unsigned>(blocks_for(V), 152u * 4) : blocks_for(V);
+    k_pairs_seen<<<nb, kThreads, local ? (size_t)tab : 0, s>>>(off, V, vl, adj_to, el, EL, VL, seen, tab);
+  }
   scan_exclusive(seen, prank, tab, sc);
   int *d_mx = sc.get<int>(1);
   CK(cudaMemsetAsync(d_mx, 0, sizeof(int), s));
