@@ -21,6 +21,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <map>
 #include <thread>
@@ -563,7 +564,7 @@ struct JobState {
   int32_t db_slot = 0;
   std::vector<PatternRec> pats;
   std::vector<int32_t> roots;
-  std::vector<PNode> stack;    // DFS-tree nodes waiting for a wave (top = back)
+  std::vector<int32_t> stack;  // DFS-tree nodes waiting for a wave (top = back), as node pool ids
   int64_t pending = 0;         // nodes on the stack or in a wave in flight
   int64_t live_bytes = 0;      // embedding-store bytes held by the job's nodes
   int64_t peak_bytes = 0;
@@ -965,7 +966,7 @@ struct Flight {
   bool busy = false;
   bool mat_pending = false;  // the ctx's materialise events still to be read
   uint64_t seq = 0;
-  std::vector<PNode> nodes;
+  std::vector<int32_t> nodes;  // node pool ids
   std::vector<NodeLayout> lays;
   NodeDesc *hn = nullptr;    // in the ctx's pinned descriptor mirror
   const NodeDesc *dn = nullptr;
@@ -1068,7 +1069,10 @@ public:
     JobState *S = job(id);
     if(!S || S->done || S->cancelled) return;
     S->cancelled = true;
-    for(PNode &p : S->stack) drop_node(*S, p);
+    for(int32_t id : S->stack) {
+      drop_node(*S, pn_[id]);
+      pn_free(id);
+    }
     stacked_ -= (int64_t)S->stack.size();
     S->stack.clear();
     if(S->pending == 0) complete(id);
@@ -1116,6 +1120,8 @@ private:
   const MineOptions &wo_;
   MineStats &st_;
   int nctx_ = kWaveCtx;
+  std::deque<PNode> pn_;          // DFS-tree nodes (stacks and waves hold their ids)
+  std::vector<int32_t> pn_free_;
   Flight fl_[kWaveCtx];
   uint64_t seq_ = 0;
   std::vector<std::unique_ptr<JobState>> jobs_;
@@ -1143,6 +1149,30 @@ private:
   {
     if(v) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(v) + ")");
   }
+
+  // DFS-tree node pool: nodes stay in place (a deque keeps references valid
+  // while it grows) and stacks and waves pass their ids around
+  int32_t pn_new()
+  {
+    int32_t id;
+    if(!pn_free_.empty()) {
+      id = pn_free_.back();
+      pn_free_.pop_back();
+    } else {
+      id = (int32_t)pn_.size();
+      pn_.emplace_back();
+    }
+    PNode &p = pn_[id];
+    p.code.assign(nullptr, 0);
+    p.cols.assign(nullptr, 0);
+    p.list_blk = -1;
+    p.list_off = nullptr;
+    p.list_ent = nullptr;
+    p.list_rows = 0;
+    p.join_lo = p.join_key = p.join_hi = 0;
+    return id;
+  }
+  void pn_free(int32_t id) { pn_free_.push_back(id); }
 
   // releases a node's columns and graph ranks
   void drop_node(JobState &S, PNode &p)
@@ -1223,7 +1253,7 @@ private:
 
     const bool extend = S.job.opt.max_edges != 1;
     std::vector<ChildOut> outs;
-    std::vector<PNode> made;
+    std::vector<int32_t> made;
     X.h_childmap.ensure(R);
     for(int32_t i = 0; i < R; i++) X.h_childmap.p[i] = -1;
     // frequent roots of this job (and partition), in the reference's order
@@ -1262,7 +1292,8 @@ private:
         ChildOut o{ c1, c0, gord, 2, (int32_t)s.n };
         X.h_childmap.p[s.key] = (int32_t)outs.size();
         outs.push_back(o);
-        PNode nn;
+        const int32_t nid = pn_new();
+        PNode &nn = pn_[nid];
         nn.job = id;
         nn.pattern = s.pid;
         nn.code.push_back(s.d);
@@ -1274,7 +1305,7 @@ private:
         nn.nrows = s.n;
         nn.support = s.sup;
         S.live_bytes += s.n * (int64_t)(2 * sizeof(int2) + sizeof(int32_t));
-        made.push_back(std::move(nn));
+        made.push_back(nid);
       }
       S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
     }
@@ -1295,7 +1326,7 @@ private:
     CK(cudaEventRecord(X.ev[5], E.stream));
     S.pending += (int64_t)made.size();
     stacked_ += (int64_t)made.size();
-    for(auto it = made.rbegin(); it != made.rend(); ++it) S.stack.push_back(std::move(*it));
+    for(auto it = made.rbegin(); it != made.rend(); ++it) S.stack.push_back(*it);
   }
 
   // Queues a wave's device work: replayed from the context's CUDA graph for
@@ -1378,7 +1409,7 @@ private:
     // every context has work and the host's share overlaps the GPU's
     int64_t limit = std::max(1, wo_.wave_nodes);
     if(nctx_ > 1 && idle > 1) limit = std::max<int64_t>(1, std::min<int64_t>(limit, (stacked_ + idle - 1) / idle));
-    std::vector<PNode> &nodes = f.nodes;
+    std::vector<int32_t> &nodes = f.nodes;
     std::vector<NodeLayout> &lays = f.lays;  // kept between waves: layouts reuse their vectors
     nodes.clear();
     int64_t rows = 0, words = 0, wkeys = 0;
@@ -1387,7 +1418,7 @@ private:
       JobState &S = *jobs_[order_[oi]];
       const Database &db = *S.job.db;
       while(!S.stack.empty() && (int64_t)nodes.size() < limit) {
-        PNode &top = S.stack.back();
+        const PNode &top = pn_[S.stack.back()];
         if(lays.size() <= nodes.size()) lays.emplace_back();
         NodeLayout &L = lays[nodes.size()];
         layout_node(top, db, L);
@@ -1402,7 +1433,7 @@ private:
         rows += top.nrows;
         words += w;
         wkeys += nk;
-        nodes.push_back(std::move(top));
+        nodes.push_back(S.stack.back());
         S.stack.pop_back();
         stacked_--;
       }
@@ -1418,10 +1449,11 @@ private:
     int32_t tot_cols = 0, tot_slots = 0, tot_edges = 0;
     bool any_join = false;
     for(int32_t n = 0; n < W; n++) {
-      tot_cols += (int32_t)nodes[n].cols.size();
+      const PNode &p = pn_[nodes[n]];
+      tot_cols += (int32_t)p.cols.size();
       tot_slots += (int32_t)lays[n].slots.size();
-      tot_edges += (int32_t)nodes[n].code.size();
-      any_join = any_join || nodes[n].list_off != nullptr;
+      tot_edges += (int32_t)p.code.size();
+      any_join = any_join || p.list_off != nullptr;
     }
     size_t off = 0;
     size_t need = 256 * 7 + sizeof(NodeDesc) * W + sizeof(int2 *) * tot_cols + sizeof(SlotDesc) * tot_slots +
@@ -1442,7 +1474,7 @@ private:
     int64_t rb = 0, bb = 0, tb = 0;
     int32_t kb = 0;
     for(int32_t n = 0; n < W; n++) {
-      const PNode &p = nodes[n];
+      const PNode &p = pn_[nodes[n]];
       const NodeLayout &L = lays[n];
       const JobState &S = *jobs_[p.job];
       const Database &db = *S.job.db;
@@ -1615,7 +1647,7 @@ private:
     }
     st_.count_ms += ms_between(X.ev[0], X.ev[1]);
     st_.support_ms += ms_between(X.ev[1], X.ev[2]);
-    std::vector<PNode> &nodes = f.nodes;
+    std::vector<int32_t> &nodes = f.nodes;
     std::vector<NodeLayout> &lays = f.lays;
     const NodeDesc *hn = f.hn;
     const int32_t W = f.W, kb = f.kb;
@@ -1647,7 +1679,7 @@ private:
     for(int64_t i = 0; i < nsel; i++) {
       const int4 e = hsel[i];
       while(n + 1 < W && hn[n + 1].key_base <= e.x) n++;
-      const JobState &S = *jobs_[nodes[n].job];
+      const JobState &S = *jobs_[pn_[nodes[n]].job];
       if(S.cancelled) continue;
       Candidate cd;
       cd.node = n;
@@ -1670,7 +1702,7 @@ private:
       st_.min_host += (int64_t)todo.size();
       E.workers->run((int64_t)todo.size(), [&](int64_t ti, int w) {
         Candidate &cd = cands[todo[ti]];
-        const auto &code = nodes[cd.node].code;
+        const auto &code = pn_[nodes[cd.node]].code;
         DFS buf[kMaxPatternEdges + 1];
         const size_t n = code.size();
         if(n + 1 > (size_t)kMaxPatternEdges) { cd.ok = false; return; }
@@ -1685,7 +1717,7 @@ private:
     std::vector<ChildOut> outs;
     std::vector<int2> pairs;
     // children in node order (a node's children are contiguous, from made_at[n])
-    std::vector<PNode> made;
+    std::vector<int32_t> made;
     std::vector<int32_t> made_at(W + 1, 0);
     // lists strategy: every node with a forward child to materialise keeps
     // per-row lists of its frequent forward extensions (built from this
@@ -1712,7 +1744,7 @@ private:
         while(a1 < acc.size() && cands[acc[a1]].node == n) a1++;
         std::sort(acc.begin() + a0, acc.begin() + a1,
                   [&](int32_t a, int32_t b) { return seq_before(cands[a].dfs, cands[b].dfs); });
-        PNode &p = nodes[n];
+        PNode &p = pn_[nodes[n]];
         JobState &S = *jobs_[p.job];
         const int32_t max_edges = S.job.opt.max_edges;
         for(size_t ai = a0; ai < a1; ai++) {
@@ -1741,7 +1773,7 @@ private:
         for(int32_t n = 0; n < W; n++)
           if(need[n]) {
             list_rb[n] = (int32_t)list_rows;
-            list_rows += nodes[n].nrows;
+            list_rows += pn_[nodes[n]].nrows;
           }
         for(const Candidate &cd : cands)
           if(need[cd.node] && cd.key < lays[cd.node].nfwd) list_n += cd.cnt;
@@ -1768,7 +1800,7 @@ private:
         for(const Mat &m : mats) {
           made_at[m.node + 1]++;
           const Candidate &cd = cands[m.cand];
-          PNode &p = nodes[m.node];
+          PNode &p = pn_[nodes[m.node]];
           JobState &S = *jobs_[p.job];
           const int64_t rowsn = cd.cnt;
           int2 *col = cv.take<int2>(rowsn);
@@ -1776,7 +1808,8 @@ private:
           ChildOut o{ col, nullptr, gord, cd.dfs.is_forward() ? 0 : 1, (int32_t)rowsn };
           pairs.push_back(make_int2(hn[m.node].key_base + cd.key, (int32_t)outs.size()));
           outs.push_back(o);
-          PNode nn;
+          const int32_t nid = pn_new();
+          PNode &nn = pn_[nid];
           nn.job = p.job;
           nn.pattern = m.pid;
           nn.code.reserve(p.code.size() + 1);
@@ -1817,7 +1850,7 @@ private:
           }
           S.live_bytes += rowsn * (int64_t)(sizeof(int2) + sizeof(int32_t));
           S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
-          made.push_back(std::move(nn));
+          made.push_back(nid);
         }
       }
       for(int32_t n = 0; n < W; n++) made_at[n + 1] += made_at[n];
@@ -1864,16 +1897,18 @@ private:
     // the parents are done: drop their column references and graph ranks
     // (stream order keeps the materialise kernel ahead of any reuse)
     std::vector<int32_t> touched;
-    for(auto &p : nodes) {
+    for(int32_t n = W - 1; n >= 0; n--) {
+      JobState &S = *jobs_[pn_[nodes[n]].job];
+      for(int32_t i = made_at[n + 1] - 1; i >= made_at[n]; i--) S.stack.push_back(made[i]);
+      S.pending += made_at[n + 1] - made_at[n];
+      stacked_ += made_at[n + 1] - made_at[n];
+    }
+    for(int32_t id : nodes) {
+      PNode &p = pn_[id];
       JobState &S = *jobs_[p.job];
       drop_node(S, p);
       if(touched.empty() || touched.back() != p.job) touched.push_back(p.job);
-    }
-    for(int32_t n = W - 1; n >= 0; n--) {
-      JobState &S = *jobs_[nodes[n].job];
-      for(int32_t i = made_at[n + 1] - 1; i >= made_at[n]; i--) S.stack.push_back(std::move(made[i]));
-      S.pending += made_at[n + 1] - made_at[n];
-      stacked_ += made_at[n + 1] - made_at[n];
+      pn_free(id);
     }
     nodes.clear();
     f.busy = false;
