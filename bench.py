@@ -226,9 +226,10 @@ def bench_batch(a, g):
     tune_s = time.perf_counter() - t0
     for _ in range(2):
         g.mine_batch(dbs, sups, collect=False, **tuned)
+        g.mine_batch(dbs, sups, collect=False, extension="lists", **tuned)
     clocks = Clocks()
     clocks.start()
-    tb, st_b, td = [], None, []
+    tb, st_b, td, tl = [], None, [], []
     for _ in range(a.steps):
         flush.fill_(1)
         (_, st_b), ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False, **tuned))
@@ -236,8 +237,13 @@ def bench_batch(a, g):
         flush.fill_(1)
         _, ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False))
         td.append(ms)
+        # the lists extension strategy on the same batch and options
+        flush.fill_(1)
+        (_, st_l), ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False, extension="lists", **tuned))
+        tl.append(ms)
     clk = clocks.stop()
     pats = st_b["patterns"]
+    assert st_l["patterns"] == pats, (st_l["patterns"], pats)
 
     def one_at_a_time(**kw):
         tot, n = 0.0, 0
@@ -262,6 +268,9 @@ def bench_batch(a, g):
             "patterns_per_step": pats,
             "autotuned": {"options": tuned, "report": report, "tuning_s": tune_s,
                           "default_options_ms": sum(td) / len(td)},
+            "lists_strategy": {"ms": sum(tl) / len(tl), "patterns_per_s": pats / (sum(tl) / len(tl) / 1000.0),
+                               "count_ms": st_l["count_ms"], "mat_ms": st_l["mat_ms"],
+                               "list_entries": st_l["list_entries"], "join_nodes": st_l["join_nodes"]},
             "one_at_a_time": {"ms": t_solo, "patterns_per_s": pats / (t_solo / 1000.0)},
             "plain_one_at_a_time": {"ms": t_plain, "patterns_per_s": pats / (t_plain / 1000.0)},
             "speedup_vs_one_at_a_time": t_solo / ms, "speedup_vs_plain": t_plain / ms,
