@@ -553,6 +553,17 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
       // lists strategy: count the record's list row
       if(list_cnt && list_entry(x, lb, lrow, lk, err)) atomicAdd(&list_cnt[lrow], 1);
     }
+    // the graph rank's bitmap word and prefix, and the child's outputs, are
+    // loaded before the cursor add so that their latencies overlap
+    uint32_t bword = 0;
+    int bpre = 0;
+    ChildOut out{};
+    if(c >= 0) {
+      const long long wi = keyword[key] + (x.w >> 5);
+      bword = bm[wi];
+      bpre = bmx[wi];
+      out = outs[c];
+    }
     // one cursor per (key, counter copy): copy q of a key starts where the
     // counts of copies 0..q-1 end, so the adds spread over many addresses
     const unsigned peers = __match_any_sync(kFull, c >= 0 ? x.x : -1);
@@ -561,9 +572,7 @@ __global__ void __launch_bounds__(256) k_mat_records(const int4 *__restrict__ re
     if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[cp * cursor_stride + key], __popc(peers));
     pos = __shfl_sync(kFull, pos, leader) + __popc(peers & lanemask_lt());
     if(c >= 0) {
-      const long long wi = keyword[key] + (x.w >> 5);
-      const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (x.w & 31)) - 1u));
-      const ChildOut out = outs[c];
+      const int rank = bpre + __popc(bword & ((1u << (x.w & 31)) - 1u));
       if(pos < out.cap) {
         out.col[pos] = make_int2(x.y, x.z);
         out.gord[pos] = rank;
