@@ -310,3 +310,25 @@ def test_option_structs_match_the_header(gs):
     assert gs._opts(extension="rmpath").extension == gs.EXTENSION_RMPATH
     with pytest.raises(ValueError):
         gs._opts(extension="bogus")
+
+
+def test_drop_in_shim_compiles_against_the_reference(tmp_path):
+    # the C++ drop-in (a gspan_cuda::gspan_cuda subclass and the
+    # get_gspan_cuda_instance factory) compiled with the reference's own
+    # headers and flags (nvcc -x cu), as a maintainer links it into the mains
+    src = os.path.join(REF_TREE, "src")
+    if not os.path.isdir(os.path.join(src, "gspan_cuda")):
+        pytest.skip("reference tree not present")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = ["nvcc", "-x", "cu", "-std=c++17", "-DLOG_INFO", "-DSTLPORT_UNAVAL",
+           "-gencode", "arch=compute_103a,code=sm_103a"]
+    cmd += ["-I" + os.path.join(src, d) for d in ("gspan_cuda", "globals", "cuda_pp", "reduction")]
+    cmd += ["-I" + os.path.join(repo, "include"), "-c",
+            os.path.join(repo, "gpu_graph_mining_gb300", "shim", "gspan_cuda_shim.cpp"),
+            "-o", str(tmp_path / "shim.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    nm = subprocess.run(["nm", "-C", str(tmp_path / "shim.o")], capture_output=True, text=True).stdout
+    assert "get_gspan_cuda_instance()" in nm
+    for sym in ("gs_db_from_arrays_device", "gs_mine", "gs_db_free", "gs_last_error"):
+        assert sym in nm, sym
