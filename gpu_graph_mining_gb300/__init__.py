@@ -104,7 +104,8 @@ class Patterns(ctypes.Structure):
 class ServerOpts(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_int64), ("pool_bytes", ctypes.c_int64),
                 ("max_active", ctypes.c_int32), ("wave_nodes", ctypes.c_int32),
-                ("threads", ctypes.c_int32), ("label_style", ctypes.c_int32)]
+                ("threads", ctypes.c_int32), ("label_style", ctypes.c_int32),
+                ("extension", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class RequestInfo(ctypes.Structure):
@@ -500,13 +501,14 @@ class Server:
     continuous batching by a native server thread."""
 
     def __init__(self, budget_bytes=0, pool_bytes=0, max_active=0, wave_nodes=0, threads=0,
-                 label_style=LABELS_FULL):
+                 label_style=LABELS_FULL, extension=EXTENSION_RMPATH):
         o = ServerOpts()
         lib().gs_server_opts_default(ctypes.byref(o))
         o.budget_bytes, o.pool_bytes = int(budget_bytes), int(pool_bytes)
         if max_active:
             o.max_active = int(max_active)
         o.wave_nodes, o.threads, o.label_style = int(wave_nodes), int(threads), int(label_style)
+        o.extension = _extension(extension)
         h = ctypes.c_void_p()
         _check(lib().gs_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h

@@ -263,6 +263,7 @@ private:
     wo_ = MineOptions();
     if(opt_.wave_nodes > 0) wo_.wave_nodes = opt_.wave_nodes;
     if(opt_.threads > 0) wo_.threads = opt_.threads;
+    wo_.extension = opt_.extension == GS_EXTENSION_LISTS ? 1 : 0;
     sched_.reset(new Scheduler(wo_, opt_.pool_bytes));
     budget_ = opt_.budget_bytes;
     if(budget_ <= 0) {
@@ -467,6 +468,10 @@ gs_status gs_server_create(const gs_server_opts *opts, gs_server **out)
   if(opts) o = *opts;
   if(o.label_style != GS_LABELS_FULL && o.label_style != GS_LABELS_SEQ) {
     gsgb::capi_set_error("unknown label style");
+    return GS_ERR_USAGE;
+  }
+  if(o.extension != GS_EXTENSION_RMPATH && o.extension != GS_EXTENSION_LISTS) {
+    gsgb::capi_set_error("unknown extension strategy");
     return GS_ERR_USAGE;
   }
   gs_server *s = new gs_server();

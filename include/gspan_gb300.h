@@ -264,6 +264,8 @@ typedef struct gs_server_opts {
   int32_t wave_nodes;   /* DFS-tree nodes per launch; 0 = default */
   int32_t threads;      /* host threads for the canonicality check; 0 = all cores */
   int32_t label_style;  /* GS_LABELS_FULL or GS_LABELS_SEQ for the results */
+  int32_t extension;    /* GS_EXTENSION_RMPATH (default) or GS_EXTENSION_LISTS, as in gs_mine_opts */
+  int32_t reserved;
 } gs_server_opts;
 
 enum { GS_REQ_QUEUED = 0, GS_REQ_RUNNING = 1, GS_REQ_DONE = 2, GS_REQ_CANCELLED = 3, GS_REQ_FAILED = 4 };

@@ -298,7 +298,8 @@ def test_option_structs_match_the_header(gs):
     import ctypes
     import re
     hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "gspan_gb300.h")).read()
-    for cname, py in (("gs_mine_opts", gs.MineOpts), ("gs_mine_stats", gs.MineStats)):
+    for cname, py in (("gs_mine_opts", gs.MineOpts), ("gs_mine_stats", gs.MineStats),
+                      ("gs_server_opts", gs.ServerOpts)):
         body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), hdr, re.S).group(1)
         body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
         names = re.findall(r"\b(?:int32_t|int64_t|double)\s+(\w+);", body)

@@ -105,3 +105,29 @@ def test_lists_full_configuration_2(gs):
     got, stats = gs.mine_collect(db, 1000, extension="lists")
     assert got == want and len(got) > 1000
     assert stats["join_nodes"] > 0 and stats["list_entries"] > 0
+
+
+def test_lists_in_the_server(gs):
+    # the lists strategy under continuous batching: requests join and leave
+    # shared waves (one is cancelled while running) and each result is the
+    # default strategy's result for the same request mined alone
+    import time
+    dbs = [gs.Database.generate(4, seed=2000 + i, scale=0.02 + 0.01 * i) for i in range(3)]
+    reqs = [(0, 0.05, 0), (1, 0.02, 5), (2, 0.05, 4), (0, 0.10, 6), (1, 0.05, 0), (2, 0.02, 8)]
+    with gs.Server(max_active=8, extension="lists") as srv:
+        ids = [srv.add_db(d) for d in dbs]
+        rids = []
+        for i, (d, f, me) in enumerate(reqs):
+            rids.append(srv.submit(ids[d], max(2, int(f * len(dbs[d]))), me))
+            if i == 2:
+                c = srv.submit(ids[2], max(2, int(0.01 * len(dbs[2]))))
+                while srv.status(c) is None and srv.stats()["running"] == 0:
+                    time.sleep(0.0005)
+                srv.cancel(c)
+        got = [srv.result(r) for r in rids]
+        _, ic = srv.result(c)
+        assert ic["state"] in (gs.REQ_CANCELLED, gs.REQ_DONE)
+    for (d, f, me), (pats, info) in zip(reqs, got):
+        assert info["state"] == gs.REQ_DONE
+        want, _ = gs.mine_collect(dbs[d], max(2, int(f * len(dbs[d]))), max_edges=me)
+        assert pats == want
