@@ -131,3 +131,24 @@ def test_lists_in_the_server(gs):
         assert info["state"] == gs.REQ_DONE
         want, _ = gs.mine_collect(dbs[d], max(2, int(f * len(dbs[d]))), max_edges=me)
         assert pats == want
+
+
+@pytest.mark.parametrize("opts", [dict(launch_mode=1), dict(min_check=1), dict(wave_rows=4096, wave_words=4096),
+                                  dict(count_grid=16)], ids=["direct", "host-min", "small-waves", "grid16"])
+def test_lists_with_engine_options(gs, opts):
+    # the lists strategy under the engine's other options gives the golden output
+    db = gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt")
+    got, stats = _lines(gs, db, 5, **opts)
+    assert got == read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s5.txt"))
+    assert stats["join_nodes"] > 0
+
+
+def test_lists_root_partition(gs):
+    # root-subtree shares mined with the lists strategy merge into the
+    # single-process output
+    from gpu_graph_mining_gb300.partition import merge_root_partitions
+    db = gs.Database.generate(2, seed=5, scale=0.02)
+    s = 40
+    want, _ = gs.mine_collect(db, s)
+    parts = [gs.mine_collect(db, s, root_part=r, root_parts=3, extension="lists")[0] for r in range(3)]
+    assert merge_root_partitions(parts) == want
