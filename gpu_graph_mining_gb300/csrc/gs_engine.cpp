@@ -714,8 +714,11 @@ struct WaveCtx {
 constexpr int kMaxDbSlots = 256;
 // Wave contexts in flight (compile-time tunable): while the GPU works through
 // the queued waves, the host completes the oldest and launches new ones.
+// Contexts beyond the first two launch only when a full wave of nodes is
+// queued: more waves in flight then keep the GPU fed, while a short queue is
+// still split in two rather than into many small waves.
 #ifndef GS_WAVE_CTX
-#define GS_WAVE_CTX 2
+#define GS_WAVE_CTX 3
 #endif
 constexpr int kWaveCtx = GS_WAVE_CTX;   // databases one scheduler keeps in its device table before it grows
 
@@ -1051,8 +1054,10 @@ public:
   {
     for(int c = 0; c < nctx_; c++)
       if(!fl_[c].busy) {
+        const bool deep = stacked_ >= std::max(1, wo_.wave_nodes);
+        if(c >= 2 && !deep) continue;
         int idle = 0;
-        for(int d = 0; d < nctx_; d++) idle += fl_[d].busy ? 0 : 1;
+        for(int d = 0; d < nctx_; d++) idle += (!fl_[d].busy && (d < 2 || deep)) ? 1 : 0;
         launch(c, idle);
       }
     int pick = -1;
