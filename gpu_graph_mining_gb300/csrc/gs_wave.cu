@@ -166,16 +166,18 @@ k_wave(const WaveArgs a)
     }
     const int s0 = join ? nslot - 1 : 0;
     const int np = nslot - s0 + (join ? 1 : 0);
-    if(lane < nslot) S.slot[lane] = a.slots[nd.slot_off + lane];
+    // the node's tables, strided over the lanes (patterns of up to KMAX = 64
+    // vertices have more columns and slots than a warp has lanes)
+    for(int t = lane; t < nslot; t += 32) S.slot[t] = a.slots[nd.slot_off + t];
     if(join && lane == 0) {
       S.join_lo = nd.join_lo;
       S.join_key = nd.join_key;
       S.join_hi = nd.join_hi;
     }
-    if(lane < k) {
-      S.vtab[lane] = a.vtab[nd.vtab_off + lane];
-      S.col[lane] = a.coltab[nd.col_off + lane];
-      S.clen[lane] = a.collen[nd.col_off + lane];
+    for(int t = lane; t < k; t += 32) {
+      S.vtab[t] = a.vtab[nd.vtab_off + t];
+      S.col[t] = a.coltab[nd.col_off + t];
+      S.clen[t] = a.collen[nd.col_off + t];
     }
     // ---- phase 1: this lane's row
     const int i = (int)((tile - nd.tile_begin) * 32) + lane;
