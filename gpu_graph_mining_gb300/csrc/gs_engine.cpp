@@ -1695,6 +1695,12 @@ private:
       cd.ok = cd.verdict == 1;
       if(cd.key < 0 || cd.key >= hn[n].nkeys) throw Error(ST_ERR_STATE, "selected key outside its node");
       if(!decode_key(lays[n], *S.job.db, cd.key, cd.dfs)) continue;
+      // a frequent pattern beyond what the embedding store and the checkers
+      // take (64 vertices, 127 edges) is refused, never dropped: its
+      // canonical form is frequent too, so the output would need it
+      const size_t pe = pn_[nodes[n]].code.size() + 1;
+      if(pe >= (size_t)kMaxPatternEdges || (cd.dfs.is_forward() && cd.dfs.to + 1 > kMaxPatternVertices))
+        throw Error(ST_ERR_LIMIT, "frequent pattern exceeds 64 vertices or 127 edges; cap max_edges");
       cands.push_back(cd);
     }
     st_.candidates += (int64_t)cands.size();

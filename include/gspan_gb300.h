@@ -214,7 +214,10 @@ GS_API void gs_mine_opts_default(gs_mine_opts *opts);
 /* Mines all frequent connected subgraphs with support >= abs_minsup:
  * replaces set_min_support + set_graph_output + run of gspan_cuda::gspan_cuda
  * (src/gspan_cuda/gspan_cuda.hpp:284-292).  Returns GS_ERR_MINSUP_TOO_LARGE
- * when abs_minsup >= number of graphs and GS_ERR_MINSUP_TOO_SMALL when < 1. */
+ * when abs_minsup >= number of graphs and GS_ERR_MINSUP_TOO_SMALL when < 1.
+ * Patterns have at most 64 vertices and 127 edges: when a frequent pattern
+ * beyond that exists the call returns GS_ERR_LIMIT (cap max_edges), never a
+ * truncated result. */
 GS_API gs_status gs_mine(gs_db *db, int32_t abs_minsup, int32_t max_edges, gs_emit_fn emit, void *user);
 GS_API gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,
                             gs_mine_stats *stats);

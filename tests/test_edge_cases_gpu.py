@@ -83,3 +83,62 @@ def test_graphs_without_edges_and_nothing_frequent(gs, oracle, tmp_path):
     assert want
     empty, _ = _check(gs, oracle, path, 19)
     assert empty == []
+
+
+def _paths(n, count, seed):
+    r = random.Random(seed)
+    graphs = []
+    for gi in range(count):
+        vl = [v % 3 for v in range(n)]
+        edges = [(v, v + 1, 0) for v in range(n - 1)]
+        # a chord of a graph-specific label: not frequent
+        a = r.randrange(n - 2)
+        edges.append((a, a + 2, 5 + gi))
+        graphs.append((vl, edges))
+    return graphs
+
+
+def test_paths_at_the_vertex_limit(gs, oracle, tmp_path):
+    # 64-vertex paths: frequent sub-paths up to 63 edges and 64 vertices, the
+    # largest patterns the miner takes (bit-set membership, 64-column kernels)
+    want, _ = _check(gs, oracle, _write(tmp_path / "p64.txt", _paths(64, 12, 1)), 10)
+    assert max(line.count("(") for line in want) == 63
+
+
+def test_paths_beyond_the_vertex_limit(gs, oracle, tmp_path):
+    # 70-vertex paths (the general membership path): patterns of more than 64
+    # vertices are refused with GS_ERR_LIMIT, never cut short silently; with
+    # max_edges they are mined exactly
+    path = _write(tmp_path / "p70.txt", _paths(70, 12, 2))
+    db = gs.Database.load(path, "txt")
+    with pytest.raises(gs.GSpanError) as e:
+        gs.mine(db, 10)
+    assert e.value.status == 8  # GS_ERR_LIMIT
+    _check(gs, oracle, path, 10, ["--max-edges", "60"])
+
+
+def test_many_labels(gs, oracle, tmp_path):
+    # 3,000 vertex labels and 40 edge labels: large label alphabets and pair
+    # tables, most roots infrequent
+    r = random.Random(21)
+    graphs = []
+    for gi in range(100):
+        n = r.randint(8, 20)
+        vl = [6 + r.randrange(3000) if r.random() < 0.3 else r.randrange(3) for _ in range(n)]
+        edges = [(r.randrange(v), v, 2 + r.randrange(40) if r.random() < 0.2 else r.randrange(2)) for v in range(1, n)]
+        graphs.append((vl, edges))
+    want, _ = _check(gs, oracle, _write(tmp_path / "labels.txt", graphs), 5)
+    assert len(want) > 50 and max(line.count("(") for line in want) >= 3
+
+
+def test_high_degree_stars(gs, oracle, tmp_path):
+    # star graphs of degree 20: rows with hundreds of items, over a million
+    # embeddings, the record buffer outgrown on a fresh engine
+    graphs = []
+    for gi in range(10):
+        n = 21 + gi % 3
+        vl = [0] + [1 + (v % 2 if gi % 2 else 0) for v in range(1, n)]
+        edges = [(0, v, 0) for v in range(1, n)]
+        graphs.append((vl, edges))
+    gs.engine_reset()
+    _check(gs, oracle, _write(tmp_path / "stars.txt", graphs), 8, ["--max-edges", "4"])
