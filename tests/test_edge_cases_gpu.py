@@ -142,3 +142,27 @@ def test_high_degree_stars(gs, oracle, tmp_path):
         graphs.append((vl, edges))
     gs.engine_reset()
     _check(gs, oracle, _write(tmp_path / "stars.txt", graphs), 8, ["--max-edges", "4"])
+
+
+@pytest.mark.parametrize("name", ["fixture_get_test_database.txt", "fixture_get_labeled_test_database.txt",
+                                  "fixture_get_labeled_test_database2.txt"])
+def test_minsup_one(gs, oracle, name):
+    # support 1: every connected subgraph of every graph is frequent
+    import os
+    from conftest import GOLDEN
+    _check(gs, oracle, os.path.join(GOLDEN, name), 1)
+
+
+def test_more_partitions_than_roots(gs):
+    # root shares beyond the number of frequent roots are empty, and the
+    # shares still merge into the single-process output
+    import os
+    from conftest import GOLDEN
+    from gpu_graph_mining_gb300.partition import merge_root_partitions
+    db = gs.Database.load(os.path.join(GOLDEN, "fixture_get_labeled_test_database.txt"), "txt")
+    want, _ = gs.mine_collect(db, 3)
+    roots = sum(1 for code, _ in want if len(code) == 1)
+    n = roots + 5
+    parts = [gs.mine_collect(db, 3, root_part=r, root_parts=n)[0] for r in range(n)]
+    assert sum(1 for p in parts if not p) >= 5
+    assert merge_root_partitions(parts) == want
