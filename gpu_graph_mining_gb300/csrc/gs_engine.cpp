@@ -1110,7 +1110,7 @@ public:
     d2h(bytes, E.d_bytes.p, sizeof(bytes));
     CK(cudaStreamSynchronize(E.stream));
     CK(cudaGetLastError());
-    if(bytes[3]) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(bytes[3]) + ")");
+    check_flags(bytes[3]);
     st_.count_bytes += (int64_t)bytes[0] - seen_bytes_[0];
     st_.mat_bytes += (int64_t)bytes[1] - seen_bytes_[1];
     seen_bytes_[0] = (int64_t)bytes[0];
@@ -1152,6 +1152,7 @@ private:
   unsigned int *err_flag() { return reinterpret_cast<unsigned int *>(E.d_bytes.p + 3); }
   static void check_flags(unsigned long long v)
   {
+    if(v & 8) throw Error(ST_ERR_LIMIT, "a pattern has 2^31 or more embeddings in one wave");
     if(v) throw Error(ST_ERR_STATE, "kernel consistency check failed (flags " + std::to_string(v) + ")");
   }
 
@@ -1698,6 +1699,8 @@ private:
       // a frequent pattern beyond what the embedding store and the checkers
       // take (64 vertices, 127 edges) is refused, never dropped: its
       // canonical form is frequent too, so the output would need it
+      if(cd.cnt < 0 || cd.cnt == INT32_MAX)
+        throw Error(ST_ERR_LIMIT, "a pattern has 2^31 or more embeddings in one wave");
       const size_t pe = pn_[nodes[n]].code.size() + 1;
       if(pe >= (size_t)kMaxPatternEdges || (cd.dfs.is_forward() && cd.dfs.to + 1 > kMaxPatternVertices))
         throw Error(ST_ERR_LIMIT, "frequent pattern exceeds 64 vertices or 127 edges; cap max_edges");

@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
                                                          int total_keys, int32_t *cnt, int cnt_copies,
                                                          long long cnt_stride, int32_t *childmap, int2 *listed,
                                                          unsigned long long *counters,
-                                                         const unsigned int *err, unsigned long long *err_copy,
+                                                         unsigned int *err, unsigned long long *err_copy,
                                                          int32_t *lnode)
 {
   const unsigned full = 0xffffffffu;
@@ -223,9 +223,22 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
     const int key = (int)i;
     int c = 0;
     if(key < total_keys) {
-      // the count pass spread its adds over copies: their total
-      c = cnt[key];
-      for(int q = 1; q < cnt_copies; q++) c += cnt[q * cnt_stride + key];
+      // the count pass spread its adds over copies: their total.  A copy that
+      // wrapped (negative) or a total past 2^31 - 1 is clamped to 2^31 - 1
+      // and flagged (bit 8): the host refuses such a key
+      long long c64 = cnt[key];
+      bool wrap = c64 < 0;
+      for(int q = 1; q < cnt_copies; q++) {
+        const int x = cnt[q * cnt_stride + key];
+        wrap = wrap || x < 0;
+        c64 += x;
+      }
+      if(wrap || c64 > (long long)INT32_MAX) {
+        atomicOr(err, 8u);
+        c = INT32_MAX;
+      } else {
+        c = (int)c64;
+      }
     }
     int n = 0;
     bool cand = false;
@@ -450,7 +463,7 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 
 KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
                             int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
-                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy,
+                            unsigned long long *counters, unsigned int *err, unsigned long long *err_copy,
                             int32_t *lnode)
 {
   KernelCall c;

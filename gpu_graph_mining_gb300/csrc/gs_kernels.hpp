@@ -1,8 +1,9 @@
 // Launchers for the mining kernels (gs_kernels.cu).  All launches go to the
 // given stream; none synchronises.  `err` receives bit flags when a kernel's
 // consistency checks fail (1: graph rank out of range, 2: back-link, vertex or
-// label-pair index out of range, 4: more child rows than counted); the
-// offending access is skipped, never performed.
+// label-pair index out of range, 4: more child rows than counted, 8: a key's
+// embedding count past 2^31 - 1); the offending access is skipped, never
+// performed.
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -111,7 +112,7 @@ void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n
 // lnode (lists strategy, may be null): reset to -1 for every key with extensions
 KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total_keys, int32_t *cnt,
                             int32_t cnt_copies, long long cnt_stride, int32_t *childmap, int2 *listed,
-                            unsigned long long *counters, const unsigned int *err, unsigned long long *err_copy,
+                            unsigned long long *counters, unsigned int *err, unsigned long long *err_copy,
                             int32_t *lnode);
 // lnode (lists strategy, may be null): lnode[key] = the key's node for every
 // frequent forward key
