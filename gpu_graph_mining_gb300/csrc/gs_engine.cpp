@@ -1695,7 +1695,10 @@ private:
       cd.verdict = wo_.min_check == 0 ? e.w : 2;
       cd.ok = cd.verdict == 1;
       if(cd.key < 0 || cd.key >= hn[n].nkeys) throw Error(ST_ERR_STATE, "selected key outside its node");
-      if(!decode_key(lays[n], *S.job.db, cd.key, cd.dfs)) continue;
+      // the kernels emit keys of valid extensions only: one that does not
+      // decode is an inconsistency, not a pattern to skip
+      if(!decode_key(lays[n], *S.job.db, cd.key, cd.dfs))
+        throw Error(ST_ERR_STATE, "selected key does not decode to an extension");
       // a frequent pattern beyond what the embedding store and the checkers
       // take (64 vertices, 127 edges) is refused, never dropped: its
       // canonical form is frequent too, so the output would need it
