@@ -1,0 +1,81 @@
+"""Randomised differential tests against the oracle: seeded random databases
+(trees with extra edges for cycles, 1-6 vertex labels and 1-4 edge labels,
+graphs of 2-24 or 66-90 vertices, supports of 10-50%, with or without an
+edge cap), mined with both extension strategies.  Every case must match the
+oracle line for line."""
+import random
+
+import pytest
+
+from conftest import run_oracle, to_lines
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed):
+    r = random.Random(seed)
+    ng = r.randint(5, 40)
+    vl_n = r.choice([1, 2, 3, 4, 6])
+    el_n = r.choice([1, 2, 3, 4])
+    big = r.random() < 0.15         # graphs beyond 64 vertices: the general membership path
+    dense = r.choice([0.0, 0.1, 0.3, 0.6])
+    graphs = []
+    for _ in range(ng):
+        n = r.randint(66, 90) if big else r.randint(2, 24)
+        vl = [r.randrange(vl_n) for _ in range(n)]
+        edges = {}
+        for v in range(1, n):
+            edges[(r.randrange(v), v)] = r.randrange(el_n)
+        for _ in range(int(dense * n)):
+            a, b = sorted(r.sample(range(n), 2))
+            edges.setdefault((a, b), r.randrange(el_n))
+        graphs.append((vl, [(a, b, l) for (a, b), l in sorted(edges.items())]))
+    minsup = min(ng - 1, max(1, int(ng * r.choice([0.1, 0.2, 0.3, 0.5]))))
+    max_edges = r.choice([3, 4]) if big else r.choice([0, 3, 4, 5, 6])
+    if dense >= 0.3 and max_edges == 0:
+        max_edges = 5
+    return graphs, minsup, max_edges
+
+
+def _write(path, graphs):
+    lines = []
+    for gi, (vl, edges) in enumerate(graphs):
+        lines.append("t # %d" % gi)
+        lines += ["v %d %d" % (v, l) for v, l in enumerate(vl)]
+        lines += ["e %d %d %d" % (a, b, l) for a, b, l in edges]
+    path.write_text("\n".join(lines) + "\n")
+    return str(path)
+
+
+@pytest.mark.parametrize("group", range(8))
+def test_random_databases_vs_oracle(gs, oracle, tmp_path, group):
+    for seed in range(group * 50, group * 50 + 50):
+        graphs, minsup, max_edges = _case(seed)
+        path = _write(tmp_path / ("case%d.txt" % seed), graphs)
+        extra = ["--max-edges", str(max_edges)] if max_edges else []
+        want = run_oracle(oracle, "txt", path, minsup, extra)
+        db = gs.Database.load(path, "txt")
+        for ext in ("rmpath", "lists"):
+            pats, _ = gs.mine(db, minsup, max_edges=max_edges, label_style=gs.LABELS_SEQ, extension=ext)
+            assert to_lines(pats, gs) == want, (seed, ext, minsup, max_edges)
+        db.free()
+
+
+@pytest.mark.parametrize("group", range(4))
+def test_random_batches_vs_oracle(gs, oracle, tmp_path, group):
+    # ten random databases (different label alphabets, graph sizes and
+    # supports) mined together in shared waves, each against the oracle
+    seeds = range(1000 + group * 10, 1000 + group * 10 + 10)
+    cases = [_case(seed) for seed in seeds]
+    # one edge cap per batch: the largest of the cases' caps, 5 where a case has none
+    cap = max(me if me else 5 for _, _, me in cases)
+    dbs, sups, wants = [], [], []
+    for seed, (graphs, minsup, _) in zip(seeds, cases):
+        path = _write(tmp_path / ("batch%d.txt" % seed), graphs)
+        wants.append(run_oracle(oracle, "txt", path, minsup, ["--max-edges", str(cap)]))
+        dbs.append(gs.Database.load(path, "txt"))
+        sups.append(minsup)
+    for ext in ("rmpath", "lists"):
+        got, _ = gs.mine_batch(dbs, sups, max_edges=cap, label_style=gs.LABELS_SEQ, extension=ext)
+        for seed, g, w in zip(seeds, got, wants):
+            assert to_lines(g, gs) == w, (seed, ext)
