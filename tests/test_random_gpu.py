@@ -79,3 +79,28 @@ def test_random_batches_vs_oracle(gs, oracle, tmp_path, group):
         got, _ = gs.mine_batch(dbs, sups, max_edges=cap, label_style=gs.LABELS_SEQ, extension=ext)
         for seed, g, w in zip(seeds, got, wants):
             assert to_lines(g, gs) == w, (seed, ext)
+
+
+def test_random_device_ingest(gs, tmp_path):
+    # random databases through the reference's cudabin arrays and the device
+    # ingest mine exactly as the same databases read from text
+    import numpy as np
+    for seed in range(2000, 2040):
+        graphs, minsup, max_edges = _case(seed)
+        path = _write(tmp_path / ("ing%d.txt" % seed), graphs)
+        host = gs.Database.load(path, "txt")
+        cb = str(tmp_path / ("ing%d.cudabin" % seed))
+        host.write(cb, "cudabin")
+        raw = np.fromfile(cb, dtype=np.int32)
+        n, esz, maxv, vc = (int(x) for x in raw[:4])
+        o = 4
+        edges = raw[o:o + esz]; o += esz
+        elab = raw[o:o + esz]; o += esz
+        vlab = raw[o:o + n * maxv]; o += n * maxv
+        voff = raw[o:o + n * maxv + 1]
+        dev = gs.Database.from_arrays(n, maxv, edges, elab, vlab, voff, vc, device=True)
+        want, _ = gs.mine_collect(host, minsup, max_edges=max_edges)
+        got, _ = gs.mine_collect(dev, minsup, max_edges=max_edges)
+        assert got == want, seed
+        host.free()
+        dev.free()
