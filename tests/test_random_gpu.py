@@ -104,3 +104,53 @@ def test_random_device_ingest(gs, tmp_path):
         assert got == want, seed
         host.free()
         dev.free()
+
+
+def test_concurrent_callers(gs, tmp_path):
+    # host threads calling the library at once: device ingests, mining of
+    # resident and of freshly ingested databases, both strategies, frees;
+    # every result equals the same call made alone
+    import threading
+    import numpy as np
+    cases = [_case(seed) for seed in range(3000, 3008)]
+    paths = [_write(tmp_path / ("cc%d.txt" % i), g) for i, (g, _, _) in enumerate(cases)]
+    dbs = [gs.Database.load(p, "txt") for p in paths]
+    arrays = []
+    for i, db in enumerate(dbs):
+        cb = str(tmp_path / ("cc%d.cudabin" % i))
+        db.write(cb, "cudabin")
+        raw = np.fromfile(cb, dtype=np.int32)
+        n, esz, maxv, vc = (int(x) for x in raw[:4])
+        o = 4
+        parts = []
+        for size in (esz, esz, n * maxv, n * maxv + 1):
+            parts.append(raw[o:o + size].copy())
+            o += size
+        arrays.append((n, maxv, parts, vc))
+    want = [gs.mine_collect(db, s, max_edges=me)[0] for db, (_, s, me) in zip(dbs, cases)]
+    errors = []
+
+    def worker(t):
+        try:
+            for rep in range(3):
+                i = (t + rep) % len(cases)
+                _, s, me = cases[i]
+                ext = "lists" if (t + rep) % 2 else "rmpath"
+                if t % 2:
+                    n, maxv, (e, el, vl, vo), vc = arrays[i]
+                    d = gs.Database.from_arrays(n, maxv, e, el, vl, vo, vc, device=True)
+                    got, _ = gs.mine_collect(d, s, max_edges=me, extension=ext)
+                    d.free()
+                else:
+                    got, _ = gs.mine_collect(dbs[i], s, max_edges=me, extension=ext)
+                if got != want[i]:
+                    errors.append((t, rep, i, ext))
+        except Exception as exc:  # reported below
+            errors.append((t, repr(exc)))
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(6)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert errors == []
