@@ -166,3 +166,19 @@ def test_more_partitions_than_roots(gs):
     parts = [gs.mine_collect(db, 3, root_part=r, root_parts=n)[0] for r in range(n)]
     assert sum(1 for p in parts if not p) >= 5
     assert merge_root_partitions(parts) == want
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_empty_and_degenerate_arrays(gs, device):
+    # no graphs, and graphs of one vertex without edges: both ingest paths
+    # accept them, and mining refuses a support it cannot reach (never a crash)
+    empty = gs.Database.from_arrays(0, 0, [], [], [], [0], 0, device=device)
+    assert len(empty) == 0
+    with pytest.raises(gs.GSpanError) as e:
+        gs.mine(empty, 1)
+    assert e.value.status == 6  # GS_ERR_MINSUP_TOO_LARGE
+    # three graphs of one vertex each (max 1 vertex per graph, no edges)
+    single = gs.Database.from_arrays(3, 1, [], [], [4, 4, 7], [0, 0, 0, 0], 3, device=device)
+    assert len(single) == 3
+    pats, _ = gs.mine(single, 2)
+    assert pats == []
