@@ -458,21 +458,15 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   } drain{ s, cx.s_copy };
   Scratch sc{ s, cx.pool, {} };
   const long long slots = (long long)G * maxv;
-  // raw arrays up (the reference's copy_to_device): the vertex offsets on the
-  // ingest stream, which needs them first; the rest on the copy stream,
-  // overlapping the per-graph pass
+  // raw arrays up (the reference's copy_to_device).  A copy from pageable
+  // memory returns only when it is done, so the vertex offsets go first and
+  // the per-graph pass is queued behind them before the other arrays are
+  // copied (on the copy stream): the GPU runs the pass while the host is in
+  // those copies.
   int32_t *d_edges = sc.get<int32_t>(esz), *d_elab = sc.get<int32_t>(esz);
   int32_t *d_vlab = sc.get<int32_t>(slots), *d_voff = sc.get<int32_t>(slots + 1);
   CK(cudaEventRecord(cx.ev_alloc, s));
   CK(cudaMemcpyAsync(d_voff, voff, sizeof(int32_t) * (slots + 1), cudaMemcpyHostToDevice, s));
-  CK(cudaStreamWaitEvent(cx.s_copy, cx.ev_alloc, 0));
-  if(esz) {
-    CK(cudaMemcpyAsync(d_edges, edges, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
-    CK(cudaMemcpyAsync(d_elab, elab, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
-  }
-  if(slots) CK(cudaMemcpyAsync(d_vlab, vlab, sizeof(int32_t) * slots, cudaMemcpyHostToDevice, cx.s_copy));
-  CK(cudaEventRecord(cx.ev_copied, cx.s_copy));
-  sc.after = cx.ev_copied;
   unsigned *flags = sc.get<unsigned>(1);
   CK(cudaMemsetAsync(flags, 0, sizeof(unsigned), s));
 
@@ -485,6 +479,14 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   CK(cudaMemcpyAsync(&rb.v_total, vbase + G, sizeof(long long), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&rb.e_total, gpos + G, sizeof(long long), cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&rb.flags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamWaitEvent(cx.s_copy, cx.ev_alloc, 0));
+  if(esz) {
+    CK(cudaMemcpyAsync(d_edges, edges, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
+    CK(cudaMemcpyAsync(d_elab, elab, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
+  }
+  if(slots) CK(cudaMemcpyAsync(d_vlab, vlab, sizeof(int32_t) * slots, cudaMemcpyHostToDevice, cx.s_copy));
+  CK(cudaEventRecord(cx.ev_copied, cx.s_copy));
+  sc.after = cx.ev_copied;
   CK(cudaStreamSynchronize(s));
   if(rb.flags & kBadTile) throw Error(ST_ERR_FORMAT, "cudabin: bad vertex offsets");
   const long long V = rb.v_total, E2 = rb.e_total;
