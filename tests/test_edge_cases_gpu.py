@@ -182,3 +182,30 @@ def test_empty_and_degenerate_arrays(gs, device):
     assert len(single) == 3
     pats, _ = gs.mine(single, 2)
     assert pats == []
+
+
+@pytest.mark.parametrize("ft,dbf,minsup,out", [
+    ("txt", "cfg1_seed1.txt", 10, "out_cfg1_seed1_s10.txt"),
+    ("bin", "fixture_labeled.bin", 2, "out_fixture_labeled_s2.txt"),
+    ("txt", "fixture_get_labeled_test_database2.txt", 3, "out_fixture_get_labeled_test_database2_s3.txt"),
+])
+def test_cli_output_is_golden(gs, tmp_path, ft, dbf, minsup, out):
+    # the command-line miner (the reference mains' interface) prints the
+    # golden patterns, in order, to stdout or to a file ("-": count only),
+    # and the reference's count line on stderr
+    import os
+    import subprocess
+    from conftest import GOLDEN, read_lines
+    want = read_lines(os.path.join(GOLDEN, out))
+    cmd = [gs.CLI_PATH, ft, os.path.join(GOLDEN, dbf), str(minsup)]
+    r = subprocess.run(cmd + ["--seq-labels"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.splitlines() == want
+    assert "total_frequent_graphs=%d" % len(want) in r.stderr
+    path = str(tmp_path / "patterns.txt")
+    r = subprocess.run(cmd + [path, "--seq-labels"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout == ""
+    assert read_lines(path) == want
+    r = subprocess.run(cmd + ["-"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout == ""
+    assert "total_frequent_graphs=%d" % len(want) in r.stderr
