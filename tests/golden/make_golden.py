@@ -167,8 +167,35 @@ def convert_runs():
             print("convert", *r)
 
 
+def fsg_molecules(path):
+    """A seeded FSG database with string labels (the format whose reader numbers
+    labels per graph by first appearance, graph_types.cpp:115-170)."""
+    import random
+    r = random.Random(5)
+    labs = ["C", "O", "N", "S", "Cl"]
+    els = ["s", "d", "t"]
+    lines = []
+    for gi in range(30):
+        n = r.randint(4, 14)
+        lines.append("t # %d" % gi)
+        lines += ["v %d %s" % (v, r.choice(labs)) for v in range(n)]
+        seen = set()
+        for v in range(1, n):
+            a = r.randrange(v)
+            seen.add((a, v))
+            lines.append("u %d %d %s" % (a, v, r.choice(els)))
+        for _ in range(n // 4):
+            a, b = sorted(r.sample(range(n), 2))
+            if (a, b) not in seen:
+                seen.add((a, b))
+                lines.append("u %d %d %s" % (a, b, r.choice(els)))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def main():
     build_ref()
+    fsg_molecules(os.path.join(HERE, "fixture_molecules.fsg"))
     with open(os.path.join(HERE, "ismin_kats.tsv"), "w") as f:
         f.write("# expected(1=min)\tcode   from src/globals/tests/dfs_ismin_tests.cpp:48-61\n")
         f.write("\n".join(ismin_kats()) + "\n")
@@ -215,6 +242,8 @@ def main():
             runs.append(("bin", "fixture_" + b, s))
     for s in (68, 34, 17, 10, 5):
         runs.append(("txt", "cfg1_seed1.txt", s))
+    for s in (3, 5, 8):
+        runs.append(("fsg", "fixture_molecules.fsg", s))
     with open(os.path.join(HERE, "golden_runs.tsv"), "w") as idx:
         idx.write("# filetype\tdatabase\tminsup\toutput\treference stderr\n")
         for ft, db, s in runs:
