@@ -154,3 +154,23 @@ def test_concurrent_callers(gs, tmp_path):
     for th in threads:
         th.join()
     assert errors == []
+
+
+def test_random_support_counts(gs):
+    # gs_support_count (the reference's compute_support_remapped_db_multiple_dfs)
+    # on random records against distinct graph ids per key counted with sets:
+    # empty input, one key or one graph, unsorted ids and duplicate records
+    r = random.Random(77)
+    shapes = [(0, 5, 3), (1, 1, 1), (50, 1, 7), (50, 9, 1), (5000, 40, 300), (20000, 700, 5000),
+              (100000, 3, 100000)]
+    for n, n_keys, n_graphs in shapes:
+        keys = [r.randrange(n_keys) for _ in range(n)]
+        gids = [r.randrange(n_graphs) for _ in range(n)]
+        if n > 10:
+            keys += keys[:n // 10]   # duplicate records
+            gids += gids[:n // 10]
+        sets = [set() for _ in range(n_keys)]
+        for k, g in zip(keys, gids):
+            sets[k].add(g)
+        want = [len(x) for x in sets]
+        assert gs.support_count(keys, gids, n_keys, n_graphs) == want, (n, n_keys, n_graphs)
