@@ -3,7 +3,8 @@
 //
 // Graph database in HBM (one per resident database):
 //   adj[E2]      uint64: low 32 bits = neighbour (global vertex id),
-//                high 32 bits = (edge label << 16) | neighbour vertex label
+//                high 32 bits = (edge label << 16) | neighbour vertex label;
+//                with adj_sorted, ascending within each vertex's entries
 //   adj_off[V+1] int32 CSR offsets, vlabel[V] dense vertex labels,
 //   vgraph[V]    graph id of each vertex,
 //   pair_idx[VL*EL*VL]  dense index of (elabel, tolabel) among the pairs that
@@ -36,7 +37,7 @@ struct DevDB {
   int32_t n_graphs;
   int32_t n_vertices;
   int32_t max_graph_vertices;
-  int32_t pad;
+  int32_t adj_sorted;  // 1: each vertex's entries ascend (adj as unsigned 64-bit values)
   const int32_t *root_off;   // [VL+1] first key of each vertex label's (elabel, tolabel) pairs
   const int32_t *pair_code;  // [root_off[VL]] (elabel << 16) | tolabel of each pair
 };

@@ -108,6 +108,12 @@ void Database::upload()
       adj[k] = ((unsigned long long)hi << 32) | w;
     }
   }, 1 << 16);
+  // each vertex's entries in ascending (edge label, neighbour label, neighbour)
+  // order: the entries a right-most-path vertex's forward rule rejects are a
+  // prefix the extension kernels skip
+  parallel_ranges(V, [&](int64_t v0, int64_t v1, int) {
+    for(int64_t v = v0; v < v1; v++) std::sort(adj.begin() + host.aoff[v], adj.begin() + host.aoff[v + 1]);
+  }, 1 << 14);
   std::vector<int32_t> off(V + 1), vg(V + 1, 0), vgb(V + 1, 0), pidx(tab, -1);
   parallel_ranges(V + 1, [&](int64_t b, int64_t e, int) {
     for(int64_t v = b; v < e; v++) off[v] = (int32_t)host.aoff[v];
@@ -129,8 +135,10 @@ void Database::upload()
   parallel_ranges(V, [&](int64_t v0, int64_t v1, int) {
     for(int64_t v = v0; v < v1; v++) {
       const int64_t a = vl_dense[v];
-      for(int64_t k = host.aoff[v]; k < host.aoff[v + 1]; k++)
-        ap[k] = pidx[(size_t)((a * EL + el_dense[k]) * VL + vl_dense[host.adj_to[k]])];
+      for(int64_t k = host.aoff[v]; k < host.aoff[v + 1]; k++) {
+        const int64_t hi = (int64_t)(adj[k] >> 32);
+        ap[k] = pidx[(size_t)((a * EL + (hi >> 16)) * VL + (hi & 0xffff))];
+      }
     }
   });
   std::vector<int32_t> vb(host.n_graphs + 1);
@@ -165,6 +173,7 @@ void Database::upload()
   dev.vbase = (const int32_t *)(b + o_vb);
   dev.adj_pair = (const int32_t *)(b + o_ap);
   dev.max_graph_vertices = maxnv;
+  dev.adj_sorted = 1;
   dev.VL = VL;
   dev.EL = EL;
   dev.n_graphs = host.n_graphs;
@@ -182,7 +191,7 @@ void Database::ensure_host()
   const int32_t G = host.n_graphs;
   std::vector<unsigned long long> adj(E2 + 1);
   std::vector<int32_t> off(V + 1), vl(V + 1), vb(G + 1);
-  CK(cudaMemcpy(adj.data(), dev.adj, sizeof(unsigned long long) * E2, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(adj.data(), adj_in ? adj_in : dev.adj, sizeof(unsigned long long) * E2, cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(off.data(), dev.adj_off, sizeof(int32_t) * (V + 1), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(vl.data(), dev.vlabel, sizeof(int32_t) * V, cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(vb.data(), dev.vbase, sizeof(int32_t) * (G + 1), cudaMemcpyDeviceToHost));
@@ -205,6 +214,7 @@ void Database::release()
     else cudaFree(d_block);
   }
   d_block = nullptr;
+  adj_in = nullptr;
   pooled = false;
   resident = false;
 }

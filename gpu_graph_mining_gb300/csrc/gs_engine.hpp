@@ -61,6 +61,8 @@ struct Database {
   bool device_only = false;
   bool pooled = false;   // d_block is from the ingest's pool (ingest_free_block)
   int64_t dev_vertices = 0, dev_adj = 0;
+  // device-built: the packed entries in input order (dev.adj may be sorted)
+  const unsigned long long *adj_in = nullptr;
 
   void prepare();   // label compaction and pair tables (host only)
   void upload();    // device copy (idempotent)

@@ -299,18 +299,48 @@ __global__ void k_pairs_index(const long long *seen, const long long *rank, int 
   }
 }
 
-// ---- 5. packed entries
+// ---- 5. packed entries: adj_in in input order (for downloads), adj with each
+// vertex's entries ascending when sort (insertion sort by the vertex's
+// thread: the caller sorts only when no vertex has more than kSortDegree
+// entries), and the pair index of every adj entry
+constexpr int kSortDegree = 1024;
+
 __global__ void k_pack(const int32_t *off, long long V, const int32_t *vl, const int32_t *adj_to, const int32_t *el,
-                       const int32_t *pair_idx, int EL, int VL, unsigned long long *adj, int32_t *adj_pair)
+                       const int32_t *pair_idx, int EL, int VL, bool sort, unsigned long long *adj_in,
+                       unsigned long long *adj, int32_t *adj_pair)
 {
   for(long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
-    const long long a = vl[v];
-    for(long long k = off[v]; k < off[v + 1]; k++) {
+    const long long a = vl[v], a0 = off[v], a1 = off[v + 1];
+    for(long long k = a0; k < a1; k++) {
       const uint32_t w = (uint32_t)adj_to[k];
       const uint32_t hi = ((uint32_t)el[k] << 16) | (uint32_t)vl[w];
-      adj[k] = ((unsigned long long)hi << 32) | w;
-      adj_pair[k] = pair_idx[(a * EL + el[k]) * VL + vl[w]];
+      const unsigned long long x = ((unsigned long long)hi << 32) | w;
+      adj_in[k] = x;
+      long long j = k;
+      if(sort)
+        for(; j > a0 && adj[j - 1] > x; --j) adj[j] = adj[j - 1];
+      adj[j] = x;
     }
+    for(long long k = a0; k < a1; k++) {
+      const unsigned long long x = adj[k];
+      adj_pair[k] = pair_idx[(a * EL + (long long)(x >> 48)) * VL + (long long)((x >> 32) & 0xffffu)];
+    }
+  }
+}
+
+// the largest vertex degree
+__global__ void k_max_degree(const int32_t *off, long long V, int *mx)
+{
+  __shared__ int shi[kThreads / 32];
+  int hi = 0;
+  for(long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    hi = max(hi, off[v + 1] - off[v]);
+  for(int o = 16; o > 0; o >>= 1) hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  if((threadIdx.x & 31) == 0) shi[threadIdx.x >> 5] = hi;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    for(int k = 1; k < kThreads / 32; k++) hi = max(hi, shi[k]);
+    atomicMax(mx, hi);
   }
 }
 
@@ -345,7 +375,7 @@ struct ReadBack {
   int minmax[4];        // vertex labels min, max; edge labels min, max
   long long label_cnt[2];
   long long nkeys;
-  int max_vertices, pad2;
+  int max_vertices, max_degree;
 };
 
 // Process-wide ingest state: the ingest stream and a copy stream, the
@@ -543,14 +573,16 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     k_pairs_seen<<<nb, kThreads, local ? (size_t)tab : 0, s>>>(off, V, vl, adj_to, el, EL, VL, seen, tab);
   }
   scan_exclusive(seen, prank, tab, sc);
-  int *d_mx = sc.get<int>(1);
-  CK(cudaMemsetAsync(d_mx, 0, sizeof(int), s));
+  int *d_mx = sc.get<int>(2);
+  CK(cudaMemsetAsync(d_mx, 0, 2 * sizeof(int), s));
   k_max_ll<<<blocks_for(G), kThreads, 0, s>>>(gnv, G, d_mx);
+  if(V) k_max_degree<<<blocks_for(V), kThreads, 0, s>>>(off, V, d_mx + 1);
   CK(cudaMemcpyAsync(&rb.nkeys, prank + tab, sizeof(long long), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&rb.max_vertices, d_mx, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&rb.max_vertices, d_mx, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const long long nkeys = rb.nkeys;
   const int mxv = rb.max_vertices;
+  const bool sort_adj = rb.max_degree <= kSortDegree;
 
   // the database block, laid out as Database::upload lays it out
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -564,7 +596,8 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   const size_t o_vb = o_ro + al(sizeof(int32_t) * (VL + 1));
   const size_t o_ap = o_vb + al(sizeof(int32_t) * (G + 1));
   const size_t o_pc = o_ap + al(sizeof(int32_t) * (E2 + 1));
-  const size_t total = o_pc + al(sizeof(int32_t) * (nkeys + 1));
+  const size_t o_in = o_pc + al(sizeof(int32_t) * (nkeys + 1));
+  const size_t total = o_in + al(sizeof(unsigned long long) * (E2 + 1));
   char *b = nullptr;
   if(cudaMallocFromPoolAsync((void **)&b, total, cx.pool, s) != cudaSuccess) {
     cudaGetLastError();
@@ -578,7 +611,8 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
       CK(cudaMemcpyAsync(ro + VL, &nk, sizeof(int32_t), cudaMemcpyHostToDevice, s));
     }
     // 5. packed entries and the rest of the block
-    k_pack<<<blocks_for(V), kThreads, 0, s>>>(off, V, vl, adj_to, el, pidx, EL, VL, (unsigned long long *)(b + o_adj),
+    k_pack<<<blocks_for(V), kThreads, 0, s>>>(off, V, vl, adj_to, el, pidx, EL, VL, sort_adj,
+                                              (unsigned long long *)(b + o_in), (unsigned long long *)(b + o_adj),
                                               (int32_t *)(b + o_ap));
     CK(cudaMemcpyAsync(b + o_off, off, sizeof(int32_t) * (V + 1), cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(b + o_vl, vl, sizeof(int32_t) * V, cudaMemcpyDeviceToDevice, s));
@@ -632,6 +666,8 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
     db.dev.vbase = (const int32_t *)(b + o_vb);
     db.dev.adj_pair = (const int32_t *)(b + o_ap);
     db.dev.max_graph_vertices = mxv;
+    db.dev.adj_sorted = sort_adj ? 1 : 0;
+    db.adj_in = (const unsigned long long *)(b + o_in);
     db.dev.VL = VL;
     db.dev.EL = EL;
     db.dev.n_graphs = G;

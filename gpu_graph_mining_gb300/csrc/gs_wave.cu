@@ -223,9 +223,24 @@ k_wave(const WaveArgs a)
       valid = false;
     }
     if(valid) {
+      const bool sorted = dbr.adj_sorted != 0;
       for(int s = s0; s < nslot; ++s) {
         const int v = S.phi[S.slot[s].vertex][lane];
-        const int a0 = __ldg(&adj_off[v]), a1 = __ldg(&adj_off[v + 1]);
+        int a0 = __ldg(&adj_off[v]);
+        const int a1 = __ldg(&adj_off[v + 1]);
+        const int fr = S.slot[s].frule;
+        if(sorted && fr != INT32_MIN) {
+          // a vertex of the right-most path below its end extends forward
+          // only by entries at or above its rule; in an ascending list the
+          // rest is a prefix, found by bisection and not scanned
+          int lo = a0, hi = a1;
+          while(lo < hi) {
+            const int mid = (int)(((unsigned)lo + (unsigned)hi) >> 1);
+            if((int)(__ldg(&adj[mid]) >> 32) < fr) lo = mid + 1;
+            else hi = mid;
+          }
+          a0 = lo;
+        }
         S.start[s - s0][lane] = a0;
         S.pre[s - s0][lane] = W;
         W += a1 - a0;

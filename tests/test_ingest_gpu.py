@@ -113,3 +113,37 @@ def test_device_ingest_repeated_pooled(gs, tmp_path):
     for i, d in live.items():
         assert gs.mine_collect(d, max(2, int(0.05 * arrs[i][0])))[0] == want[i]
         d.free()
+
+
+@pytest.mark.parametrize("hub", [1000, 1100])
+def test_device_ingest_hub_degrees(gs, oracle, tmp_path, hub):
+    # a hub vertex with 1000 entries (the device ingest sorts every vertex's
+    # entries) or 1100 (beyond its per-thread sort bound: the entries stay in
+    # input order and the extension kernels scan every entry): the same
+    # patterns as the oracle and the host-built database, the same arrays
+    # written back
+    import random
+    from conftest import run_oracle, to_lines
+    r = random.Random(hub)
+    lines = []
+    for gi in range(6):
+        n = hub + 1 + gi
+        lines.append("t # %d" % gi)
+        lines += ["v %d %d" % (v, r.randrange(3) if v else 0) for v in range(n)]
+        edges = [(0, v, r.randrange(2)) for v in range(1, n)]
+        edges += [(v, v + 1, 0) for v in range(1, n - 1, 7)]
+        lines += ["e %d %d %d" % e for e in edges]
+    path = tmp_path / "hub.txt"
+    path.write_text("\n".join(lines) + "\n")
+    db = gs.Database.load(str(path), "txt")
+    n, maxv, edges, elab, vlab, voff, vc = _cudabin(db, tmp_path)
+    d = gs.Database.from_arrays(n, maxv, edges, elab, vlab, voff, vc, device=True)
+    want = run_oracle(oracle, "txt", str(path), 4, ["--max-edges", "2"])
+    assert len(want) > 5
+    for x in (db, d):
+        pats, _ = gs.mine(x, 4, max_edges=2, label_style=gs.LABELS_SEQ)
+        assert to_lines(pats, gs) == want
+    ph, pd = str(tmp_path / "h.txt"), str(tmp_path / "d.txt")
+    db.write(ph, "txt")
+    d.write(pd, "txt")
+    assert open(ph).read() == open(pd).read()
