@@ -72,18 +72,22 @@ void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uin
 // sized for 8/16/32/64 pattern vertices); collen[] parallels coltab[]: the
 // length of every column.
 // small_graphs: every graph of the wave's databases has <= 64 vertices.
+// rule_skip: in databases with sorted adjacency (DevDB::adj_sorted), a
+// right-most-path vertex's entries below its forward rule are bisected past
+// instead of scanned.
 KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                            bool small_graphs, const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
                            unsigned long long *rec_n, int32_t grid_per_sm, int32_t cnt_copies,
-                           long long cnt_stride, bool join);
+                           long long cnt_stride, bool join, bool rule_skip);
 void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long total_tiles, int32_t kmax,
                              bool small_graphs,
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned long long *bytes, unsigned int *err, bool join, cudaStream_t s);
+                             unsigned long long *bytes, unsigned int *err, bool join, bool rule_skip,
+                             cudaStream_t s);
 
 // Materialise from the count pass's records {wave key, x, y, graph rank}:
 // children whose key is selected get column element (x, y) and their graph

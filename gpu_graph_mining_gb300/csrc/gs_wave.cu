@@ -78,6 +78,7 @@ struct WaveArgs {
   // apart; warp w adds into copy w % cnt_copies (summed by the screening pass)
   int cnt_copies;
   long long cnt_stride;
+  int rule_skip;  // bisect past forward-rule prefixes of sorted adjacency lists
 };
 
 template <int KMAX> struct Smem {
@@ -223,7 +224,7 @@ k_wave(const WaveArgs a)
       valid = false;
     }
     if(valid) {
-      const bool sorted = dbr.adj_sorted != 0;
+      const bool sorted = a.rule_skip && dbr.adj_sorted != 0;
       for(int s = s0; s < nslot; ++s) {
         const int v = S.phi[S.slot[s].vertex][lane];
         int a0 = __ldg(&adj_off[v]);
@@ -515,10 +516,11 @@ KernelCall wave_count_call(const NodeDesc *nodes, int32_t nnodes, long long tota
                            const int32_t *vtab, const DevDB *dbs, uint32_t *bm, int32_t *cnt,
                            unsigned long long *bytes, unsigned int *err, int4 *rec, long long rec_cap,
                            unsigned long long *rec_n, int32_t grid_per_sm, int32_t cnt_copies,
-                           long long cnt_stride, bool join)
+                           long long cnt_stride, bool join, bool rule_skip)
 {
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, bm, nullptr, cnt,
-              nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n, cnt_copies, cnt_stride };
+              nullptr, nullptr, nullptr, bytes, err, rec, rec_cap, rec_n, cnt_copies, cnt_stride,
+              rule_skip ? 1 : 0 };
   if(small_graphs)
     return join ? count_call<true, true>(kmax, a, grid_per_sm) : count_call<true, false>(kmax, a, grid_per_sm);
   return join ? count_call<false, true>(kmax, a, grid_per_sm) : count_call<false, false>(kmax, a, grid_per_sm);
@@ -529,11 +531,12 @@ void launch_wave_materialize(const NodeDesc *nodes, int32_t nnodes, long long to
                              const int2 *const *coltab, const int32_t *collen, const SlotDesc *slots,
                              const int32_t *vtab, const DevDB *dbs, const uint32_t *bm, const int32_t *bmx,
                              const int32_t *childmap, int32_t *cursor, const ChildOut *outs,
-                             unsigned long long *bytes, unsigned int *err, bool join, cudaStream_t s)
+                             unsigned long long *bytes, unsigned int *err, bool join, bool rule_skip,
+                             cudaStream_t s)
 {
   if(total_tiles <= 0) return;
   WaveArgs a{ nodes, nnodes, total_tiles, coltab, collen, slots, vtab, dbs, const_cast<uint32_t *>(bm), bmx,
-              nullptr, childmap, cursor, outs, bytes, err, nullptr, 0, nullptr, 0, 0 };
+              nullptr, childmap, cursor, outs, bytes, err, nullptr, 0, nullptr, 0, 0, rule_skip ? 1 : 0 };
   dispatch<true>(kmax, small_graphs, join, a, s);
 }
 
