@@ -300,9 +300,10 @@ __global__ void k_pairs_index(const long long *seen, const long long *rank, int 
 }
 
 // ---- 5. packed entries: adj_in in input order (for downloads), adj with each
-// vertex's entries ascending when sort (insertion sort by the vertex's
-// thread: the caller sorts only when no vertex has more than kSortDegree
-// entries), and the pair index of every adj entry
+// vertex's entries ascending when sort (by the vertex's thread: a sorting
+// network in registers up to 8 entries, else an insertion sort in place; the
+// caller sorts only when no vertex has more than kSortDegree entries), and
+// the pair index of every adj entry
 constexpr int kSortDegree = 1024;
 
 __global__ void k_pack(const int32_t *off, long long V, const int32_t *vl, const int32_t *adj_to, const int32_t *el,
@@ -311,20 +312,47 @@ __global__ void k_pack(const int32_t *off, long long V, const int32_t *vl, const
 {
   for(long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x) {
     const long long a = vl[v], a0 = off[v], a1 = off[v + 1];
-    for(long long k = a0; k < a1; k++) {
+    auto entry = [&](long long k) {
       const uint32_t w = (uint32_t)adj_to[k];
       const uint32_t hi = ((uint32_t)el[k] << 16) | (uint32_t)vl[w];
-      const unsigned long long x = ((unsigned long long)hi << 32) | w;
+      return ((unsigned long long)hi << 32) | w;
+    };
+    auto emit = [&](long long k, unsigned long long x) {
+      adj[k] = x;
+      adj_pair[k] = pair_idx[(a * EL + (long long)(x >> 48)) * VL + (long long)((x >> 32) & 0xffffu)];
+    };
+    if(sort && a1 - a0 <= 8) {
+      // up to 8 entries: held in registers (padded with the largest value)
+      // and ordered by Batcher's odd-even merge network (19 comparators)
+      unsigned long long r[8];
+#pragma unroll
+      for(int t = 0; t < 8; t++) {
+        r[t] = a0 + t < a1 ? entry(a0 + t) : ~0ull;
+        if(a0 + t < a1) adj_in[a0 + t] = r[t];
+      }
+      constexpr int net[19][2] = { { 0, 1 }, { 2, 3 }, { 4, 5 }, { 6, 7 }, { 0, 2 }, { 1, 3 }, { 4, 6 },
+                                   { 5, 7 }, { 1, 2 }, { 5, 6 }, { 0, 4 }, { 1, 5 }, { 2, 6 }, { 3, 7 },
+                                   { 2, 4 }, { 3, 5 }, { 1, 2 }, { 3, 4 }, { 5, 6 } };
+#pragma unroll
+      for(int c = 0; c < 19; c++) {
+        const unsigned long long x = r[net[c][0]], y = r[net[c][1]];
+        r[net[c][0]] = x < y ? x : y;
+        r[net[c][1]] = x < y ? y : x;
+      }
+#pragma unroll
+      for(int t = 0; t < 8; t++)
+        if(a0 + t < a1) emit(a0 + t, r[t]);
+      continue;
+    }
+    for(long long k = a0; k < a1; k++) {
+      const unsigned long long x = entry(k);
       adj_in[k] = x;
       long long j = k;
       if(sort)
         for(; j > a0 && adj[j - 1] > x; --j) adj[j] = adj[j - 1];
       adj[j] = x;
     }
-    for(long long k = a0; k < a1; k++) {
-      const unsigned long long x = adj[k];
-      adj_pair[k] = pair_idx[(a * EL + (long long)(x >> 48)) * VL + (long long)((x >> 32) & 0xffffu)];
-    }
+    for(long long k = a0; k < a1; k++) emit(k, adj[k]);
   }
 }
 
