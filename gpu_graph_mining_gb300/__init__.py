@@ -32,6 +32,7 @@ EXPORTS = [
     "gs_db_generate", "gs_db_convert",
     "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
     "gs_mine", "gs_mine_ex", "gs_mine_collect", "gs_patterns_free", "gs_mine_batch", "gs_support_count",
+    "gs_filter_backward",
     "gs_support_count_noalloc",
     "gs_dfs_code_is_min", "gs_engine_reset", "gs_engine_set_pool_bytes",
     "gs_server_opts_default", "gs_server_create", "gs_server_add_db", "gs_server_submit", "gs_server_poll",
@@ -183,6 +184,8 @@ def lib():
     L.gs_mine_batch.restype = i32
     L.gs_support_count.argtypes = [pi32, pi32, i64, i32, i32, pi32]
     L.gs_support_count.restype = i32
+    L.gs_filter_backward.argtypes = [pi32, i64, pi32, i64, pi32, pi32, ctypes.POINTER(i64)]
+    L.gs_filter_backward.restype = i32
     L.gs_support_count_noalloc.argtypes = [vp, vp, i64, i32, i32, vp, vp]
     L.gs_support_count_noalloc.restype = i32
     L.gs_dfs_code_is_min.argtypes = [pi32, i32]
@@ -441,6 +444,27 @@ def support_count(keys, graph_ids, n_keys, n_graphs):
     out = (ctypes.c_int32 * max(1, n_keys))()
     _check(lib().gs_support_count(k, g, n, int(n_keys), int(n_graphs), out))
     return list(out)[:n_keys]
+
+
+def filter_backward(column, records, dfs):
+    """Backward child column (GPU): the (vertex, back_link) elements of
+    column at the rows named by the extension records (8-tuples {from, to,
+    fromlabel, elabel, tolabel, from_grph, to_grph, row}) equal to the
+    backward edge dfs, in row order (the reference's
+    filter_backward_embeddings)."""
+    n = len(column)
+    col = (ctypes.c_int32 * max(2, 2 * n))(*[int(x) for e in column for x in e])
+    flat = [int(x) for r in records for x in r]
+    if any(len(r) != 8 for r in records):
+        raise ValueError("a record has 8 fields")
+    rec = (ctypes.c_int32 * max(8, len(flat)))(*flat)
+    if len(dfs) != 5:
+        raise ValueError("a DFS edge has 5 fields")
+    d = (ctypes.c_int32 * 5)(*[int(x) for x in dfs])
+    out = (ctypes.c_int32 * max(2, 2 * n))()
+    n_out = ctypes.c_int64(0)
+    _check(lib().gs_filter_backward(col, n, rec, len(records), d, out, ctypes.byref(n_out)))
+    return [(out[2 * i], out[2 * i + 1]) for i in range(n_out.value)]
 
 
 def dfs_code_is_min(code):

@@ -386,6 +386,15 @@ gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids, int64_
   return GS_OK;
 }
 
+gs_status gs_filter_backward(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
+                             const int32_t *dfs, int32_t *out, int64_t *n_out)
+{
+  std::string err;
+  int rc = gsgb::filter_backward_host(column, n_rows, records, n_records, dfs, out, n_out, err);
+  if(rc != 0) return set_err(rc, err);
+  return GS_OK;
+}
+
 int32_t gs_dfs_code_is_min(const int32_t *d, int32_t n)
 {
   if(!d || n < 1 || n > gsgb::kMaxPatternEdges) return -1;

@@ -2231,6 +2231,70 @@ int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int3
   return rc;
 }
 
+int filter_backward_host(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
+                         const int32_t *dfs, int32_t *out, int64_t *n_out, std::string &err)
+{
+  if(n_rows < 0 || n_records < 0 || !dfs || !n_out || (n_rows > 0 && (!column || !out)) ||
+     (n_records > 0 && !records)) {
+    err = "invalid arguments";
+    return ST_ERR_USAGE;
+  }
+  // the reference aborts on a forward edge (DFS::is_forward: from < to)
+  if(dfs[0] <= dfs[1]) {
+    err = "the edge to filter by is not backward (from > to)";
+    return ST_ERR_USAGE;
+  }
+  if(n_rows >= (int64_t)INT32_MAX) {
+    err = "more than 2^31 - 2 rows";
+    return ST_ERR_LIMIT;
+  }
+  for(int64_t i = 0; i < n_records; i++) {
+    const int32_t *x = records + 8 * i;
+    if(x[0] == dfs[0] && x[1] == dfs[1] && x[2] == dfs[2] && x[3] == dfs[3] && x[4] == dfs[4] &&
+       (x[7] < 0 || x[7] >= n_rows)) {
+      err = "record " + std::to_string(i) + " names a row outside the column";
+      return ST_ERR_USAGE;
+    }
+  }
+  *n_out = 0;
+  if(n_rows == 0) return ST_OK;
+  std::lock_guard<std::mutex> g(g_mu);
+  char *blk = nullptr;
+  cudaStream_t s = nullptr;
+  int rc = ST_OK;
+  try {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_col = 0, o_rec = o_col + al(8 * (size_t)n_rows);
+    const size_t o_pos = o_rec + al(32 * (size_t)std::max<int64_t>(n_records, 1));
+    const size_t o_scr = o_pos + al(4 * (size_t)(n_rows + 1));
+    const size_t o_out = o_scr + al(4 * (size_t)std::max<int64_t>(filter_backward_scratch(n_rows), 1));
+    const size_t total = o_out + al(8 * (size_t)n_rows);
+    CK(cudaSetDevice(0));
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaMalloc(&blk, total));
+    CK(cudaMemcpyAsync(blk + o_col, column, 8 * (size_t)n_rows, cudaMemcpyHostToDevice, s));
+    if(n_records > 0) CK(cudaMemcpyAsync(blk + o_rec, records, 32 * (size_t)n_records, cudaMemcpyHostToDevice, s));
+    int32_t *pos = (int32_t *)(blk + o_pos);
+    CK(cudaMemsetAsync(pos, 0, 4 * (size_t)(n_rows + 1), s));
+    launch_filter_backward((const int2 *)(blk + o_col), n_rows, (const int32_t *)(blk + o_rec), n_records, dfs, pos,
+                           (int32_t *)(blk + o_scr), (int2 *)(blk + o_out), s);
+    int32_t cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, pos + n_rows, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if(cnt > 0) CK(cudaMemcpyAsync(out, blk + o_out, 8 * (size_t)cnt, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    *n_out = cnt;
+  } catch(const Error &e) {
+    err = e.what();
+    rc = e.code;
+  }
+  if(s) cudaStreamSynchronize(s);
+  if(blk) cudaFree(blk);
+  if(s) cudaStreamDestroy(s);
+  return rc;
+}
+
 void engine_reset()
 {
   {

@@ -193,6 +193,12 @@ private:
 int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int32_t n_keys, int32_t n_graphs,
                        int32_t *support, std::string &err);
 
+// Backward child column: out = the elements ({vertex, back_link}) of column at
+// the rows named by the records (8 ints each) equal to the backward edge dfs,
+// in row order; *n_out their count (host arrays, GPU work).
+int filter_backward_host(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
+                         const int32_t *dfs, int32_t *out, int64_t *n_out, std::string &err);
+
 // Autotuning of the wave options for a workload (the jobs, mined as one
 // batch): coordinate descent over the work chunk (wave_nodes), the row budget
 // per wave (wave_rows) and the count kernel's grid cap (count_grid); each

@@ -506,7 +506,42 @@ KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const ui
   return c;
 }
 
+// ---- backward child column on its own (gs_filter_backward)
+// flag[row] = 1 for every record {from, to, fromlabel, elabel, tolabel,
+// from_grph, to_grph, row} equal to the edge e0..e4
+__global__ void __launch_bounds__(kBlock) k_bwd_mark(const int32_t *__restrict__ rec, long long nrec, int e0, int e1,
+                                                     int e2, int e3, int e4, int32_t *flag, long long nrows)
+{
+  for(long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += (long long)gridDim.x * blockDim.x) {
+    const int32_t *x = rec + 8 * r;
+    if(x[0] == e0 && x[1] == e1 && x[2] == e2 && x[3] == e3 && x[4] == e4 && (unsigned long long)x[7] < (unsigned long long)nrows)
+      flag[x[7]] = 1;
+  }
+}
+
+// the flagged rows' elements in row order: pos = the flags' exclusive scan
+// (n + 1 entries), row r flagged iff pos[r + 1] > pos[r]
+__global__ void __launch_bounds__(kBlock) k_bwd_gather(const int2 *__restrict__ col, const int32_t *__restrict__ pos,
+                                                       long long n, int2 *out)
+{
+  for(long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    const int p = pos[r];
+    if(pos[r + 1] > p) out[p] = col[r];
+  }
+}
+
 int64_t list_scan_scratch(int64_t n) { return xscan_scratch(n) + 1; }
+
+int64_t filter_backward_scratch(int64_t nrows) { return xscan_scratch(nrows + 1); }
+
+void launch_filter_backward(const int2 *col, int64_t nrows, const int32_t *rec, int64_t nrec, const int32_t *e,
+                            int32_t *pos, int32_t *scratch, int2 *out, cudaStream_t s)
+{
+  if(nrows <= 0) return;
+  if(nrec > 0) k_bwd_mark<<<grid_for(nrec), kBlock, 0, s>>>(rec, nrec, e[0], e[1], e[2], e[3], e[4], pos, nrows);
+  xscan(pos, nrows + 1, scratch, s);
+  k_bwd_gather<<<grid_for(nrows), kBlock, 0, s>>>(col, pos, nrows, out);
+}
 
 void launch_fill_lists(const int4 *rec, long long nrec, const ListBuild &lb, int32_t *off, int64_t nrows_total,
                        int2 *ent, int64_t ent_cap, int32_t *scratch, unsigned int *err, cudaStream_t s)

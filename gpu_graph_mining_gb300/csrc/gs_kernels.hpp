@@ -149,6 +149,17 @@ struct ListBuild {
   const int32_t *rowbase;
 };
 int64_t list_scan_scratch(int64_t n);
+
+// Backward child column on its own (gs_filter_backward; the reference's
+// filter_backward_embeddings, src/gspan_cuda/filter_backward.cpp:288-352):
+// out = the elements of col at the rows named by the records (8 ints each,
+// {from, to, fromlabel, elabel, tolabel, from_grph, to_grph, row}) equal to
+// the edge e[0..5), in row order; pos[nrows + 1] (zeroed by the caller) ends
+// holding the exclusive scan of the row flags (pos[nrows] = the count).  scratch holds
+// filter_backward_scratch(nrows) ints.
+int64_t filter_backward_scratch(int64_t nrows);
+void launch_filter_backward(const int2 *col, int64_t nrows, const int32_t *rec, int64_t nrec, const int32_t *e,
+                            int32_t *pos, int32_t *scratch, int2 *out, cudaStream_t s);
 void launch_fill_lists(const int4 *rec, long long nrec, const ListBuild &lb, int32_t *off, int64_t nrows_total,
                        int2 *ent, int64_t ent_cap, int32_t *scratch, unsigned int *err, cudaStream_t s);
 

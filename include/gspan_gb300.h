@@ -373,6 +373,28 @@ GS_API gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids,
 GS_API gs_status gs_support_count_noalloc(const int32_t *d_keys, const int32_t *d_graph_ids, int64_t n_records,
                                           int32_t n_keys, int32_t n_graphs, int32_t *d_support, void *stream);
 
+/* Backward child column: the rows of an embedding column that carry one
+ * backward extension.  The GPU form of gspan_cuda::filter_backward_embeddings
+ * (src/gspan_cuda/filter_backward.cpp:288-352), which marks the rows named by
+ * the matching extension records, scans the marks and copies the marked
+ * elements.  Host arrays:
+ *   column   n_rows elements {vertex, back_link} (2 x int32 each), the
+ *            parent's last embedding column;
+ *   records  n_records extension records in the reference's
+ *            extension_element_t layout (cuda_datastructures.hpp:13-55),
+ *            8 x int32 {from, to, fromlabel, elabel, tolabel, from_grph,
+ *            to_grph, row};
+ *   dfs      the backward DFS edge {from, to, fromlabel, elabel, tolabel};
+ *            a record matches when all five fields are equal;
+ *   out      room for n_rows elements: receives the elements of the rows
+ *            named by matching records, in row order, each once;
+ *   n_out    receives their count.
+ * GS_ERR_USAGE for a forward edge (from < to: the reference aborts), a
+ * matching record whose row is outside [0, n_rows), or a null array that
+ * must be given; GS_ERR_LIMIT beyond 2^31 - 2 rows. */
+GS_API gs_status gs_filter_backward(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
+                                    const int32_t *dfs, int32_t *out, int64_t *n_out);
+
 /* Canonicality of a DFS code (n_edges tuples {from, to, fromlabel, elabel,
  * tolabel}, either label convention): 1 if minimal, 0 if not, -1 on bad
  * input.  Same semantics as the sequential reference's gSpan::is_min

@@ -9,6 +9,7 @@ or REF=...).  It
       - src/globals/test_support.cpp:10-158            three 18-graph fixture databases
       - src/gspan_cuda/tests/compute_support_remapped_test.cpp:23-71  support KAT
       - src/gspan_cuda/tests/extract_extensions_test.cpp:30-157       candidate/support KAT
+      - src/gspan_cuda/tests/filter_backward_embeddings_test.cpp:30-131  backward-filter KAT
   * copies the reference's BIN fixture databases (testdata/labeled.bin,
     testdata/unlabeled.bin),
   * writes the synthetic configuration-1 database (seed 1) with this
@@ -100,6 +101,39 @@ def extract_kat():
     dfs = re.findall(r"DFS\((\d+), (\d+), (\d+), (\d+), (\d+)\)", res)
     supp = re.search(r"int supp_res\[\] = \{([^}]*)\}", src).group(1)
     return recs, mvc, dfs, [int(x) for x in supp.split(",")]
+
+
+def filter_backward_kat():
+    src = read("src/gspan_cuda/tests/filter_backward_embeddings_test.cpp")
+    body = src[src.index("TEST(filter_backward_embeddings, basic_test)"):]
+
+    def elements(name):
+        part = body[body.index(name + "[] = {"):]
+        part = part[:part.index("};")]
+        return re.findall(r"embedding_element\((-?\d+),\s*(-?\d+)\)", part)
+
+    # the filtered column is the last of the embedding's columns (ptr[])
+    cols = re.search(r"embedding_element \*ptr\[\] = \{([^}]*)\}", body).group(1).split(",")
+    col = elements(cols[-1].strip())
+    recs = re.findall(r"extension_element_t\(\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),"
+                      r"\s*(\d+)\)", body[body.index("exts_array[]"):])
+    dfs = re.search(r"types::DFS dfs_elem\((\d+), (\d+), (\d+), (\d+), (\d+)\);", body).groups()
+    res = elements("emb_res")
+    return col, recs, dfs, res
+
+
+def write_filter_backward_kat():
+    col, recs, dfs, res = filter_backward_kat()
+    with open(os.path.join(HERE, "filter_backward_kat.tsv"), "w") as f:
+        f.write("# filter_backward_embeddings_test.cpp:30-131: the last embedding column (vertex back_link), the "
+                "extension records (from to fl el tl from_grph to_grph row), the backward edge, the filtered column\n")
+        for e in col:
+            f.write("col\t%s\n" % " ".join(e))
+        for r in recs:
+            f.write("rec\t%s\n" % " ".join(r))
+        f.write("dfs\t%s\n" % " ".join(dfs))
+        for e in res:
+            f.write("res\t%s\n" % " ".join(e))
 
 
 def run_ref(ftype, db, minsup, out):
@@ -223,6 +257,8 @@ def main():
             f.write("rec\t%s\n" % " ".join(r))
         for d, e in zip(dfs, exp):
             f.write("dfs\t%s\t%d\n" % (" ".join(d), e))
+
+    write_filter_backward_kat()
 
     for b in ("labeled.bin", "unlabeled.bin"):
         shutil.copyfile(os.path.join(REF, "testdata", b), os.path.join(HERE, "fixture_" + b))

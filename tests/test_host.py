@@ -210,6 +210,19 @@ def test_server_validates_requests_on_the_host(gs):
         assert s["submitted"] == 0 and s["running"] == 0
 
 
+def test_filter_backward_validates_on_the_host(gs):
+    # argument checks before any device work: a forward edge (the reference
+    # aborts), a matching record naming a row outside the column
+    col = [(1, 0), (4, 1)]
+    with pytest.raises(gs.GSpanError) as e:
+        gs.filter_backward(col, [(0, 1, 0, 0, 0, 0, 0, 0)], (0, 1, 0, 0, 0))
+    assert e.value.status == 1
+    with pytest.raises(gs.GSpanError) as e:
+        gs.filter_backward(col, [(2, 0, 5, 0, 2, 0, 0, 2)], (2, 0, 5, 0, 2))
+    assert e.value.status == 1
+    assert gs.filter_backward([], [], (2, 0, 5, 0, 2)) == []
+
+
 def _convert_runs():
     rows = []
     for line in read_lines(os.path.join(GOLDEN, "convert", "convert_runs.tsv")):

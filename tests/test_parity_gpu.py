@@ -190,6 +190,49 @@ def test_support_count_rejects_out_of_range(gs):
         gs.support_count([0, 5], [0, 0], 2, 4)
 
 
+def _filter_kat():
+    col, recs, res, dfs = [], [], [], None
+    for line in read_lines(os.path.join(GOLDEN, "filter_backward_kat.tsv")):
+        if line.startswith("#"):
+            continue
+        tag, rest = line.split("\t")
+        vals = tuple(int(x) for x in rest.split())
+        if tag == "col":
+            col.append(vals)
+        elif tag == "rec":
+            recs.append(vals)
+        elif tag == "dfs":
+            dfs = vals
+        else:
+            res.append(vals)
+    return col, recs, dfs, res
+
+
+def test_filter_backward_kat(gs):
+    # filter_backward_embeddings_test.cpp: the last column's rows named by
+    # the records of the backward edge (2, 0, 5, 0, 2), in row order
+    col, recs, dfs, res = _filter_kat()
+    assert gs.filter_backward(col, recs, dfs) == res == [(1, 0), (12, 3), (28, 5)]
+
+
+def test_filter_backward_random(gs):
+    # seeded random columns and records (matching and other edges, rows named
+    # twice, records out of row order) against the rows kept in a Python set;
+    # an empty column, and an edge no record carries
+    import random
+    r = random.Random(5)
+    edge = (4, 1, 2, 0, 3)
+    for n, m in [(0, 0), (1, 3), (50, 40), (5000, 9000), (300000, 200000)]:
+        col = [(r.randrange(1 << 30), r.randrange(1 << 20)) for _ in range(n)]
+        recs = []
+        for _ in range(m if n else 0):
+            e = edge if r.random() < 0.4 else (4, r.choice([0, 2, 3]), 2, r.randrange(2), 3)
+            recs.append(e + (r.randrange(100), r.randrange(100), r.randrange(n)))
+        rows = sorted({x[7] for x in recs if x[:5] == edge})
+        assert gs.filter_backward(col, recs, edge) == [col[i] for i in rows], (n, m)
+        assert gs.filter_backward(col, recs, (4, 0, 9, 9, 9)) == []
+
+
 def _fullsize():
     rows = []
     for line in read_lines(os.path.join(GOLDEN, "fullsize.tsv")):
