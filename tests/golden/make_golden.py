@@ -10,6 +10,7 @@ or REF=...).  It
       - src/gspan_cuda/tests/compute_support_remapped_test.cpp:23-71  support KAT
       - src/gspan_cuda/tests/extract_extensions_test.cpp:30-157       candidate/support KAT
       - src/gspan_cuda/tests/filter_backward_embeddings_test.cpp:30-131  backward-filter KAT
+      - src/gspan_cuda/tests/compute_support_mult_block_test.cpp:15-146 support KAT over two blocks
   * copies the reference's BIN fixture databases (testdata/labeled.bin,
     testdata/unlabeled.bin),
   * writes the synthetic configuration-1 database (seed 1) with this
@@ -91,6 +92,28 @@ def support_kat():
     dfs = re.findall(r"DFS\((\d+), (\d+), (\d+), (\d+), (\d+)\)", src[src.index("types::DFS dfs_array[]"):])
     exp = re.search(r"int expected_supports \[\] = \{([^}]*)\}", src).group(1)
     return recs, mvc, dfs, [int(x) for x in exp.split(",")]
+
+
+def mult_block_kat():
+    src = read("src/gspan_cuda/tests/compute_support_mult_block_test.cpp")
+    recs = re.findall(r"extension_element_t\(\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+),\s*(\d+)\)", src)
+    mvc = int(re.search(r"int max_graph_vertex_count = (\d+);", src).group(1))
+    arr = src[src.index("types::DFS dfs_array[]"):]
+    arr = arr[:arr.index("};")]
+    dfs = re.findall(r"DFS\((\d+), (\d+), (\d+), (\d+), (\d+)\)", arr)
+    exp = re.search(r"int expected_supports \[\] = \{([^}]*)\}", src).group(1)
+    return recs, mvc, dfs, [int(x) for x in exp.split(",")]
+
+
+def write_mult_block_kat():
+    recs, mvc, dfs, exp = mult_block_kat()
+    with open(os.path.join(HERE, "support_mult_block_kat.tsv"), "w") as f:
+        f.write("# compute_support_mult_block_test.cpp:15-146: records (from to fl el tl from_grph to_grph row), "
+                "max_graph_vertex_count=%d\n" % mvc)
+        for r in recs:
+            f.write("rec\t%s\n" % " ".join(r))
+        for d, e in zip(dfs, exp):
+            f.write("dfs\t%s\t%d\n" % (" ".join(d), e))
 
 
 def extract_kat():
@@ -259,6 +282,7 @@ def main():
             f.write("dfs\t%s\t%d\n" % (" ".join(d), e))
 
     write_filter_backward_kat()
+    write_mult_block_kat()
 
     for b in ("labeled.bin", "unlabeled.bin"):
         shutil.copyfile(os.path.join(REF, "testdata", b), os.path.join(HERE, "fixture_" + b))

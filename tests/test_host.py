@@ -210,6 +210,41 @@ def test_server_validates_requests_on_the_host(gs):
         assert s["submitted"] == 0 and s["running"] == 0
 
 
+@pytest.mark.parametrize("name", ["support_kat.tsv", "extract_kat.tsv", "support_mult_block_kat.tsv"])
+def test_support_kat_fixtures_restated(name):
+    # the expected supports of the reference's support KATs equal the distinct
+    # graphs (from_grph // max_graph_vertex_count) among each edge's records
+    recs, want = [], {}
+    for line in read_lines(os.path.join(GOLDEN, name)):
+        if line.startswith("#"):
+            mvc = int(line.rsplit("=", 1)[1])
+            continue
+        kind, rest = line.split("\t", 1)
+        if kind == "rec":
+            recs.append(tuple(int(x) for x in rest.split()))
+        else:
+            d, sup = rest.split("\t")
+            want[tuple(int(x) for x in d.split())] = int(sup)
+    got = {d: len({r[5] // mvc for r in recs if r[:5] == d}) for d in want}
+    assert got == want and len(want) >= 5
+
+
+def test_filter_backward_kat_fixture_restated():
+    # the reference's filter KAT: the last column's rows named by the records
+    # of the backward edge, in row order
+    col, recs, res, dfs = [], [], [], None
+    for line in read_lines(os.path.join(GOLDEN, "filter_backward_kat.tsv")):
+        if line.startswith("#"):
+            continue
+        tag, rest = line.split("\t")
+        vals = tuple(int(x) for x in rest.split())
+        {"col": col, "rec": recs, "res": res}.get(tag, []).append(vals)
+        if tag == "dfs":
+            dfs = vals
+    rows = sorted({r[7] for r in recs if r[:5] == dfs})
+    assert [col[i] for i in rows] == res and len(res) == 3
+
+
 def test_filter_backward_validates_on_the_host(gs):
     # argument checks before any device work: a forward edge (the reference
     # aborts), a matching record naming a row outside the column

@@ -174,7 +174,7 @@ def _kat(path):
     return recs, dfs, mvc
 
 
-@pytest.mark.parametrize("name", ["support_kat.tsv", "extract_kat.tsv"])
+@pytest.mark.parametrize("name", ["support_kat.tsv", "extract_kat.tsv", "support_mult_block_kat.tsv"])
 def test_support_kats(gs, name):
     # records (from, to, fl, el, tl, from_grph, to_grph, row); graph = vertex // max_graph_vertex_count
     recs, dfs, mvc = _kat(os.path.join(GOLDEN, name))
