@@ -304,7 +304,9 @@ __global__ void k_pairs_index(const long long *seen, const long long *rank, int 
 // network in registers up to 8 entries, else an insertion sort in place; the
 // caller sorts only when no vertex has more than kSortDegree entries), and
 // the pair index of every adj entry
-constexpr int kSortDegree = 1024;
+// an insertion sort of d entries makes about d * d / 4 dependent global
+// accesses: 256 bounds one thread's sort to about 16,000
+constexpr int kSortDegree = 256;
 
 __global__ void k_pack(const int32_t *off, long long V, const int32_t *vl, const int32_t *adj_to, const int32_t *el,
                        const int32_t *pair_idx, int EL, int VL, bool sort, unsigned long long *adj_in,
