@@ -395,7 +395,10 @@ __global__ void k_narrow(const long long *x, long long n, int32_t *out)
     out[i] = (int32_t)x[i];
 }
 
-constexpr unsigned long long kKeepBytes = 4ull << 30;
+// A 1,000,000-graph database (80 M adjacency entries) peaks at about 4.5 GB
+// of scratch plus block; below that keep size every ingest re-mapped the
+// difference, which measured tens of milliseconds on some steps.
+constexpr unsigned long long kKeepBytes = 16ull << 30;
 
 // Values read back to the host at the ingest's synchronisation points
 // (pinned, so the copies are asynchronous).
