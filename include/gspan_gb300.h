@@ -88,7 +88,11 @@ GS_API gs_db *gs_db_from_arrays(int32_t db_size, int32_t edges_sizes, int32_t ma
  * gs_db_from_arrays; the database is resident when the call returns.  The
  * host arrays are built only if the database is written (gs_db_write).
  * Vertex label values must span at most 2^22 and the label alphabet must
- * keep |VL|*|EL|*|VL| <= 2^25, else GS_ERR_LIMIT (use gs_db_from_arrays). */
+ * keep |VL|*|EL|*|VL| <= 2^25, else GS_ERR_LIMIT (use gs_db_from_arrays).
+ * Memory: the scratch and the database come from a stream-ordered pool that
+ * keeps up to 16 GiB of device memory between ingests (gs_engine_reset
+ * returns it), and such a database holds its adjacency twice (8 more bytes
+ * per entry): sorted for mining and in input order for gs_db_write. */
 GS_API gs_db *gs_db_from_arrays_device(int32_t db_size, int32_t edges_sizes, int32_t max_graph_vertex_count,
                                        int32_t vertex_count, const int32_t *edges, const int32_t *edges_labels,
                                        const int32_t *vertex_labels, const int32_t *vertex_offsets,
@@ -402,7 +406,8 @@ GS_API gs_status gs_filter_backward(const int32_t *column, int64_t n_rows, const
  * (src/globals/dfs_ismin.cpp:23-160) mirrors; host-only, no GPU needed. */
 GS_API int32_t gs_dfs_code_is_min(const int32_t *dfs5xN, int32_t n_edges);
 
-/* Frees the miner's device pool and scratch buffers. */
+/* Frees the miner's device pool and scratch buffers, and returns the
+ * device ingest's cached pool memory. */
 GS_API void gs_engine_reset(void);
 /* Caps the device pool (bytes; 0 = 70% of free device memory). */
 GS_API void gs_engine_set_pool_bytes(int64_t bytes);
