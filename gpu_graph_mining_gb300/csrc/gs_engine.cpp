@@ -722,9 +722,21 @@ struct WaveCtx {
 };
 
 constexpr int kMaxDbSlots = 256;
-// waves whose databases hold at most this many adjacency bytes (12 per
-// entry) skip the entries below a forward rule (sorted adjacency)
-constexpr int64_t kRuleSkipAdjBytes = 96ll << 20;
+// Waves whose databases hold at most three quarters of the L2 in adjacency
+// bytes (12 per entry) skip the entries below a forward rule (sorted
+// adjacency): about 97 MiB on a GB300.
+int64_t rule_skip_adj_bytes()
+{
+  static const int64_t v = [] {
+    int l2 = 0;
+    if(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, 0) != cudaSuccess || l2 <= 0) {
+      cudaGetLastError();
+      l2 = 128 << 20;
+    }
+    return (int64_t)l2 * 3 / 4;
+  }();
+  return v;
+}
 // Wave contexts in flight (compile-time tunable): while the GPU works through
 // the queued waves, the host completes the oldest and launches new ones.
 // Contexts beyond the first two launch only when a full wave of nodes is
@@ -1580,7 +1592,7 @@ private:
     // the adjacency stays in L2 (configuration 2, 72 MB: count kernel 3%
     // faster) and cost more than the skipped items save beyond it
     // (configuration 5, 960 MB: 10% slower)
-    f.rule_skip = adj_bytes <= kRuleSkipAdjBytes;
+    f.rule_skip = adj_bytes <= rule_skip_adj_bytes();
     f.tb = tb;
     // copies of the wave's counters: the warps of a large node all add into that
     // node's few counters; copies spread them over L2 slices (summed by screening)
