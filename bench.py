@@ -1,25 +1,33 @@
 """Benchmark: frequent patterns per second of the GB300 gSpan miner.
 
-Workload (default): generator configuration 2 -- 100,000 graphs, Poisson(30)
-edges per graph, 5 vertex / 5 edge labels, 50 embedded seed patterns --
-mined at minsup 1% (1000 graphs).  One step = one complete mining pass at
-that support (every frequent pattern of the database enumerated, supports
-counted, canonicality checked, patterns emitted to the host).
+Workload (default): generator configuration 5 -- 1,000,000 graphs, Poisson(40)
+edges per graph, 10 Zipf(1.2) vertex labels, 3 edge labels, 200 embedded
+seed patterns of 3-8 edges (80 M adjacency entries, about 1 GB, far beyond
+the 129 MB L2) -- mined at minsup 0.5% (5000 graphs).  One step = one
+complete mining pass at that support (every frequent pattern of the database
+enumerated, supports counted, canonicality checked, patterns written to the
+host).
 
 value      : patterns / second with the database already resident in HBM
 e2e        : same metric through the C ABI from host arrays: the reference's
              cudabin arrays copied to the GPU and converted there
              (gs_db_from_arrays_device), mined, every pattern written to the
              host buffer -- all inside the timed step
-roofline   : the count kernel (k_wave_count, the dominant kernel): algorithmic
-             bytes per launch / kernel time, both measured inside the library on
-             its own stream with CUDA events, against the measured HBM peak
+roofline   : the count kernel (k_wave count, the dominant kernel): algorithmic
+             bytes / kernel time, both measured inside the library on its own
+             stream with CUDA events, against the measured HBM peak; the
+             materialise and selection kernels beside it
 cpu_baseline: the oracle (C restatement of the reference's sequential gSpan) on
-             one host core, time-bounded sample of the same workload
+             one host core, a time-bounded sample of the same workload
+Nested, same line: configuration 2 (100,000 graphs) at minsup 1/2/5%, the
+64-database batch (configuration 3) against the same databases mined one at
+a time, and the serving streams (configuration 4) with p50/p99 latency.
 
---impl reference times the reference's CPU implementation (the oracle port,
-since the reference's own sources are not present on the GPU host) on all host
-cores, one process per core over disjoint root subtrees, time-bounded.
+--impl reference times the reference's CPU implementation -- the oracle port,
+since the reference's sources are not present on the GPU host -- on all host
+cores (one process per core over disjoint root subtrees), without loading
+anything of this package: the oracle generates the same seeded database
+itself.
 
 Multi-GPU (torchrun, N > 1): every rank mines a disjoint set of root subtrees
 of the same database (no data exchange); the step time is the max over ranks.
@@ -43,7 +51,9 @@ if WORLD > 1:
     # one GPU per rank: the native library sees only this rank's device
     os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
 
-L2_BYTES = 129 * 1024 * 1024
+ORACLE = os.path.join(REPO, "oracle", "_build", "gspan_oracle")
+METRIC = "frequent patterns/sec"
+UNIT = "patterns/s"
 
 
 def parse():
@@ -52,21 +62,29 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--config", type=int, default=2)
+    p.add_argument("--config", type=int, default=5)
     p.add_argument("--scale", type=float, default=1.0)
-    p.add_argument("--minsup-frac", type=float, default=0.01)
+    p.add_argument("--minsup-frac", type=float, default=None,
+                   help="default: 0.5%% for configuration 5, 1%% otherwise")
     p.add_argument("--wave-nodes", type=int, default=None)
     p.add_argument("--launch-mode", type=int, default=0, help="0: per-wave CUDA graphs, 1: direct launches")
     p.add_argument("--extension", default="rmpath", choices=["rmpath", "lists"],
                    help="extension strategy: rmpath scans every right-most-path vertex (default); lists joins "
                         "the parent's per-row lists (the reference's gspan_cuda_lists)")
-    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="cpu_baseline: the oracle's time bound")
+    p.add_argument("--ref-seconds", type=float, default=3.0,
+                   help="--impl reference: each step's time bound per process")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="the headline workload only (no configuration-2 sweep, batch or serving keys)")
     p.add_argument("--workload", default="mine", choices=["mine", "batch", "serving"],
                    help="mine: one database (the default line); batch: 64 databases mined together vs one at "
                         "a time; serving: Poisson request streams against 8 resident databases")
     p.add_argument("--requests", type=float, default=1.0, help="serving: scale of the request counts")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.minsup_frac is None:
+        a.minsup_frac = 0.005 if a.config == 5 else 0.01
+    return a
 
 
 def peaks():
@@ -76,6 +94,14 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def workload_name(config, scale, minsup_frac):
+    return "config%d: generator configuration %d x%.3g, minsup %.2f%%" % (config, config, scale, 100 * minsup_frac)
+
+
+def gen_spec(config, scale, seed=0):
+    return "%d,%d,%r" % (config, seed, float(scale))
 
 
 class Clocks:
@@ -131,23 +157,110 @@ class Clocks:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(mhz)}
 
 
-def count_traffic(a, alg_bytes_per_step, launches_per_step):
-    """DRAM bytes per count-kernel launch from the committed ncu capture
-    (profiles/k_wave_count_traffic_config2.json): as captured for the same
-    workload, else scaled by this run's algorithmic bytes per launch."""
+# ---------------------------------------------------------------- reference arm
+
+def ensure_oracle():
+    if not os.path.exists(ORACLE):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle")])
+
+
+def parse_oracle_lines(stderr):
+    """The oracle's stderr: one load line, then one timing line per pass."""
+    load, passes = {}, []
+    for line in stderr.splitlines():
+        d = {}
+        for tok in line.split():
+            if "=" in tok:
+                k, v = tok.split("=", 1)
+                d[k] = v
+        if "load_time" in d:
+            load = d
+        elif "total_time" in d:
+            passes.append((float(d["total_time"]), int(float(d["total_frequent_graphs"])), "stopped" in d))
+    return load, passes
+
+
+def oracle_passes(spec, minsup, seconds, repeat, cores):
+    """Runs the oracle on a generated database as `cores` processes over
+    disjoint root subtrees, each mining `repeat` passes stopped after
+    `seconds`.  Returns the load line and, per pass, (max elapsed over the
+    processes, patterns found by all, any process stopped)."""
+    ensure_oracle()
+    procs = []
+    for i in range(cores):
+        cmd = [ORACLE, "gen", spec, str(minsup), "-", "--time-limit", str(seconds), "--repeat", str(repeat)]
+        if cores > 1:
+            cmd += ["--roots", "%d/%d" % (i, cores)]
+        procs.append(subprocess.Popen(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True))
+    outs = []
+    for p in procs:
+        err = p.communicate()[1]
+        if p.returncode != 0:
+            raise RuntimeError("oracle failed (%d): %s" % (p.returncode, err[-500:]))
+        outs.append(parse_oracle_lines(err))
+    load = outs[0][0]
+    res = []
+    for j in range(repeat):
+        res.append((max(o[1][j][0] for o in outs), sum(o[1][j][1] for o in outs), any(o[1][j][2] for o in outs)))
+    return load, res
+
+
+def config_from_load(a, load, minsup):
+    return {"workload": workload_name(a.config, a.scale, a.minsup_frac), "graphs": int(load["graphs"]),
+            "vertices": int(load["vertices"]), "adjacency_entries": int(load["adjacency_entries"]),
+            "minsup": minsup, "l2": "flushed between steps (256 MiB write)"}
+
+
+def bench_reference(a):
+    """The reference's sequential gSpan (src/gspan/gspan.cpp:281-351, restated
+    by the oracle) on all host cores.  Nothing of the GPU package is loaded:
+    the oracle generates the seeded database itself (a CPU test checks that it
+    is byte for byte the one the GPU arm mines)."""
+    if RANK != 0:
+        return
+    cores = os.cpu_count() or 1
+    spec = gen_spec(a.config, a.scale)
+    ensure_oracle()
+    n_graphs = int(subprocess.check_output([ORACLE, "--gen-count", spec], text=True))
+    minsup = max(1, int(round(a.minsup_frac * n_graphs)))
+    load, res = oracle_passes(spec, minsup, a.ref_seconds, a.warmup + a.steps, cores)
+    timed = res[a.warmup:]
+    vals = [p / el if el > 0 else 0.0 for el, p, _ in timed]
+    v = sum(vals) / len(vals)
+    stopped = any(s for _, _, s in timed)
+    ms = 1000.0 * sum(el for el, _, _ in timed) / len(timed)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": config_from_load(a, load, minsup),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "oracle (C restatement of src/gspan, pinned to the reference binary) on the "
+                                       "full generated database at minsup %d, one process per core over disjoint "
+                                       "root subtrees; each step is one pass of every process %s after %.1f s; "
+                                       "patterns found by all / the slowest process's time"
+                                       % (minsup, "stopped" if stopped else "complete", a.ref_seconds)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "patterns_per_step": [p for _, p, _ in timed]}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def count_traffic(tag, alg_bytes_per_step, launches_per_step):
+    """DRAM bytes per count-kernel launch from the committed ncu capture of this
+    workload (profiles/k_wave_count_traffic_<tag>.json), scaled by this run's
+    algorithmic bytes per launch when the capture saw a different amount."""
+    path = os.path.join(REPO, "profiles", "k_wave_count_traffic_%s.json" % tag)
     try:
-        with open(os.path.join(REPO, "profiles", "k_wave_count_traffic_config2.json")) as f:
+        with open(path) as f:
             p = json.load(f)
     except Exception:
         return None, None
     if launches_per_step <= 0:
         return None, None
     per_launch = alg_bytes_per_step / launches_per_step
-    if a.config == 2 and a.scale == 1.0 and abs(a.minsup_frac - 0.01) < 1e-12:
-        return float(p["dram_bytes_per_launch"]), "ncu capture of this workload: " + p["command"]
     ratio = p["dram_bytes_per_pass"] / p["algorithmic_bytes_per_pass"]
-    return ratio * per_launch, ("scaled from the configuration-2 capture by algorithmic bytes per launch "
-                                "(traffic/algorithmic = %.3f)" % ratio)
+    return ratio * per_launch, ("ncu capture %s (DRAM / algorithmic bytes = %.3f, applied to this run's "
+                                "algorithmic bytes per launch): %s" % (os.path.basename(path), ratio, p["command"]))
 
 
 def cudabin_arrays(db, tmpdir):
@@ -167,57 +280,147 @@ def cudabin_arrays(db, tmpdir):
     return n, esz, maxv, vc, arrs
 
 
-def run_oracle_sample(db_txt, minsup, seconds, part=None):
-    oracle = os.path.join(REPO, "oracle", "_build", "gspan_oracle")
-    if not os.path.exists(oracle):
-        subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle")])
-    cmd = [oracle, "txt", db_txt, str(minsup), "-", "--time-limit", str(seconds)]
-    if part is not None:
-        cmd += ["--roots", "%d/%d" % part]
-    return subprocess.Popen(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+def cpu_oracle_sample(spec, minsup, seconds):
+    """cpu_baseline: the oracle on one core, one pass stopped after `seconds`."""
+    _, res = oracle_passes(spec, minsup, seconds, 1, 1)
+    el, pats, stopped = res[0]
+    return pats, el, stopped
 
 
-def parse_oracle(stderr):
-    d = {}
-    for tok in stderr.split():
-        if "=" in tok:
-            k, v = tok.split("=", 1)
-            d[k] = v
-    return float(d.get("total_time", "nan")), int(float(d.get("total_frequent_graphs", "0"))), "stopped" in d
+class Timer:
+    """Barrier + synchronize on both sides; CUDA events on torch's stream
+    bracket the call (the library's own stream work is ordered inside it by
+    the call's synchronous return)."""
+
+    def __init__(self, torch, dist, flush):
+        self.torch, self.dist, self.flush = torch, dist, flush
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+        self.torch.cuda.synchronize()
+
+    def run(self, fn):
+        torch = self.torch
+        self.flush.fill_(1)
+        self.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        r = fn()
+        e1.record()
+        self.barrier()
+        return r, e0.elapsed_time(e1)
 
 
-def cpu_oracle(db_txt, minsup, seconds, cores):
-    t0 = time.time()
-    procs = [run_oracle_sample(db_txt, minsup, seconds, (i, cores) if cores > 1 else None) for i in range(cores)]
-    res = [parse_oracle(p.communicate()[1]) for p in procs]
-    wall = time.time() - t0
-    elapsed = max(r[0] for r in res)
-    pats = sum(r[1] for r in res)
-    stopped = any(r[2] for r in res)
-    return pats, elapsed, stopped, wall
+def roofline(stats_all, peak, peak_kind, traffic, traffic_note):
+    """Achieved GB/s of the count, materialise and selection kernels: their
+    algorithmic bytes (counted inside the kernels) / their device time (CUDA
+    events on the engine's stream), averaged over the timed steps."""
+    n = len(stats_all)
+
+    def avg(k):
+        return sum(s[k] for s in stats_all) / n
+
+    def kern(bytes_key, ms_key):
+        b, ms = avg(bytes_key), avg(ms_key)
+        gbps = (b / (ms / 1000.0)) / 1e9 if ms > 0 else 0.0
+        return {"achieved": gbps, "frac": gbps / peak if peak else None, "algorithmic_bytes_per_step": b,
+                "kernel_ms_per_step": ms}
+    count = kern("count_bytes", "count_ms")
+    mat = kern("mat_bytes", "mat_ms")
+    sel = kern("sel_bytes", "sel_ms")
+    waves = avg("waves")
+    return {"bound": "hbm", "kernel": "k_wave count", "achieved": count["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": count["frac"], "peak_kind": peak_kind, "traffic": traffic, "traffic_source": traffic_note,
+            "algorithmic_bytes_per_step": count["algorithmic_bytes_per_step"],
+            "kernel_ms_per_step": count["kernel_ms_per_step"], "launches_per_step": waves,
+            "kernels": {"k_wave count": count, "materialise (k_mat_records, k_wave materialise)": mat,
+                        "selection (k_screen_keys + k_count_listed)": sel,
+                        "k_is_min": {"kernel_ms_per_step": avg("min_ms"), "note": "shared memory only"}}}
 
 
-def _timed(fn):
-    import torch
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    r = fn()
-    torch.cuda.synchronize()
-    return r, (time.perf_counter() - t0) * 1000.0
+def mine_timed(g, tm, db, minsup, steps, warmup, kw):
+    for _ in range(warmup):
+        g.mine_collect(db, minsup, decode=False, **kw)
+    times, stats_all, n = [], [], None
+    for _ in range(steps):
+        # every pattern lands in a host buffer (gs_mine_collect), freed after timing
+        (n, st), ms = tm.run(lambda: g.mine_collect(db, minsup, decode=False, **kw))
+        times.append(ms)
+        stats_all.append(st)
+    return times, stats_all, n
 
 
-def bench_batch(a, g):
+def e2e_timed(g, tm, db, minsup, steps, kw):
+    """The reference's set_database(graph_database_cuda&) path: host cudabin
+    arrays in, converted and indexed on the GPU, mined, patterns to the host."""
+    import ctypes
+    times, h2d, d2h = [], 0, 0
+    with tempfile.TemporaryDirectory() as td:
+        n, esz, maxv, vc, arrs = cudabin_arrays(db, td)
+        P = ctypes.POINTER(ctypes.c_int32)
+
+        def ptr(x):
+            return x.ctypes.data_as(P)
+
+        def step():
+            st = ctypes.c_int32(0)
+            h = g.lib().gs_db_from_arrays_device(n, esz, maxv, vc, ptr(arrs["edges"]), ptr(arrs["edges_labels"]),
+                                                 ptr(arrs["vertex_labels"]), ptr(arrs["vertex_offsets"]),
+                                                 ctypes.byref(st))
+            if not h:
+                raise RuntimeError(g.lib().gs_last_error().decode())
+            d = g.Database(h)
+            _, s = g.mine_collect(d, minsup, decode=False, **kw)
+            d.free()
+            return s
+        raw = sum(int(x.nbytes) for x in arrs.values())
+        for i in range(steps + 1):
+            s, ms = tm.run(step)
+            if i > 0:  # the first pass is a warm-up
+                times.append(ms)
+                # the cudabin arrays uploaded by the ingest, plus the miner's own copies
+                h2d, d2h = s["h2d_bytes"] + raw, s["d2h_bytes"]
+    return times, h2d, d2h
+
+
+def config2_sweep(a, g, tm):
+    """Configuration 2 (100,000 graphs) at minsup 1, 2 and 5%: resident
+    patterns/s, the three kernels' GB/s at 1%, and end to end at 1%."""
+    peak, peak_kind = peaks()
+    db = g.Database.generate(2)
+    db.upload()
+    steps = max(3, min(a.steps, 10))
+    out = {"workload": "generator configuration 2 (100,000 graphs)", "graphs": len(db), "steps": steps}
+    for frac in (0.01, 0.02, 0.05):
+        ms_ = max(1, int(round(frac * len(db))))
+        times, stats_all, n = mine_timed(g, tm, db, ms_, steps, 3, {})
+        ms = sum(times) / len(times)
+        r = {"minsup": ms_, "patterns": n, "ms_per_step": ms, "value": n / (ms / 1000.0)}
+        if frac == 0.01:
+            cb = sum(s["count_bytes"] for s in stats_all) / len(stats_all)
+            w = sum(s["waves"] for s in stats_all) / len(stats_all)
+            traffic, note = count_traffic("config2", cb, w)
+            r["roofline"] = roofline(stats_all, peak, peak_kind, traffic, note)
+            et, h2d, d2h = e2e_timed(g, tm, db, ms_, steps, {})
+            e = sum(et) / len(et)
+            r["e2e"] = {"value": n / (e / 1000.0), "ms_per_step": e, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h}
+        out["minsup_%g%%" % (100 * frac)] = r
+    db.free()
+    return out
+
+
+def bench_batch(a, g, tm, steps):
     """64 databases (generator configuration 3, seeds 1000..1063: 1,000-50,000
     graphs log-uniform, 2-20 vertex and edge labels, 10-40 mean edges) at
     minsup 5%: all mined in shared waves by one gs_mine_batch call, against the
     same 64 mined one at a time (batched engine, and the plain one-node-per-
     launch form).  No pattern output in any arm (patterns are counted)."""
-    import torch
     dbs = [g.Database.generate(3, seed=1000 + i, scale=a.scale) for i in range(64)]
     sups = [max(1, int(round(0.05 * len(d)))) for d in dbs]
     for d in dbs:
         d.upload()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda:0")
     for _ in range(max(3, a.warmup)):
         g.mine_batch(dbs, sups, collect=False)
     # untimed: the autotuner picks the wave options for this workload
@@ -230,16 +433,13 @@ def bench_batch(a, g):
     clocks = Clocks()
     clocks.start()
     tb, st_b, td, tl = [], None, [], []
-    for _ in range(a.steps):
-        flush.fill_(1)
-        (_, st_b), ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False, **tuned))
+    for _ in range(steps):
+        (_, st_b), ms = tm.run(lambda: g.mine_batch(dbs, sups, collect=False, **tuned))
         tb.append(ms)
-        flush.fill_(1)
-        _, ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False))
+        _, ms = tm.run(lambda: g.mine_batch(dbs, sups, collect=False))
         td.append(ms)
         # the lists extension strategy on the same batch and options
-        flush.fill_(1)
-        (_, st_l), ms = _timed(lambda: g.mine_batch(dbs, sups, collect=False, extension="lists", **tuned))
+        (_, st_l), ms = tm.run(lambda: g.mine_batch(dbs, sups, collect=False, extension="lists", **tuned))
         tl.append(ms)
     clk = clocks.stop()
     pats = st_b["patterns"]
@@ -248,8 +448,7 @@ def bench_batch(a, g):
     def one_at_a_time(**kw):
         tot, n = 0.0, 0
         for d, s in zip(dbs, sups):
-            flush.fill_(1)
-            (_, st), ms = _timed(lambda: g.mine(d, s, collect=False, **kw))
+            (_, st), ms = tm.run(lambda: g.mine(d, s, collect=False, **kw))
             tot += ms
             n += st["patterns"]
         return tot, n
@@ -259,7 +458,7 @@ def bench_batch(a, g):
     assert n_solo == pats == n_plain, (n_solo, pats, n_plain)
     ms = sum(tb) / len(tb)
     line = {"metric": "frequent patterns/sec", "value": pats / (ms / 1000.0), "unit": "patterns/s", "n_gpus": 1,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "steps": steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": "batch: 64 databases of generator configuration 3 (seeds 1000-1063), minsup 5%, "
                                    "one gs_mine_batch call with autotuned wave options",
@@ -274,11 +473,13 @@ def bench_batch(a, g):
             "one_at_a_time": {"ms": t_solo, "patterns_per_s": pats / (t_solo / 1000.0)},
             "plain_one_at_a_time": {"ms": t_plain, "patterns_per_s": pats / (t_plain / 1000.0)},
             "speedup_vs_one_at_a_time": t_solo / ms, "speedup_vs_plain": t_plain / ms,
-            "clocks": clk, "gpu_launches": int(st_b["launches"]) * a.steps, "stats_last_step": st_b}
-    print(json.dumps(line))
+            "clocks": clk, "gpu_launches": int(st_b["launches"]) * steps, "stats_last_step": st_b}
+    for d in dbs:
+        d.free()
+    return line
 
 
-def bench_serving(a, g):
+def bench_serving(a, g, tm):
     """8 resident databases (generator configuration 4, seeds 2000..2007:
     10,000-200,000 graphs); Poisson request streams at 5, 20, 50 and 200
     requests/s (seed 7), each request = (database uniform, minsup uniform from
@@ -334,7 +535,7 @@ def bench_serving(a, g):
     def serial(**kw):
         tot, n = 0.0, 0
         for d, s, me in last_reqs:
-            (_, st), ms = _timed(lambda: g.mine(dbs[d], s, max_edges=me, collect=False, **kw))
+            (_, st), ms = tm.run(lambda: g.mine(dbs[d], s, max_edges=me, collect=False, **kw))
             tot += ms
             n += st["patterns"]
         return tot, n
@@ -355,58 +556,20 @@ def bench_serving(a, g):
             "server": {"max_running": sst["max_running"], "completed": sst["completed"], "waves": sst["waves"],
                        "peak_pool_bytes": sst["peak_pool_bytes"]},
             "clocks": clk}
-    print(json.dumps(line))
+    for d in dbs:
+        d.free()
+    return line
 
 
 def main():
     a = parse()
+    if a.impl == "reference":
+        bench_reference(a)
+        return
     import gpu_graph_mining_gb300 as g
     if not os.path.exists(g.LIB_PATH):
         from gpu_graph_mining_gb300 import build as b
         b.build()
-    if a.workload != "mine" and a.impl == "gb300":
-        if RANK == 0:
-            (bench_batch if a.workload == "batch" else bench_serving)(a, g)
-        return
-
-    workload = "config%d: generator configuration %d x%.3g, minsup %.2f%%" % (a.config, a.config, a.scale,
-                                                                             100 * a.minsup_frac)
-    metric = "frequent patterns/sec"
-    unit = "patterns/s"
-    db = g.Database.generate(a.config, scale=a.scale)
-    minsup = max(1, int(round(a.minsup_frac * len(db))))
-    info = db.info()
-    config = {"workload": workload, "graphs": info["graphs"], "vertices": info["vertices"],
-              "adjacency_entries": info["adjacency_entries"], "minsup": minsup,
-              "l2": "flushed between steps (256 MiB write)"}
-
-    if a.impl == "reference":
-        if RANK != 0:
-            return
-        cores = os.cpu_count() or 1
-        with tempfile.TemporaryDirectory() as td:
-            p = os.path.join(td, "db.txt")
-            db.write(p, "txt")
-            for _ in range(a.warmup):  # short warm-up samples (page cache, CPU clocks)
-                cpu_oracle(p, minsup, 1.0, cores)
-            vals = []
-            t_all = 0.0
-            for _ in range(a.steps):
-                pats, el, stopped, wall = cpu_oracle(p, minsup, a.cpu_seconds, cores)
-                vals.append(pats / el if el > 0 else 0.0)
-                t_all += el
-        v = sum(vals) / len(vals)
-        line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": 0, "steps": a.steps,
-                "warmup": a.warmup, "ms_per_step": 1000 * t_all / a.steps, "higher_is_better": True,
-                "scaling": "strong", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": config,
-                "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port",
-                                 "sample": "oracle (C restatement of src/gspan) on the full database at the same "
-                                           "minsup, one process per core over disjoint root subtrees, each stopped "
-                                           "after %.0f s; patterns found / elapsed" % a.cpu_seconds},
-                "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return
-
     import torch
     dist = None
     if WORLD > 1:
@@ -414,15 +577,22 @@ def main():
         torch.cuda.set_device(0)
         dist.init_process_group("nccl")
     dev = torch.device("cuda:0")
-    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+    # written between timed steps: larger than the 129 MB L2
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+    tm = Timer(torch, dist, flush)
+    if a.workload != "mine":
+        if RANK == 0:
+            line = bench_batch(a, g, tm, a.steps) if a.workload == "batch" else bench_serving(a, g, tm)
+            print(json.dumps(line))
+        return
 
-    def barrier():
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
+    db = g.Database.generate(a.config, scale=a.scale)
+    minsup = max(1, int(round(a.minsup_frac * len(db))))
+    info = db.info()
+    config = {"workload": workload_name(a.config, a.scale, a.minsup_frac), "graphs": info["graphs"],
+              "vertices": info["vertices"], "adjacency_entries": info["adjacency_entries"], "minsup": minsup,
+              "l2": "flushed between steps (256 MiB write)"}
     part = dict(root_part=RANK, root_parts=WORLD) if WORLD > 1 else {}
-    db.upload()
     kw = dict(part)
     if a.wave_nodes is not None:
         kw["wave_nodes"] = a.wave_nodes
@@ -431,29 +601,16 @@ def main():
     if a.extension != "rmpath":
         kw["extension"] = a.extension
         config["extension"] = a.extension
-    # warm-up (also creates the engine's pool and scratch)
+    db.upload()
+
+    # ---- resident-database timing (the warm-up also creates the engine's pool and scratch)
+    clocks = Clocks()
     for _ in range(max(3, a.warmup)):
         g.mine_collect(db, minsup, decode=False, **kw)
-
-    # ---- resident-database timing
-    clocks = Clocks()
     clocks.start()
-    times, stats_all = [], []
-    n_patterns = None
-    for _ in range(a.steps):
-        flush_buf.fill_(1)
-        barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        # every pattern lands in a host buffer (gs_mine_collect), freed after timing
-        n_patterns, st = g.mine_collect(db, minsup, decode=False, **kw)
-        e1.record()
-        barrier()
-        times.append(e0.elapsed_time(e1))
-        stats_all.append(st)
+    times, stats_all, pats_local = mine_timed(g, tm, db, minsup, a.steps, 0, kw)
     clk = clocks.stop()
     ms = sum(times) / len(times)
-    pats_local = n_patterns
     if dist:
         t = torch.tensor([ms, float(pats_local)], device=dev)
         mx = t.clone()
@@ -464,57 +621,16 @@ def main():
     else:
         ms_job, pats_job = ms, pats_local
     value = pats_job / (ms_job / 1000.0)
-
-    # roofline of the count kernel (mean over timed steps)
-    cb = sum(s["count_bytes"] for s in stats_all) / len(stats_all)
-    cms = sum(s["count_ms"] for s in stats_all) / len(stats_all)
-    mb = sum(s["mat_bytes"] for s in stats_all) / len(stats_all)
-    mms = sum(s["mat_ms"] for s in stats_all) / len(stats_all)
     peak, peak_kind = peaks()
+    cb = sum(s["count_bytes"] for s in stats_all) / len(stats_all)
     waves = sum(s["waves"] for s in stats_all) / len(stats_all)
-    count_gbps = (cb / (cms / 1000.0)) / 1e9 if cms > 0 else 0.0
-    mat_gbps = (mb / (mms / 1000.0)) / 1e9 if mms > 0 else 0.0
-    # the dominant kernel is the one with more device time per step
-    if mms > cms:
-        dom, achieved, dom_bytes, dom_ms, other = "k_wave materialise", mat_gbps, mb, mms, ("k_wave count", count_gbps)
-    else:
-        dom, achieved, dom_bytes, dom_ms, other = "k_wave count", count_gbps, cb, cms, ("k_wave materialise", mat_gbps)
+    tag = "config%d" % a.config if a.scale == 1.0 and a.extension == "rmpath" else "none"
+    traffic, traffic_note = count_traffic(tag, cb, waves)
+    roof = roofline(stats_all, peak, peak_kind, traffic, traffic_note)
     launches_per_step = sum(s["launches"] for s in stats_all) / len(stats_all)
-    traffic, traffic_note = count_traffic(a, cb, waves) if dom == "k_wave count" else (None, None)
 
-    # ---- end-to-end through the C ABI from host arrays
-    e2e_times, h2d, d2h = [], 0, 0
-    with tempfile.TemporaryDirectory() as td:
-        n, esz, maxv, vc, arrs = cudabin_arrays(db, td)
-        import ctypes
-        import numpy as np
-        P = ctypes.POINTER(ctypes.c_int32)
-
-        def ptr(x):
-            return x.ctypes.data_as(P)
-        for i in range(a.steps + 1):
-            flush_buf.fill_(1)
-            barrier()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            st = ctypes.c_int32(0)
-            # the reference's set_database(graph_database_cuda&) path: host arrays in,
-            # converted and indexed on the GPU
-            h = g.lib().gs_db_from_arrays_device(n, esz, maxv, vc, ptr(arrs["edges"]), ptr(arrs["edges_labels"]),
-                                                 ptr(arrs["vertex_labels"]), ptr(arrs["vertex_offsets"]),
-                                                 ctypes.byref(st))
-            if not h:
-                raise RuntimeError(g.lib().gs_last_error().decode())
-            d = g.Database(h)
-            _, s = g.mine_collect(d, minsup, decode=False, **kw)
-            d.free()
-            e1.record()
-            barrier()
-            if i > 0:  # the first pass is a warm-up
-                e2e_times.append(e0.elapsed_time(e1))
-                # the cudabin arrays uploaded by the ingest, plus the miner's own copies
-                raw = sum(int(x.nbytes) for x in arrs.values())
-                h2d, d2h = s["h2d_bytes"] + raw, s["d2h_bytes"]
+    # ---- end to end through the C ABI from host arrays
+    e2e_times, h2d, d2h = e2e_timed(g, tm, db, minsup, a.steps, kw)
     e2e_ms = sum(e2e_times) / len(e2e_times)
     if dist:
         t = torch.tensor([e2e_ms], device=dev)
@@ -526,34 +642,38 @@ def main():
         dist.destroy_process_group() if dist else None
         return
 
-    cpu = None
-    if not a.no_cpu_baseline and WORLD == 1:
-        with tempfile.TemporaryDirectory() as td:
-            p = os.path.join(td, "db.txt")
-            db.write(p, "txt")
-            pats, el, stopped, _ = cpu_oracle(p, minsup, a.cpu_seconds, 1)
-        cpu = {"value": pats / el if el > 0 else None, "unit": unit, "cores": 1, "kind": "port",
-               "sample": "oracle (C restatement of src/gspan, pinned to the reference) on the full database at "
-                         "minsup %d, %s after %.1f s: %d patterns" % (minsup, "stopped" if stopped else "finished",
-                                                                      el, pats)}
-
     line = {
-        "metric": metric, "value": value, "unit": unit, "n_gpus": WORLD, "steps": a.steps, "warmup": a.warmup,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_job, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic", "config": config,
         "patterns_per_step": pats_job,
-        "e2e": {"value": e2e, "unit": unit, "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "peak_kind": peak_kind, "traffic": traffic,
-                     "traffic_source": traffic_note,
-                     "algorithmic_bytes_per_step": dom_bytes, "kernel_ms_per_step": dom_ms,
-                     "launches_per_step": waves, "other_kernel": {"kernel": other[0], "achieved": other[1]}},
-        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": len(e2e_times)},
+        "roofline": roof,
+        "cpu_baseline": None,
         "clocks": clk,
         "gpu_launches": int(launches_per_step * a.steps),
         "stats_last_step": stats_all[-1],
     }
+    db.free()
+    if not a.no_cpu_baseline and WORLD == 1:
+        pats, el, stopped = cpu_oracle_sample(gen_spec(a.config, a.scale), minsup, a.cpu_seconds)
+        line["cpu_baseline"] = {
+            "value": pats / el if el > 0 else None, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "oracle (C restatement of src/gspan, pinned to the reference binary) on the full generated "
+                      "database at minsup %d, one pass %s after %.1f s: %d patterns" %
+                      (minsup, "stopped" if stopped else "complete", el, pats)}
+    if not a.no_extras and WORLD == 1 and a.config == 5:
+        # the other workloads, each timed the same way (flush, barrier, CUDA events)
+        line["config2"] = config2_sweep(a, g, tm)
+        nb = max(3, min(a.steps, 5))
+        bl = bench_batch(a, g, tm, nb)
+        line["batch"] = {k: bl[k] for k in ("value", "ms_per_step", "steps", "patterns_per_step", "config",
+                                            "autotuned", "lists_strategy", "one_at_a_time", "plain_one_at_a_time",
+                                            "speedup_vs_one_at_a_time", "speedup_vs_plain", "clocks")}
+        sl = bench_serving(a, g, tm)
+        line["serving"] = {k: sl[k] for k in ("value", "config", "streams", "serial_plain_at_200",
+                                              "serial_batched_at_200", "server", "clocks")}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -30,12 +30,21 @@
  *   read_database_cudabin src/globals/dbio.cpp:381-404 + convert_to_host_representation
  *                       src/globals/cuda_graph_types.cpp:268-293
  *
+ *   generate            the seeded benchmark databases (configurations 1-5),
+ *                       the same bytes as the GPU miner's generator writes
+ *
  * Usage: gspan_oracle <txt|fsg|bin|cudabin> <file> <abs-minsup> [out|-] [--max-edges N]
- *        [--graph-limit G] [--time-limit SECONDS] [--roots i/n]
+ *        [--graph-limit G] [--time-limit SECONDS] [--roots i/n] [--repeat K]
+ *        gspan_oracle gen <config[,seed[,scale]]> <abs-minsup> [same options]
+ *        gspan_oracle --write-gen <config[,seed[,scale]]> <out.txt>
+ *        gspan_oracle --gen-count <config[,seed[,scale]]>
  * --time-limit stops the traversal after that many seconds (a bounded sample
  * for timing; the output is then a prefix of the full output).  --roots i/n
  * mines only the frequent root edges whose index is i modulo n (independent
- * subtrees; the union over i = 0..n-1 is the full output).
+ * subtrees; the union over i = 0..n-1 is the full output).  --repeat K mines
+ * K times over one load (timing samples).  `gen` mines a generated database
+ * without a file; --write-gen writes one as txt; --gen-count prints its
+ * graph count.
  * Output: one line per frequent pattern, "<code>\t<support>", in the
  * reference's traversal order; codes use the reference's sequential-miner
  * convention (fromlabel -1 after the first edge, tolabel -1 on backward edges).
@@ -48,6 +57,7 @@
 #include <string.h>
 #include <stdint.h>
 #include <time.h>
+#include <math.h>
 
 /* ------------------------------------------------------------------ graphs */
 
@@ -374,6 +384,369 @@ static int read_bin_db(const char *path, odb *db, int graph_limit)
   }
   fclose(f);
   return 0;
+}
+
+/* ------------------------------------------------------- seeded generator */
+
+/* The seeded synthetic databases of the benchmark configurations 1-5, made
+ * here so that the timed CPU arm and the full-size pins read no file written
+ * by the GPU miner's library.  The stream is xoshiro256** seeded through
+ * splitmix64 (Blackman & Vigna), which gives the same values on every
+ * platform; labels come from cumulative weight tables, Poisson draws from
+ * Knuth's product of uniforms.  A graph is built in the order the txt writer
+ * lists it ("v" lines by vertex, then every edge once, from its lower
+ * endpoint, in the order the endpoint's adjacency holds it), so the graphs
+ * equal what read_text_db makes of the same database written as txt.  A CPU
+ * test checks that the txt this program writes hashes to the committed
+ * checksums and to the GPU miner's generator output. */
+
+typedef struct { uint64_t s[4]; } orng;
+
+static uint64_t splitmix64(uint64_t *x)
+{
+  uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static void rng_seed(orng *r, uint64_t seed)
+{
+  for(int i = 0; i < 4; i++) r->s[i] = splitmix64(&seed);
+}
+
+static uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static uint64_t rng_next(orng *r)
+{
+  uint64_t *s = r->s;
+  uint64_t out = rotl64(s[1] * 5, 7) * 9;
+  uint64_t t = s[1] << 17;
+  s[2] ^= s[0]; s[3] ^= s[1]; s[1] ^= s[2]; s[0] ^= s[3];
+  s[2] ^= t; s[3] = rotl64(s[3], 45);
+  return out;
+}
+
+/* 53 random bits in [0, 1) */
+static double rng_uniform(orng *r) { return (double)(rng_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+
+/* inclusive range */
+static int64_t rng_range(orng *r, int64_t lo, int64_t hi)
+{
+  return lo + (int64_t)(rng_next(r) % (uint64_t)(hi - lo + 1));
+}
+
+static int rng_poisson(orng *r, double mean)
+{
+  double lim = exp(-mean), p = 1.0;
+  int k = 0;
+  do { k++; p *= rng_uniform(r); } while(p > lim);
+  return k - 1;
+}
+
+typedef struct { double cdf[128]; int n; } ocat;
+
+static void cat_set(ocat *c, const double *w, int n)
+{
+  double s = 0;
+  c->n = n;
+  for(int i = 0; i < n; i++) { s += w[i]; c->cdf[i] = s; }
+  for(int i = 0; i < n; i++) c->cdf[i] /= s;
+}
+
+/* first index whose cumulative weight is >= u, clamped to the last */
+static int cat_draw(const ocat *c, orng *r)
+{
+  double u = rng_uniform(r);
+  int lo = 0, hi = c->n;
+  while(lo < hi) {
+    int mid = (lo + hi) / 2;
+    if(c->cdf[mid] < u) lo = mid + 1; else hi = mid;
+  }
+  return lo < c->n ? lo : c->n - 1;
+}
+
+typedef struct {
+  int64_t n_graphs;
+  int mode;               /* 0: spanning tree + ring edges; 1: embedded seed patterns */
+  int vmin, vmax;         /* mode 0 vertex count range */
+  double ring_per_vertex;
+  double mean_edges;      /* mode 1: edge budget ~ Poisson(mean) */
+  int n_vlabels;
+  double vzipf;           /* 0 = uniform */
+  int n_elabels;
+  double eweights[8];
+  int n_eweights;
+  int n_seeds;
+  double seed_mean_edges;
+  int seed_min_edges, seed_max_edges;  /* max 0 = unbounded */
+  double seed_cover;
+  uint64_t seed;
+} ogen;
+
+/* a small graph under construction: edges in creation order, per-vertex
+ * neighbour lists for the adjacency test */
+typedef struct {
+  int nv, vcap, ne, ecap;
+  int *vl, *ef, *et, *el;
+  int **nb, *nbn, *nbcap;
+} sgraph;
+
+static void sg_clear(sgraph *s) { s->nv = 0; s->ne = 0; }
+
+static int sg_vertex(sgraph *s, int label)
+{
+  if(s->nv == s->vcap) {
+    int nc = s->vcap ? 2 * s->vcap : 32;
+    s->vl = xrealloc(s->vl, sizeof(int) * nc);
+    s->nb = xrealloc(s->nb, sizeof(int *) * nc);
+    s->nbn = xrealloc(s->nbn, sizeof(int) * nc);
+    s->nbcap = xrealloc(s->nbcap, sizeof(int) * nc);
+    for(int i = s->vcap; i < nc; i++) { s->nb[i] = 0; s->nbcap[i] = 0; }
+    s->vcap = nc;
+  }
+  s->vl[s->nv] = label;
+  s->nbn[s->nv] = 0;
+  return s->nv++;
+}
+
+static int sg_adjacent(const sgraph *s, int a, int b)
+{
+  for(int i = 0; i < s->nbn[a]; i++) if(s->nb[a][i] == b) return 1;
+  return 0;
+}
+
+static void sg_nb_push(sgraph *s, int a, int b)
+{
+  if(s->nbn[a] == s->nbcap[a]) {
+    s->nbcap[a] = s->nbcap[a] ? 2 * s->nbcap[a] : 8;
+    s->nb[a] = xrealloc(s->nb[a], sizeof(int) * s->nbcap[a]);
+  }
+  s->nb[a][s->nbn[a]++] = b;
+}
+
+static void sg_edge(sgraph *s, int a, int b, int label)
+{
+  if(s->ne == s->ecap) {
+    int nc = s->ecap ? 2 * s->ecap : 64;
+    s->ef = xrealloc(s->ef, sizeof(int) * nc);
+    s->et = xrealloc(s->et, sizeof(int) * nc);
+    s->el = xrealloc(s->el, sizeof(int) * nc);
+    s->ecap = nc;
+  }
+  s->ef[s->ne] = a; s->et[s->ne] = b; s->el[s->ne] = label; s->ne++;
+  sg_nb_push(s, a, b);
+  sg_nb_push(s, b, a);
+}
+
+/* a chord between two distinct non-adjacent vertices, 24 tries at most */
+static int sg_chord(sgraph *s, orng *r, int label)
+{
+  int n = s->nv;
+  if(n < 3) return 0;
+  for(int tries = 0; tries < 24; tries++) {
+    int a = (int)rng_range(r, 0, n - 1), b = (int)rng_range(r, 0, n - 1);
+    if(a == b || sg_adjacent(s, a, b)) continue;
+    sg_edge(s, a, b, label);
+    return 1;
+  }
+  return 0;
+}
+
+static void sg_free(sgraph *s)
+{
+  for(int i = 0; i < s->vcap; i++) free(s->nb[i]);
+  free(s->vl); free(s->ef); free(s->et); free(s->el); free(s->nb); free(s->nbn); free(s->nbcap);
+}
+
+/* Append a generated graph in txt order: vertices, then for every vertex v in
+ * order its incident edges in creation order whose other end is above v.
+ * With `txt` set, also write it as a "t/v/e" graph numbered `gid`. */
+static void sg_emit(const sgraph *s, gbuild *b, odb *db, FILE *txt, int64_t gid)
+{
+  gb_reset(b);
+  for(int v = 0; v < s->nv; v++) gb_vertex(b, v, s->vl[v]);
+  if(txt) {
+    fprintf(txt, "t # %lld\n", (long long)gid);
+    for(int v = 0; v < s->nv; v++) fprintf(txt, "v %d %d\n", v, s->vl[v]);
+  }
+  /* incident edges of v in creation order: scan the edge list once per vertex
+   * would be quadratic; bucket them instead */
+  int *cnt = calloc((size_t)s->nv + 1, sizeof(int));
+  for(int i = 0; i < s->ne; i++) { cnt[s->ef[i] + 1]++; cnt[s->et[i] + 1]++; }
+  for(int v = 0; v < s->nv; v++) cnt[v + 1] += cnt[v];
+  int *inc = xmalloc(sizeof(int) * (2 * (size_t)s->ne + 1));
+  int *pos = xmalloc(sizeof(int) * ((size_t)s->nv + 1));
+  memcpy(pos, cnt, sizeof(int) * (size_t)s->nv);
+  for(int i = 0; i < s->ne; i++) { inc[pos[s->ef[i]]++] = i; inc[pos[s->et[i]]++] = i; }
+  for(int v = 0; v < s->nv; v++)
+    for(int k = cnt[v]; k < cnt[v + 1]; k++) {
+      int i = inc[k];
+      int to = s->ef[i] == v ? s->et[i] : s->ef[i];
+      if(to > v) {
+        gb_edge(b, v, to, s->el[i]);
+        if(txt) fprintf(txt, "e %d %d %d\n", v, to, s->el[i]);
+      }
+    }
+  free(cnt); free(inc); free(pos);
+  if(db) db_push(db, b);
+}
+
+static void generate(const ogen *p, odb *db, FILE *txt)
+{
+  orng r;
+  rng_seed(&r, p->seed);
+  ocat vcat, ecat;
+  {
+    double w[128];
+    for(int i = 0; i < p->n_vlabels; i++) w[i] = p->vzipf > 0 ? 1.0 / pow((double)(i + 1), p->vzipf) : 1.0;
+    cat_set(&vcat, w, p->n_vlabels);
+    double e[128];
+    for(int i = 0; i < p->n_elabels; i++) e[i] = p->n_eweights == p->n_elabels ? p->eweights[i] : 1.0;
+    cat_set(&ecat, e, p->n_elabels);
+  }
+  gbuild b;
+  memset(&b, 0, sizeof(b));
+  sgraph s;
+  memset(&s, 0, sizeof(s));
+  if(p->mode == 0) {
+    for(int64_t g = 0; g < p->n_graphs; g++) {
+      sg_clear(&s);
+      int nv = (int)rng_range(&r, p->vmin, p->vmax);
+      for(int v = 0; v < nv; v++) sg_vertex(&s, cat_draw(&vcat, &r));
+      for(int v = 1; v < nv; v++) {
+        /* the edge label is drawn before the parent vertex */
+        int lab = cat_draw(&ecat, &r);
+        int a = (int)rng_range(&r, 0, v - 1);
+        sg_edge(&s, a, v, lab);
+      }
+      double x = nv * p->ring_per_vertex;
+      int extra = (int)floor(x + rng_uniform(&r));
+      for(int i = 0; i < extra; i++) { int lab = cat_draw(&ecat, &r); sg_chord(&s, &r, lab); }
+      sg_emit(&s, &b, db, txt, g);
+    }
+  } else {
+    sgraph *seeds = calloc((size_t)(p->n_seeds > 0 ? p->n_seeds : 1), sizeof(sgraph));
+    for(int i = 0; i < p->n_seeds; i++) {
+      int ne = rng_poisson(&r, p->seed_mean_edges);
+      if(ne < p->seed_min_edges) ne = p->seed_min_edges;
+      if(p->seed_max_edges > 0 && ne > p->seed_max_edges) ne = p->seed_max_edges;
+      sgraph *sp = &seeds[i];
+      sg_vertex(sp, cat_draw(&vcat, &r));
+      for(int e = 0; e < ne; e++) {
+        if(sp->nv >= 3 && rng_uniform(&r) < 0.25) {
+          int lab = cat_draw(&ecat, &r);
+          if(sg_chord(sp, &r, lab)) continue;
+        }
+        int a = (int)rng_range(&r, 0, sp->nv - 1);
+        int bv = sg_vertex(sp, cat_draw(&vcat, &r));
+        sg_edge(sp, a, bv, cat_draw(&ecat, &r));
+      }
+    }
+    int *first = 0;
+    int nfirst = 0, capfirst = 0;
+    for(int64_t g = 0; g < p->n_graphs; g++) {
+      int budget = rng_poisson(&r, p->mean_edges);
+      if(budget < 1) budget = 1;
+      sg_clear(&s);
+      nfirst = 0;
+      int covered = 0;
+      while(p->n_seeds > 0 && covered < p->seed_cover * budget) {
+        const sgraph *sp = &seeds[rng_range(&r, 0, p->n_seeds - 1)];
+        int base = s.nv;
+        if(nfirst == capfirst) { capfirst = capfirst ? 2 * capfirst : 64; first = xrealloc(first, sizeof(int) * capfirst); }
+        first[nfirst++] = base;
+        for(int v = 0; v < sp->nv; v++) sg_vertex(&s, sp->vl[v]);
+        for(int e = 0; e < sp->ne; e++) sg_edge(&s, base + sp->ef[e], base + sp->et[e], sp->el[e]);
+        covered += sp->ne;
+      }
+      if(s.nv == 0) {
+        sg_vertex(&s, cat_draw(&vcat, &r));
+        if(nfirst == capfirst) { capfirst = capfirst ? 2 * capfirst : 64; first = xrealloc(first, sizeof(int) * capfirst); }
+        first[nfirst++] = 0;
+      }
+      int used = covered;
+      /* link the copies into one connected graph */
+      for(int c = 1; c < nfirst; c++) {
+        int lo = first[c];
+        int hi = c + 1 < nfirst ? first[c + 1] - 1 : s.nv - 1;
+        int a = (int)rng_range(&r, lo, hi);
+        int bv = (int)rng_range(&r, 0, lo - 1);
+        sg_edge(&s, a, bv, cat_draw(&ecat, &r));
+        used++;
+      }
+      /* the rest of the budget: new leaves and chords */
+      while(used < budget) {
+        int leaf = rng_uniform(&r) < 0.5;
+        if(!leaf) { int lab = cat_draw(&ecat, &r); leaf = !sg_chord(&s, &r, lab); }
+        if(leaf) {
+          int a = (int)rng_range(&r, 0, s.nv - 1);
+          int bv = sg_vertex(&s, cat_draw(&vcat, &r));
+          sg_edge(&s, a, bv, cat_draw(&ecat, &r));
+        }
+        used++;
+      }
+      sg_emit(&s, &b, db, txt, g);
+    }
+    free(first);
+    for(int i = 0; i < p->n_seeds; i++) sg_free(&seeds[i]);
+    free(seeds);
+  }
+  sg_free(&s);
+  free(b.vlabel); free(b.ef); free(b.et); free(b.el);
+}
+
+static int64_t scaled_count(int64_t n, double scale)
+{
+  int64_t v = llround((double)n * scale);
+  return v > 1 ? v : 1;
+}
+
+/* The five benchmark configurations; seed 0 picks the configuration's
+ * default seed.  Returns -1 for an unknown configuration. */
+static int gen_config(int config, uint64_t seed, double scale, ogen *p)
+{
+  memset(p, 0, sizeof(*p));
+  p->n_graphs = 340; p->vmin = 10; p->vmax = 60; p->ring_per_vertex = 0.05; p->mean_edges = 30.0;
+  p->n_vlabels = 5; p->n_elabels = 5; p->n_seeds = 50; p->seed_mean_edges = 4.0; p->seed_min_edges = 1;
+  p->seed_cover = 0.5; p->seed = 1;
+  switch(config) {
+  case 1:  /* stands in for testdata/Chemical_340 */
+    p->mode = 0; p->n_graphs = scaled_count(340, scale); p->vmin = 10; p->vmax = 60; p->ring_per_vertex = 0.05;
+    p->n_vlabels = 66; p->vzipf = 1.5; p->n_elabels = 4;
+    p->eweights[0] = 0.6; p->eweights[1] = 0.3; p->eweights[2] = 0.08; p->eweights[3] = 0.02; p->n_eweights = 4;
+    p->seed = seed ? seed : 1;
+    return 0;
+  case 2:  /* stands in for the PAFI T100000E5PL4P50TL30V5 database */
+    p->mode = 1; p->n_graphs = scaled_count(100000, scale); p->mean_edges = 30; p->n_vlabels = 5; p->n_elabels = 5;
+    p->seed = seed ? seed : 2;
+    return 0;
+  case 3: {  /* one database of the 64-database batch: sizes and alphabets from its seed */
+    orng r;
+    rng_seed(&r, seed ? seed : 1000);
+    double lg = log(1000.0) + rng_uniform(&r) * (log(50000.0) - log(1000.0));
+    p->mode = 1; p->n_graphs = scaled_count(llround(exp(lg)), scale);
+    p->n_vlabels = (int)rng_range(&r, 2, 20); p->n_elabels = (int)rng_range(&r, 2, 20);
+    p->mean_edges = 10.0 + 30.0 * rng_uniform(&r);
+    p->seed = seed ? seed : 1000;
+    return 0;
+  }
+  case 4: {  /* one of the 8 resident serving databases */
+    orng r;
+    rng_seed(&r, seed ? seed : 2000);
+    double lg = log(10000.0) + rng_uniform(&r) * (log(200000.0) - log(10000.0));
+    p->mode = 1; p->n_graphs = scaled_count(llround(exp(lg)), scale);
+    p->seed = seed ? seed : 2000;
+    return 0;
+  }
+  case 5:  /* large single database */
+    p->mode = 1; p->n_graphs = scaled_count(1000000, scale); p->mean_edges = 40; p->n_vlabels = 10; p->vzipf = 1.2;
+    p->n_elabels = 3; p->n_seeds = 200; p->seed_mean_edges = 5.5; p->seed_min_edges = 3; p->seed_max_edges = 8;
+    p->seed = seed ? seed : 5;
+    return 0;
+  default:
+    return -1;
+  }
 }
 
 /* ---------------------------------------------------------------- DFS code */
@@ -895,36 +1268,85 @@ static void run(ominer *m)
   free(roots.x);
 }
 
+/* "config[,seed[,scale]]" -> generator parameters */
+static int parse_gen(const char *spec, ogen *p)
+{
+  int config = 0;
+  unsigned long long seed = 0;
+  double scale = 1.0;
+  char tail;
+  int n = sscanf(spec, "%d,%llu,%lf%c", &config, &seed, &scale, &tail);
+  if(n < 1 || n > 3 || scale <= 0) return -1;
+  return gen_config(config, (uint64_t)seed, scale, p);
+}
+
+static double elapsed_s(const struct timespec *a, const struct timespec *b)
+{
+  return (b->tv_sec - a->tv_sec) + 1e-9 * (b->tv_nsec - a->tv_nsec);
+}
+
 int main(int argc, char **argv)
 {
+  if(argc == 3 && strcmp(argv[1], "--gen-count") == 0) {
+    /* the graph count of a generated database, without generating it */
+    ogen p;
+    if(parse_gen(argv[2], &p) != 0) { fprintf(stderr, "bad generator spec %s\n", argv[2]); return 1; }
+    printf("%lld\n", (long long)p.n_graphs);
+    return 0;
+  }
+  if(argc == 4 && strcmp(argv[1], "--write-gen") == 0) {
+    /* write a generated database as txt and exit */
+    ogen p;
+    if(parse_gen(argv[2], &p) != 0) { fprintf(stderr, "bad generator spec %s\n", argv[2]); return 1; }
+    FILE *f = fopen(argv[3], "w");
+    if(!f) { fprintf(stderr, "cannot open %s\n", argv[3]); return 4; }
+    generate(&p, 0, f);
+    fclose(f);
+    return 0;
+  }
   if(argc < 4) {
-    fprintf(stderr, "usage: %s <txt|fsg|bin|cudabin> <file> <abs-minsup> [out|-] [--max-edges N] [--graph-limit G] [--time-limit S]\n", argv[0]);
+    fprintf(stderr, "usage: %s <txt|fsg|bin|cudabin|gen> <file|config[,seed[,scale]]> <abs-minsup> [out|-] "
+                    "[--max-edges N] [--graph-limit G] [--time-limit S] [--roots i/n] [--repeat K]\n"
+                    "       %s --write-gen <config[,seed[,scale]]> <out.txt>\n"
+                    "       %s --gen-count <config[,seed[,scale]]>\n", argv[0], argv[0], argv[0]);
     return 1;
   }
   const char *ft = argv[1];
   if(ft[0] == '-') ft++;
   const char *outpath = 0;
-  int max_edges = 0, graph_limit = 0;
+  int max_edges = 0, graph_limit = 0, repeat = 1;
   double time_limit = 0;
   int root_part = 0, root_parts = 1;
   for(int i = 4; i < argc; i++) {
     if(strcmp(argv[i], "--max-edges") == 0 && i + 1 < argc) max_edges = atoi(argv[++i]);
     else if(strcmp(argv[i], "--graph-limit") == 0 && i + 1 < argc) graph_limit = atoi(argv[++i]);
     else if(strcmp(argv[i], "--time-limit") == 0 && i + 1 < argc) time_limit = atof(argv[++i]);
+    else if(strcmp(argv[i], "--repeat") == 0 && i + 1 < argc) repeat = atoi(argv[++i]);
     else if(strcmp(argv[i], "--roots") == 0 && i + 1 < argc) {
       if(sscanf(argv[++i], "%d/%d", &root_part, &root_parts) != 2 || root_parts < 1 || root_part < 0 ||
          root_part >= root_parts) { fprintf(stderr, "bad --roots i/n\n"); return 1; }
     }
     else outpath = argv[i];
   }
+  if(repeat < 1) { fprintf(stderr, "bad --repeat\n"); return 1; }
   odb db = { 0, 0, 0 };
   int rc;
+  struct timespec tl0, tl1;
+  clock_gettime(CLOCK_MONOTONIC, &tl0);
   if(strcmp(ft, "txt") == 0) rc = read_text_db(argv[2], 0, &db, graph_limit);
   else if(strcmp(ft, "fsg") == 0) rc = read_text_db(argv[2], 1, &db, graph_limit);
   else if(strcmp(ft, "cudabin") == 0) rc = read_cudabin_db(argv[2], &db, graph_limit);
   else if(strcmp(ft, "bin") == 0) rc = read_bin_db(argv[2], &db, graph_limit);
+  else if(strcmp(ft, "gen") == 0) {
+    ogen p;
+    if(parse_gen(argv[2], &p) != 0) { fprintf(stderr, "bad generator spec %s\n", argv[2]); return 1; }
+    if(graph_limit > 0 && p.n_graphs > graph_limit) p.n_graphs = graph_limit;
+    generate(&p, &db, 0);
+    rc = 0;
+  }
   else { fprintf(stderr, "unknown filetype\n"); return 1; }
   if(rc != 0) { fprintf(stderr, "cannot read database %s\n", argv[2]); return 4; }
+  clock_gettime(CLOCK_MONOTONIC, &tl1);
   int minsup = atoi(argv[3]);
   if(minsup >= db.n) {
     fprintf(stderr, "error: user specified support %d is greater then the database size %d\n", minsup, db.n);
@@ -946,13 +1368,27 @@ int main(int argc, char **argv)
     m.out = fopen(outpath, "w");
     if(!m.out) { fprintf(stderr, "cannot open %s\n", outpath); return 4; }
   }
-  struct timespec t0, t1;
-  clock_gettime(CLOCK_MONOTONIC, &t0);
-  m.t0 = t0;
-  run(&m);
-  clock_gettime(CLOCK_MONOTONIC, &t1);
-  double secs = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
-  if(m.out && m.out != stdout) fclose(m.out);
-  fprintf(stderr, "total_time=%.6f total_frequent_graphs=%.0f%s\n", secs, m.count, m.stopped ? " stopped=time_limit" : "");
+  {
+    long long nv = 0, na = 0;
+    for(int i = 0; i < db.n; i++) { nv += db.g[i].nv; na += db.g[i].off[db.g[i].nv]; }
+    fprintf(stderr, "load_time=%.6f graphs=%d vertices=%lld adjacency_entries=%lld\n", elapsed_s(&tl0, &tl1), db.n,
+            nv, na);
+  }
+  /* --repeat K mines the database K times (one timing line each, output
+   * written on the first pass only), so that timed samples share one load */
+  for(int rep = 0; rep < repeat; rep++) {
+    struct timespec t0, t1;
+    m.count = 0;
+    m.stopped = 0;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    m.t0 = t0;
+    run(&m);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    if(rep == 0 && m.out && m.out != stdout) { fclose(m.out); m.out = 0; }
+    if(rep == 0 && m.out == stdout) { fflush(stdout); m.out = 0; }
+    fprintf(stderr, "total_time=%.6f total_frequent_graphs=%.0f%s\n", elapsed_s(&t0, &t1), m.count,
+            m.stopped ? " stopped=time_limit" : "");
+    fflush(stderr);
+  }
   return 0;
 }

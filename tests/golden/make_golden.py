@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference.
 
-Run in a container that holds the reference tree (default /root/reference,
-or REF=...).  It
+Run where the reference tree is present (REF=<path>; by default a checkout
+named "reference" beside this repository).  It
   * builds the reference's own sequential gSpan (src/gspan) from its sources
     through oracle/Makefile (`make -C oracle ref` -> oracle/_ref/gspan_ref),
   * reads the reference's test sources as text to recover their vectors:
@@ -31,7 +31,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("REF", os.path.abspath(os.path.join(REPO, "..", "reference")))
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "gspan_ref")
 REF_CONVERT = os.path.join(REPO, "oracle", "_ref", "convertdb_ref")
 

@@ -1,6 +1,7 @@
 """CPU tests: the oracle against the reference's golden vectors, the C ABI's
 exports, canonicality KATs, database I/O and the generators.  No GPU call."""
 import hashlib
+import json
 import os
 import re
 import subprocess
@@ -9,7 +10,8 @@ import pytest
 
 from conftest import GOLDEN, REPO, golden_runs, read_lines, run_oracle
 
-REF_TREE = os.environ.get("REF", "/root/reference")
+# the reference tree: $REF, by default a checkout named "reference" beside this repository
+REF_TREE = os.environ.get("REF", os.path.abspath(os.path.join(REPO, "..", "reference")))
 
 
 def test_header_symbols_exported(gs):
@@ -166,6 +168,51 @@ def test_generator_deterministic(gs, tmp_path):
     gs.Database.generate(1, seed=1).write(c)
     assert hashlib.sha256(open(c, "rb").read()).hexdigest() == \
         hashlib.sha256(open(os.path.join(GOLDEN, "cfg1_seed1.txt"), "rb").read()).hexdigest()
+
+
+@pytest.mark.parametrize("config,seed,scale", [(1, 1, 1.0), (2, 0, 0.01), (2, 9, 0.005), (3, 1000, 0.05),
+                                               (3, 1041, 0.02), (4, 2003, 0.01), (5, 0, 0.002), (5, 77, 0.001)])
+def test_oracle_generator_matches_product_generator(gs, oracle, tmp_path, config, seed, scale):
+    # the oracle makes the benchmark databases itself (the timed CPU arm and
+    # the full-size pins load nothing of the package): same bytes as txt
+    a, b = str(tmp_path / "o.txt"), str(tmp_path / "p.txt")
+    subprocess.check_call([oracle, "--write-gen", "%d,%d,%r" % (config, seed, scale), a])
+    gs.Database.generate(config, seed=seed, scale=scale).write(b)
+    assert open(a, "rb").read() == open(b, "rb").read()
+    n = int(subprocess.check_output([oracle, "--gen-count", "%d,%d,%r" % (config, seed, scale)], text=True))
+    assert n == len(gs.Database.generate(config, seed=seed, scale=scale))
+
+
+def test_oracle_generator_matches_pinned_checksums(oracle, tmp_path):
+    # the committed configuration-1 fixture and the full-size databases'
+    # checksums in the pin tables (configuration 2: 100,000 graphs)
+    p = str(tmp_path / "c1.txt")
+    subprocess.check_call([oracle, "--write-gen", "1", p])
+    assert open(p, "rb").read() == open(os.path.join(GOLDEN, "cfg1_seed1.txt"), "rb").read()
+    rows = [r.split("\t") for r in read_lines(os.path.join(GOLDEN, "fullsize.tsv")) if not r.startswith("#")]
+    for c, seed, scale, dbsha in {tuple(r[:4]) for r in rows if r[0] == "2"}:
+        subprocess.check_call([oracle, "--write-gen", "%s,%s,%s" % (c, seed, scale), p])
+        assert hashlib.sha256(open(p, "rb").read()).hexdigest() == dbsha
+
+
+def test_oracle_gen_input_equals_txt_input(oracle, tmp_path):
+    p = str(tmp_path / "d.txt")
+    subprocess.check_call([oracle, "--write-gen", "2,4,0.01", p])
+    assert run_oracle(oracle, "gen", "2,4,0.01", 30) == run_oracle(oracle, "txt", p, 30)
+
+
+def test_reference_arm_loads_nothing_of_the_package(oracle):
+    # bench.py --impl reference times the oracle only: the package (and its
+    # native library) must not be imported in that process
+    code = ("import runpy, sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--scale', '0.002', "
+            "'--steps', '2', '--warmup', '1', '--ref-seconds', '0.2']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "assert not [m for m in sys.modules if m.startswith('gpu_graph_mining_gb300')], 'package imported'")
+    r = subprocess.run(["python", "-c", code], cwd=REPO, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["steps"] == 2
+    assert line["config"]["graphs"] == 2000 and line["config"]["minsup"] == 10
 
 
 def test_generator_shapes(gs):
