@@ -84,7 +84,8 @@ class MineStats(ctypes.Structure):
                 ("host_build_ms", ctypes.c_double), ("host_wait_ms", ctypes.c_double),
                 ("host_select_ms", ctypes.c_double), ("host_emit_ms", ctypes.c_double),
                 ("min_host_checks", ctypes.c_int64), ("list_entries", ctypes.c_int64),
-                ("join_nodes", ctypes.c_int64)]
+                ("join_nodes", ctypes.c_int64), ("sel_bytes", ctypes.c_int64), ("sel_ms", ctypes.c_double),
+                ("min_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -86,6 +86,9 @@ void fill_stats(const gsgb::MineStats &s, gs_mine_stats *o)
   o->min_host_checks = s.min_host;
   o->list_entries = s.list_entries;
   o->join_nodes = s.join_nodes;
+  o->sel_bytes = s.sel_bytes;
+  o->sel_ms = s.sel_ms;
+  o->min_ms = s.min_ms;
 }
 
 struct BatchCtx {
@@ -144,6 +147,7 @@ gs_db *gs_db_from_arrays_device(int32_t db_size, int32_t edges_sizes, int32_t ma
                                 int32_t vertex_count, const int32_t *edges, const int32_t *edges_labels,
                                 const int32_t *vertex_labels, const int32_t *vertex_offsets, gs_status *status)
 {
+  gsgb::DeviceScope device_scope;
   (void)vertex_count;
   if(db_size < 0 || edges_sizes < 0 || max_graph_vertex_count < 0 ||
      (edges_sizes > 0 && (!edges || !edges_labels)) || !vertex_offsets ||
@@ -179,6 +183,7 @@ gs_db *gs_db_generate(int32_t config, uint64_t seed, double scale, gs_status *st
 
 gs_status gs_db_write(const gs_db *db, const char *path, int32_t filetype)
 {
+  gsgb::DeviceScope device_scope;
   if(!db || !path) return set_err(GS_ERR_USAGE, "null argument");
   try {
     const_cast<gs_db *>(db)->d.ensure_host();
@@ -232,6 +237,7 @@ gs_status gs_db_get_info(const gs_db *db, gs_db_info *info)
 
 gs_status gs_db_upload(gs_db *db)
 {
+  gsgb::DeviceScope device_scope;
   if(!db) return set_err(GS_ERR_USAGE, "null database");
   try {
     db->d.upload();
@@ -241,7 +247,11 @@ gs_status gs_db_upload(gs_db *db)
   return GS_OK;
 }
 
-void gs_db_free(gs_db *db) { delete db; }
+void gs_db_free(gs_db *db)
+{
+  gsgb::DeviceScope device_scope;
+  delete db;
+}
 
 void gs_mine_opts_default(gs_mine_opts *o)
 {
@@ -264,6 +274,7 @@ void gs_mine_opts_default(gs_mine_opts *o)
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,
                      gs_mine_stats *stats)
 {
+  gsgb::DeviceScope device_scope;
   if(!db) return set_err(GS_ERR_USAGE, "null database");
   std::vector<gsgb::MineJob> jobs(1);
   gsgb::MineOptions mo;
@@ -314,6 +325,7 @@ gs_status gs_mine(gs_db *db, int32_t abs_minsup, int32_t max_edges, gs_emit_fn e
 gs_status gs_mine_batch(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, const gs_mine_opts *opts,
                         gs_batch_emit_fn emit, void *user, gs_mine_stats *stats)
 {
+  gsgb::DeviceScope device_scope;
   if(n < 0 || (n > 0 && (!dbs || !abs_minsups))) return set_err(GS_ERR_USAGE, "invalid batch");
   gsgb::MineOptions mo;
   fill_opts(opts, mo);
@@ -341,6 +353,7 @@ gs_status gs_mine_batch(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups
 gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, gs_mine_opts *opts,
                       gs_tune_report *report)
 {
+  gsgb::DeviceScope device_scope;
   if(n <= 0 || !dbs || !abs_minsups || !opts) return set_err(GS_ERR_USAGE, "invalid autotune arguments");
   gsgb::MineOptions mo;
   fill_opts(opts, mo);
@@ -380,6 +393,7 @@ gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, 
 gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids, int64_t n_records, int32_t n_keys,
                            int32_t n_graphs, int32_t *support)
 {
+  gsgb::DeviceScope device_scope;
   std::string err;
   int rc = gsgb::support_count_host(keys, graph_ids, n_records, n_keys, n_graphs, support, err);
   if(rc != 0) return set_err(rc, err);
@@ -389,6 +403,7 @@ gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids, int64_
 gs_status gs_filter_backward(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
                              const int32_t *dfs, int32_t *out, int64_t *n_out)
 {
+  gsgb::DeviceScope device_scope;
   std::string err;
   int rc = gsgb::filter_backward_host(column, n_rows, records, n_records, dfs, out, n_out, err);
   if(rc != 0) return set_err(rc, err);
@@ -409,7 +424,11 @@ int32_t gs_dfs_code_is_min(const int32_t *d, int32_t n)
   return checker.is_min(code.data(), n) ? 1 : 0;
 }
 
-void gs_engine_reset(void) { gsgb::engine_reset(); }
+void gs_engine_reset(void)
+{
+  gsgb::DeviceScope device_scope;
+  gsgb::engine_reset();
+}
 
 void gs_engine_set_pool_bytes(int64_t bytes) { gsgb::engine_set_pool_bytes(bytes); }
 

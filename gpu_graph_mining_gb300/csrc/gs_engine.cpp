@@ -657,6 +657,7 @@ constexpr int kHeadFlags = 1;     // consistency flags after the count pass
 constexpr int kHeadSelected = 2;  // selected candidates   } counters of
 constexpr int kHeadExt = 3;       // embeddings of all keys } the support
 constexpr int kHeadListed = 4;    // keys counted          } selection
+constexpr int kHeadSelBytes = 5;  // algorithmic bytes     }
 constexpr size_t kHeadBytes = 64;
 
 // Device scratch and pinned mirrors of one wave in flight.  Two of them let
@@ -688,8 +689,8 @@ struct WaveCtx {
   HBuf<ChildOut> h_outs;
   HBuf<long long> h_keyword;
   HBuf<unsigned long long> h_misc;  // [0] records written, [1] consistency flags, [2..3] = d_selc
-  // 0/1 count, 1/2 support, 3 results copied, 4/5 materialise
-  cudaEvent_t ev[6] = {};
+  // 0/1 count, 1/6 selection, 6/2 canonicality, 3 results copied, 4/5 materialise
+  cudaEvent_t ev[7] = {};
   bool have_events = false;
   std::vector<WaveGraph> graphs;
 
@@ -1377,6 +1378,7 @@ private:
       CK(cudaEventRecord(X.ev[1], E.stream));
       CK(q.screen.run(E.stream));
       CK(q.listed.run(E.stream));
+      CK(cudaEventRecord(X.ev[6], E.stream));
       if(q.with_min) CK(q.ismin.run(E.stream));
       CK(cudaEventRecord(X.ev[2], E.stream));
       CK(cudaMemcpyAsync(q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost, E.stream));
@@ -1398,7 +1400,7 @@ private:
       cudaGraph_t g;
       CK(cudaGraphCreate(&g, 0));
       G->g = g;
-      cudaGraphNode_t e0, e1, e2, e3, last;
+      cudaGraphNode_t e0, e1, e2, e3, e6, last;
       CK(cudaGraphAddMemcpyNode1D(&G->h2d, g, nullptr, 0, q.desc_dst, q.desc_src, q.desc_bytes,
                                   cudaMemcpyHostToDevice));
       CK(cudaGraphAddMemsetNode(&G->mz, g, &G->h2d, 1, &mz));
@@ -1408,7 +1410,8 @@ private:
       CK(cudaGraphAddEventRecordNode(&e1, g, &G->count, 1, X.ev[1]));
       CK(cudaGraphAddKernelNode(&G->screen, g, &e1, 1, &ks));
       CK(cudaGraphAddKernelNode(&G->listed, g, &G->screen, 1, &kl));
-      last = G->listed;
+      CK(cudaGraphAddEventRecordNode(&e6, g, &G->listed, 1, X.ev[6]));
+      last = e6;
       if(q.with_min) {
         CK(cudaGraphAddKernelNode(&G->ismin, g, &last, 1, &km));
         last = G->ismin;
@@ -1692,6 +1695,8 @@ private:
     }
     st_.count_ms += ms_between(X.ev[0], X.ev[1]);
     st_.support_ms += ms_between(X.ev[1], X.ev[2]);
+    st_.sel_ms += ms_between(X.ev[1], X.ev[6]);
+    st_.min_ms += ms_between(X.ev[6], X.ev[2]);
     std::vector<int32_t> &nodes = f.nodes;
     std::vector<NodeLayout> &lays = f.lays;
     const NodeDesc *hn = f.hn;
@@ -1701,6 +1706,7 @@ private:
     const int64_t nsel = (int64_t)hh[kHeadSelected];
     const long long nrec = f.rec ? (long long)hh[kHeadRecords] : -1;
     st_.extensions += (int64_t)hh[kHeadExt];
+    st_.sel_bytes += (int64_t)hh[kHeadSelBytes];
     // the count kernel's bytes per extension (bitmap word and counter, and the
     // record when records are on), counted here rather than in its inner loop
     st_.count_bytes += (int64_t)hh[kHeadExt] * (8 + (f.rec ? 16 : 0));

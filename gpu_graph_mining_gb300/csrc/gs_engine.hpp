@@ -33,6 +33,28 @@ enum Status {
   ST_ERR_STATE = 12,
 };
 
+// The library runs its device work on device 0: one GPU per process (a
+// process that wants another GPU restricts CUDA_VISIBLE_DEVICES).  Every C-ABI
+// entry point that touches the device holds a DeviceScope for the call: device
+// 0 is made current, and the caller's thread gets back the device it had.
+struct DeviceScope {
+  int prev = -1;
+  DeviceScope()
+  {
+    if(cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+    if(prev != 0) cudaSetDevice(0);
+  }
+  ~DeviceScope()
+  {
+    if(prev > 0) cudaSetDevice(prev);
+  }
+  DeviceScope(const DeviceScope &) = delete;
+  DeviceScope &operator=(const DeviceScope &) = delete;
+};
+
 struct Error : public std::runtime_error {
   int code;
   Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
@@ -134,6 +156,9 @@ struct MineStats {
   int64_t min_host = 0;      // candidates whose canonicality was checked on the host
   int64_t list_entries = 0;  // lists strategy: per-row list entries built
   int64_t join_nodes = 0;    // lists strategy: nodes extended through a join
+  int64_t sel_bytes = 0;     // algorithmic bytes of the selection kernels (screen, count listed)
+  double sel_ms = 0;         // summed kernel time of the selection kernels
+  double min_ms = 0;         // summed kernel time of the GPU canonicality checks
 };
 
 struct MineJob {

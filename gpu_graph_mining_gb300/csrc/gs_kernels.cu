@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  unsigned long long ext = 0;
+  unsigned long long ext = 0, bytes = 0;
   // the consistency flags so far (the count pass has finished) travel back
   // with the wave's results
   if(blockIdx.x == 0 && threadIdx.x == 0) *err_copy = *err;
@@ -239,6 +239,7 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
       } else {
         c = (int)c64;
       }
+      bytes += 4ull * (unsigned)cnt_copies;  // the counter copies read
     }
     int n = 0;
     bool cand = false;
@@ -248,6 +249,7 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
       ext += (unsigned long long)c;
       n = find_node_by_key(nodes, nnodes, key);
       cand = c >= nodes[n].minsup;
+      bytes += lnode ? 8 : 4;  // child map (and list node) reset
     }
     if(cand && cnt_copies > 1) {
       // a key that may be materialised: copy 0 keeps the total, copy q >= 1
@@ -259,7 +261,9 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
         run += x;
       }
       cnt[key] = c;
+      bytes += 4ull * (unsigned)cnt_copies;  // the copies turned into offsets
     }
+    if(cand) bytes += 8;  // the listed entry
     const unsigned m = __ballot_sync(full, cand);
     if(m) {
       unsigned long long at = 0;
@@ -268,8 +272,12 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
       if(cand) listed[at + __popc(m & lanemask_lt())] = make_int2(key, n);
     }
   }
-  for(int o = 16; o > 0; o >>= 1) ext += __shfl_down_sync(full, ext, o);
+  for(int o = 16; o > 0; o >>= 1) {
+    ext += __shfl_down_sync(full, ext, o);
+    bytes += __shfl_down_sync(full, bytes, o);
+  }
   if(lane == 0 && ext) atomicAdd(&counters[1], ext);
+  if(lane == 0 && bytes) atomicAdd(&counters[3], bytes);
 }
 
 __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restrict__ nodes,
@@ -299,6 +307,9 @@ __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restr
       if(w < nd.words) bmx[wbase + w] = running + incl - pc;
       running += __shfl_sync(full, incl, 31);
     }
+    // algorithmic bytes: the listed entry, each bitmap word read and its
+    // prefix written, and for a selected key its word offset, result and counter
+    if(lane == 0) atomicAdd(&counters[3], 8ull + 8ull * (unsigned)nd.words + (running >= nd.minsup ? 32ull : 0ull));
     if(lane == 0 && running >= nd.minsup) {
       keyword[kn.x] = wbase;
       const unsigned long long at = atomicAdd(&counters[0], 1ull);

@@ -27,9 +27,7 @@ constexpr int kBlock = 256;
 // The scratch shared by every call on a device.
 static __device__ __align__(256) uint32_t g_noalloc_bitmap[kScratchWords];
 
-// Device address of g_noalloc_bitmap per device, looked up once per device.
 std::mutex g_mu;
-uint32_t *g_addr[kMaxDevices] = {};
 
 }  // namespace
 
@@ -75,39 +73,82 @@ __global__ void k_count(const uint32_t *__restrict__ bm, int n_keys, int words, 
   }
 }
 
-int grid_for(long long n)
+// Per device: the scratch's device address and the SM count, looked up once.
+struct DevInfo {
+  uint32_t *addr = nullptr;
+  int sms = 0;
+};
+DevInfo g_dev[kMaxDevices];
+
+int grid_for(long long n, int sms)
 {
   long long b = (n + kBlock - 1) / kBlock;
   if(b < 1) b = 1;
-  return (int)(b < 152LL * 8 ? b : 152LL * 8);
+  const long long cap = 8LL * sms;  // 8 blocks of 256 threads per SM, grid-stride beyond
+  return (int)(b < cap ? b : cap);
 }
 
-// Address of the scratch on the current device; the first call per device
-// resolves it with cudaGetSymbolAddress (which may load the module).
-gs_status scratch_address(uint32_t **out)
-{
-  int dev = 0;
-  if(cudaGetDevice(&dev) != cudaSuccess) {
-    cudaGetLastError();
-    t_msg = "gs_support_count_noalloc: no current CUDA device";
-    return GS_ERR_CUDA;
+// Restores the calling thread's current device on every return path.
+struct CurrentDevice {
+  int prev = -1;
+  bool changed = false;
+  bool set(int dev)
+  {
+    if(cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+    if(prev == dev) return true;
+    if(cudaSetDevice(dev) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    changed = prev >= 0;
+    return true;
   }
+  ~CurrentDevice()
+  {
+    if(changed) cudaSetDevice(prev);
+  }
+};
+
+// The device that owns `p` (device or managed memory), or -1.
+int device_of(const void *p)
+{
+  cudaPointerAttributes a;
+  if(cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  if(a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return -1;
+  return a.device;
+}
+
+// Scratch address and SM count of device `dev`, which must be current.  The
+// first call per device resolves the address with cudaGetSymbolAddress
+// (which may load the module) and caches it for the life of the process.
+gs_status device_info(int dev, DevInfo *out)
+{
   if(dev < 0 || dev >= kMaxDevices) {
     t_msg = "gs_support_count_noalloc: device index out of range";
     return GS_ERR_LIMIT;
   }
   std::lock_guard<std::mutex> g(g_mu);
-  if(!g_addr[dev]) {
+  DevInfo &d = g_dev[dev];
+  if(!d.addr) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_bitmap);
-    if(e != cudaSuccess || !p) {
+    int sms = 0;
+    if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if(e != cudaSuccess || !p || sms <= 0) {
       cudaGetLastError();
       t_msg = "gs_support_count_noalloc: cudaGetSymbolAddress of the scratch failed";
       return GS_ERR_CUDA;
     }
-    g_addr[dev] = (uint32_t *)p;
+    d.sms = sms;
+    d.addr = (uint32_t *)p;
   }
-  *out = g_addr[dev];
+  *out = d;
   return GS_OK;
 }
 
@@ -128,17 +169,58 @@ extern "C" gs_status gs_support_count_noalloc(const int32_t *d_keys, const int32
     t_msg = "gs_support_count_noalloc: n_keys * ceil(n_graphs/32) exceeds the 1048576-word (4 MiB) scratch";
     return GS_ERR_LIMIT;
   }
-  uint32_t *bm = nullptr;
-  gs_status st = scratch_address(&bm);
-  if(st != GS_OK) return st;
+  // The work runs on the device that holds d_support; the stream must belong to it.
+  const int dev = device_of(d_support);
+  if(dev < 0) {
+    t_msg = "gs_support_count_noalloc: d_support is not device memory";
+    return GS_ERR_USAGE;
+  }
   cudaStream_t s = (cudaStream_t)stream;
+  CurrentDevice cur;
+  if(!cur.set(dev)) {
+    t_msg = "gs_support_count_noalloc: cannot make the device of d_support current";
+    return GS_ERR_CUDA;
+  }
+  if(s) {
+    int sdev = -1;
+    if(cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+      cudaGetLastError();
+      t_msg = "gs_support_count_noalloc: invalid stream";
+      return GS_ERR_USAGE;
+    }
+    if(sdev != dev) {
+      t_msg = "gs_support_count_noalloc: the stream belongs to another device than d_support";
+      return GS_ERR_USAGE;
+    }
+  }
+  // An error left pending by the caller's earlier work is reported as such
+  // and left in place (peek, not get), so a launch error below is this call's.
+  const cudaError_t pending = cudaPeekAtLastError();
+  if(pending != cudaSuccess) {
+    t_msg = "gs_support_count_noalloc: an earlier CUDA error is pending; nothing was launched";
+    return GS_ERR_CUDA;
+  }
+  DevInfo di;
+  gs_status st = device_info(dev, &di);
+  if(st != GS_OK) return st;
+  uint32_t *bm = di.addr;
   const long long nw = (long long)n_keys * words;
-  k_clear<<<grid_for(nw), kBlock, 0, s>>>(bm, nw);
-  if(n_records > 0)
-    k_mark<<<grid_for(n_records), kBlock, 0, s>>>(bm, d_keys, d_graph_ids, n_records, n_keys, n_graphs, (int)words);
-  k_count<<<grid_for((long long)n_keys * 32), kBlock, 0, s>>>(bm, n_keys, (int)words, d_support);
+  k_clear<<<grid_for(nw, di.sms), kBlock, 0, s>>>(bm, nw);
   if(cudaGetLastError() != cudaSuccess) {
-    t_msg = "gs_support_count_noalloc: kernel launch failed";
+    t_msg = "gs_support_count_noalloc: launch of the scratch clear failed";
+    return GS_ERR_CUDA;
+  }
+  if(n_records > 0) {
+    k_mark<<<grid_for(n_records, di.sms), kBlock, 0, s>>>(bm, d_keys, d_graph_ids, n_records, n_keys, n_graphs,
+                                                          (int)words);
+    if(cudaGetLastError() != cudaSuccess) {
+      t_msg = "gs_support_count_noalloc: launch of the record marking failed";
+      return GS_ERR_CUDA;
+    }
+  }
+  k_count<<<grid_for((long long)n_keys * 32, di.sms), kBlock, 0, s>>>(bm, n_keys, (int)words, d_support);
+  if(cudaGetLastError() != cudaSuccess) {
+    t_msg = "gs_support_count_noalloc: launch of the popcount failed";
     return GS_ERR_CUDA;
   }
   return GS_OK;

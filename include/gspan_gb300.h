@@ -11,6 +11,13 @@
  * the database readers of src/globals/dbio.hpp:9-37 and the output sink
  * graph_output::output_graph(const DFSCode&, size_t support)
  * (src/globals/graph_output.hpp:12).
+ *
+ * Device: the miner, the database uploads and ingests, gs_support_count and
+ * gs_filter_backward run on CUDA device 0 of the process (one GPU per
+ * process; choose the GPU with CUDA_VISIBLE_DEVICES).  Each such call makes
+ * device 0 current for its duration and gives the calling thread back the
+ * device it had current.  gs_support_count_noalloc runs on the device of its
+ * output buffer instead.
  */
 #ifndef GSPAN_GB300_H
 #define GSPAN_GB300_H
@@ -211,6 +218,9 @@ typedef struct gs_mine_stats {
   int64_t min_host_checks; /* candidates whose canonicality was checked on the host */
   int64_t list_entries;    /* GS_EXTENSION_LISTS: parent-row list entries built */
   int64_t join_nodes;      /* GS_EXTENSION_LISTS: DFS-tree nodes extended through a join */
+  int64_t sel_bytes;       /* algorithmic bytes of the candidate selection kernels */
+  double sel_ms;           /* summed device time of the candidate selection kernels */
+  double min_ms;           /* summed device time of the GPU canonicality checks */
 } gs_mine_stats;
 
 GS_API void gs_mine_opts_default(gs_mine_opts *opts);
@@ -363,16 +373,21 @@ GS_API gs_status gs_support_count(const int32_t *keys, const int32_t *graph_ids,
  * exits; it must hold n_keys * ceil(n_graphs / 32) 32-bit words, at most
  * GS_NOALLOC_MAX_BITMAP_WORDS (1,048,576), else the call returns
  * GS_ERR_LIMIT and launches nothing.  Records whose key or graph id is out of
- * range are ignored.  Work is queued on `stream` (a cudaStream_t; NULL = the
- * default stream) and the call returns without synchronising; support is
- * ready when the stream reaches that point.
+ * range are ignored.  The work runs on the device that holds d_support (the
+ * caller's current device is restored before returning); `stream` (a
+ * cudaStream_t; NULL = the default stream) must belong to that device, else
+ * GS_ERR_USAGE.  The call queues the work and returns without synchronising;
+ * support is ready when the stream reaches that point.  A CUDA error left
+ * pending by earlier work of the calling thread is reported as GS_ERR_CUDA
+ * before anything is launched, and left in place for its owner.
  *
  * The first call on each device looks up the scratch's device address
- * (cudaGetSymbolAddress, which may load the module): make that first call
- * before any stream capture.  Every call shares the one scratch array and
- * clears the part it uses before use, so calls that may overlap on the GPU
- * (different streams, or threads without ordering) race and give wrong
- * results: serialise them. */
+ * (cudaGetSymbolAddress, which may load the module) and keeps it for the life
+ * of the process: make that first call before any stream capture, and do not
+ * call it again after cudaDeviceReset (the kept address is then stale).
+ * Every call shares the one scratch array and clears the part it uses before
+ * use, so calls that may overlap on the GPU (different streams, or threads
+ * without ordering) race and give wrong results: serialise them. */
 #define GS_NOALLOC_MAX_BITMAP_WORDS (1u << 20)
 GS_API gs_status gs_support_count_noalloc(const int32_t *d_keys, const int32_t *d_graph_ids, int64_t n_records,
                                           int32_t n_keys, int32_t n_graphs, int32_t *d_support, void *stream);
