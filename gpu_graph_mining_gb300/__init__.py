@@ -32,7 +32,7 @@ EXPORTS = [
     "gs_db_generate", "gs_db_convert",
     "gs_db_write", "gs_db_size", "gs_db_get_info", "gs_db_upload", "gs_db_free", "gs_mine_opts_default",
     "gs_mine", "gs_mine_ex", "gs_mine_collect", "gs_patterns_free", "gs_mine_batch", "gs_support_count",
-    "gs_filter_backward",
+    "gs_filter_backward", "gs_segmented_scan", "gs_segmented_reduce",
     "gs_support_count_noalloc",
     "gs_dfs_code_is_min", "gs_engine_reset", "gs_engine_set_pool_bytes",
     "gs_server_opts_default", "gs_server_create", "gs_server_add_db", "gs_server_submit", "gs_server_poll",
@@ -187,6 +187,11 @@ def lib():
     L.gs_support_count.restype = i32
     L.gs_filter_backward.argtypes = [pi32, i64, pi32, i64, pi32, pi32, ctypes.POINTER(i64)]
     L.gs_filter_backward.restype = i32
+    pu32 = ctypes.POINTER(ctypes.c_uint32)
+    L.gs_segmented_scan.argtypes = [pu32, i64, i32, pu32]
+    L.gs_segmented_scan.restype = i32
+    L.gs_segmented_reduce.argtypes = [pu32, i64, pu32, pu32, i32, i32, pu32, ctypes.POINTER(i64)]
+    L.gs_segmented_reduce.restype = i32
     L.gs_support_count_noalloc.argtypes = [vp, vp, i64, i32, i32, vp, vp]
     L.gs_support_count_noalloc.restype = i32
     L.gs_dfs_code_is_min.argtypes = [pi32, i32]
@@ -466,6 +471,33 @@ def filter_backward(column, records, dfs):
     n_out = ctypes.c_int64(0)
     _check(lib().gs_filter_backward(col, n, rec, len(records), d, out, ctypes.byref(n_out)))
     return [(out[2 * i], out[2 * i + 1]) for i in range(n_out.value)]
+
+
+def segmented_scan(data, exclusive=False):
+    """The reference's packed segmented scan on the GPU: bit 31 of a value
+    starts a segment; returns the unpacked running sums (uint32)."""
+    n = len(data)
+    arr = (ctypes.c_uint32 * max(1, n))(*[int(x) & 0xffffffff for x in data])
+    out = (ctypes.c_uint32 * max(1, n))()
+    _check(lib().gs_segmented_scan(arr, n, 1 if exclusive else 0, out))
+    return list(out)[:n]
+
+
+def segmented_reduce(data, segment_count, segment_sizes, exclusive=False):
+    """The reference's segmented reduction: the segmented scan at the last
+    element of each segment, segments given as runs of equal sizes."""
+    n = len(data)
+    arr = (ctypes.c_uint32 * max(1, n))(*[int(x) & 0xffffffff for x in data])
+    g = len(segment_count)
+    if len(segment_sizes) != g:
+        raise ValueError("segment_count and segment_sizes differ in length")
+    cnt = (ctypes.c_uint32 * max(1, g))(*segment_count)
+    siz = (ctypes.c_uint32 * max(1, g))(*segment_sizes)
+    m = sum(int(c) for c in segment_count)
+    res = (ctypes.c_uint32 * max(1, m))()
+    nr = ctypes.c_int64(0)
+    _check(lib().gs_segmented_reduce(arr, n, cnt, siz, g, 1 if exclusive else 0, res, ctypes.byref(nr)))
+    return list(res)[:nr.value]
 
 
 def dfs_code_is_min(code):

@@ -410,6 +410,40 @@ gs_status gs_filter_backward(const int32_t *column, int64_t n_rows, const int32_
   return GS_OK;
 }
 
+gs_status gs_segmented_scan(const uint32_t *data, int64_t n, int32_t exclusive, uint32_t *out)
+{
+  gsgb::DeviceScope device_scope;
+  std::string err;
+  int rc = gsgb::segmented_scan_host(data, n, nullptr, 0, exclusive != 0, out, err);
+  if(rc != 0) return set_err(rc, err);
+  return GS_OK;
+}
+
+gs_status gs_segmented_reduce(const uint32_t *data, int64_t n, const uint32_t *segment_count,
+                              const uint32_t *segment_sizes, int32_t groups, int32_t exclusive, uint32_t *results,
+                              int64_t *n_results)
+{
+  gsgb::DeviceScope device_scope;
+  if(groups < 0 || (groups > 0 && (!segment_count || !segment_sizes)) || !n_results)
+    return set_err(GS_ERR_USAGE, "invalid arguments");
+  // the last element of every segment, group by group
+  std::vector<int64_t> ends;
+  int64_t at = 0;
+  for(int32_t gi = 0; gi < groups; gi++)
+    for(uint32_t c = 0; c < segment_count[gi]; c++) {
+      at += segment_sizes[gi];
+      if(segment_sizes[gi] == 0 || at > n) return set_err(GS_ERR_USAGE, "the segments do not fit the array");
+      ends.push_back(at - 1);
+    }
+  *n_results = (int64_t)ends.size();
+  if(ends.empty()) return GS_OK;
+  if(!results) return set_err(GS_ERR_USAGE, "null results");
+  std::string err;
+  int rc = gsgb::segmented_scan_host(data, n, ends.data(), (int64_t)ends.size(), exclusive != 0, results, err);
+  if(rc != 0) return set_err(rc, err);
+  return GS_OK;
+}
+
 int32_t gs_dfs_code_is_min(const int32_t *d, int32_t n)
 {
   if(!d || n < 1 || n > gsgb::kMaxPatternEdges) return -1;

@@ -2313,6 +2313,66 @@ int filter_backward_host(const int32_t *column, int64_t n_rows, const int32_t *r
   return rc;
 }
 
+// The reference's segmented scan / reduce over packed uint32 arrays
+// (cuda_segmented_scan::scan, cuda_segmented_reduction::reduce,
+// src/reduction/cuda_segmented_scan.hpp, cuda_segmented_reduction.cpp:
+// 98-134): one device pass each, host arrays in and out.
+int segmented_scan_host(const uint32_t *data, int64_t n, const int64_t *ends, int64_t n_ends, int exclusive,
+                        uint32_t *out, std::string &err)
+{
+  if(n < 0 || n_ends < 0 || (n > 0 && !data) || (n_ends > 0 && (!ends || !out)) || (n_ends == 0 && n > 0 && !out)) {
+    err = "invalid arguments";
+    return ST_ERR_USAGE;
+  }
+  if(n >= (int64_t)INT32_MAX) {
+    err = "more than 2^31 - 2 elements";
+    return ST_ERR_LIMIT;
+  }
+  for(int64_t j = 0; j < n_ends; j++)
+    if(ends[j] < 0 || ends[j] >= n) {
+      err = "segment end " + std::to_string(j) + " is outside the array";
+      return ST_ERR_USAGE;
+    }
+  if(n == 0) return ST_OK;
+  std::lock_guard<std::mutex> g(g_mu);
+  char *blk = nullptr;
+  cudaStream_t s = nullptr;
+  int rc = ST_OK;
+  try {
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_x = 0, o_scr = o_x + al(4 * (size_t)n);
+    const size_t o_ends = o_scr + al(4 * (size_t)segmented_scan_scratch(n));
+    const size_t o_res = o_ends + al(8 * (size_t)std::max<int64_t>(n_ends, 1));
+    const size_t o_err = o_res + al(4 * (size_t)std::max<int64_t>(n_ends, 1)), total = o_err + al(4);
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaMalloc(&blk, total));
+    uint32_t *x = (uint32_t *)(blk + o_x);
+    unsigned int *derr = (unsigned int *)(blk + o_err);
+    CK(cudaMemcpyAsync(x, data, 4 * (size_t)n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(derr, 0, 4, s));
+    launch_segmented_scan(x, n, exclusive, (int32_t *)(blk + o_scr), x, s);
+    unsigned int herr = 0;
+    if(n_ends > 0) {
+      CK(cudaMemcpyAsync(blk + o_ends, ends, 8 * (size_t)n_ends, cudaMemcpyHostToDevice, s));
+      launch_gather_ends(x, n, (const long long *)(blk + o_ends), n_ends, (uint32_t *)(blk + o_res), derr, s);
+      CK(cudaMemcpyAsync(out, blk + o_res, 4 * (size_t)n_ends, cudaMemcpyDeviceToHost, s));
+    } else {
+      CK(cudaMemcpyAsync(out, x, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaMemcpyAsync(&herr, derr, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    if(herr) throw Error(ST_ERR_STATE, "segment end outside the array on the device");
+  } catch(const Error &e) {
+    err = e.what();
+    rc = e.code;
+  }
+  if(s) cudaStreamSynchronize(s);
+  if(blk) cudaFree(blk);
+  if(s) cudaStreamDestroy(s);
+  return rc;
+}
+
 void engine_reset()
 {
   {

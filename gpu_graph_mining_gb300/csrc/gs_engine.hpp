@@ -221,6 +221,11 @@ int support_count_host(const int32_t *keys, const int32_t *gids, int64_t n, int3
 // Backward child column: out = the elements ({vertex, back_link}) of column at
 // the rows named by the records (8 ints each) equal to the backward edge dfs,
 // in row order; *n_out their count (host arrays, GPU work).
+// Segmented scan of packed uint32 values (bit 31 starts a segment): with
+// n_ends == 0 the whole scanned array goes to out[n]; otherwise out[j] =
+// scanned[ends[j]].
+int segmented_scan_host(const uint32_t *data, int64_t n, const int64_t *ends, int64_t n_ends, int exclusive,
+                        uint32_t *out, std::string &err);
 int filter_backward_host(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
                          const int32_t *dfs, int32_t *out, int64_t *n_out, std::string &err);
 

@@ -40,7 +40,7 @@ inline unsigned blocks_for(long long n)
 {
   long long b = (n + kThreads - 1) / kThreads;
   if(b < 1) b = 1;
-  const long long cap = 152LL * 64;
+  const long long cap = 64LL * gsgb::sm_count();
   return (unsigned)(b < cap ? b : cap);
 }
 
@@ -602,7 +602,7 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   {
     // few blocks when the table is block-local: each merges the whole table once
     const bool local = tab <= kSmemTab;
-    const unsigned nb = local ? std::min<unsigned>(blocks_for(V), 152u * 4) : blocks_for(V);
+    const unsigned nb = local ? std::min<unsigned>(blocks_for(V), 4u * (unsigned)gsgb::sm_count()) : blocks_for(V);
     k_pairs_seen<<<nb, kThreads, local ? (size_t)tab : 0, s>>>(off, V, vl, adj_to, el, EL, VL, seen, tab);
   }
   scan_exclusive(seen, prank, tab, sc);

@@ -412,7 +412,7 @@ KernelCall is_min_call(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *sl
   }
   KernelCall c;
   c.func = (const void *)k_is_min;
-  c.grid = dim3(152 * 2);
+  c.grid = dim3((unsigned)(2 * sm_count()));
   c.block = dim3(kMinWarps * 32);
   c.smem = (unsigned)smem;
   c.arg(nodes);

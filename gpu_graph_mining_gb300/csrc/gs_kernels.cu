@@ -11,6 +11,19 @@
 
 namespace gsgb {
 
+int sm_count()
+{
+  static const int n = [] {
+    int v = 0;
+    if(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 152;
+    }
+    return v;
+  }();
+  return n;
+}
+
 namespace {
 
 constexpr int kBlock = 256;
@@ -441,7 +454,7 @@ inline int grid_for(long long n)
 {
   long long b = (n + kBlock - 1) / kBlock;
   if(b < 1) b = 1;
-  const long long cap = 152LL * 16;  // 16 resident CTAs per SM worth of work, grid-stride beyond
+  const long long cap = 16LL * sm_count();  // 16 resident CTAs per SM worth of work, grid-stride beyond
   return (int)(b < cap ? b : cap);
 }
 
@@ -502,7 +515,7 @@ KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const ui
 {
   KernelCall c;
   c.func = (const void *)k_count_listed;
-  c.grid = dim3(152 * 8);
+  c.grid = dim3((unsigned)(8 * sm_count()));
   c.block = dim3(kBlock);
   c.arg(nodes);
   c.arg(listed);
@@ -515,6 +528,89 @@ KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const ui
   c.arg(counters);
   c.arg(lnode);
   return c;
+}
+
+// ---- the reference's packed segmented scan and reduce as single operators
+// (gs_segmented_scan / gs_segmented_reduce).  Element i holds a value in bits
+// 0-30 and, in bit 31, a flag that starts a new segment (element 0 always
+// starts one): the packed layout of src/reduction/segscanpacked.cu.  The
+// segmented scan is two plain scans: one over the values (positions P) and
+// one over the flags (segment numbers); a segment's result is P minus P at
+// its first element.  Sums wrap modulo 2^32 like the reference's uint scans.
+
+__global__ void __launch_bounds__(kBlock) k_seg_split(const uint32_t *__restrict__ x, long long n, int32_t *val,
+                                                     int32_t *pos, int32_t *head, int32_t *seg)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t v = x[i];
+    const int32_t h = (i == 0 || (v >> 31)) ? 1 : 0;
+    val[i] = (int32_t)(v & 0x7fffffffu);
+    pos[i] = (int32_t)(v & 0x7fffffffu);
+    head[i] = h;
+    seg[i] = h;
+  }
+}
+
+// pos, seg: exclusive scans of the values and of the flags
+__global__ void __launch_bounds__(kBlock) k_seg_base(const int32_t *__restrict__ pos, const int32_t *__restrict__ head,
+                                                    const int32_t *__restrict__ seg, long long n, int32_t *base)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    if(head[i]) base[seg[i]] = pos[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_seg_out(const int32_t *__restrict__ val, const int32_t *__restrict__ pos,
+                                                   const int32_t *__restrict__ head, const int32_t *__restrict__ seg,
+                                                   const int32_t *__restrict__ base, long long n, int exclusive,
+                                                   uint32_t *out)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for(long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int32_t s = seg[i] + head[i] - 1;
+    uint32_t r = (uint32_t)pos[i] - (uint32_t)base[s];
+    if(!exclusive) r += (uint32_t)val[i];
+    out[i] = r;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_gather_ends(const uint32_t *__restrict__ scanned,
+                                                       const long long *__restrict__ ends, long long m, long long n,
+                                                       uint32_t *res, unsigned int *err)
+{
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for(long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < m; j += stride) {
+    const long long e = ends[j];
+    if(e < 0 || e >= n) {
+      atomicOr(err, 1u);
+      res[j] = 0;
+    } else {
+      res[j] = scanned[e];
+    }
+  }
+}
+
+int64_t segmented_scan_scratch(int64_t n) { return 5 * n + xscan_scratch(n); }
+
+void launch_segmented_scan(const uint32_t *x, int64_t n, int exclusive, int32_t *scratch, uint32_t *out,
+                           cudaStream_t s)
+{
+  if(n <= 0) return;
+  int32_t *val = scratch, *pos = val + n, *head = pos + n, *seg = head + n, *base = seg + n, *xs = base + n;
+  const int g = grid_for(n);
+  k_seg_split<<<g, kBlock, 0, s>>>(x, n, val, pos, head, seg);
+  xscan(pos, n, xs, s);
+  xscan(seg, n, xs, s);
+  k_seg_base<<<g, kBlock, 0, s>>>(pos, head, seg, n, base);
+  k_seg_out<<<g, kBlock, 0, s>>>(val, pos, head, seg, base, n, exclusive, out);
+}
+
+void launch_gather_ends(const uint32_t *scanned, int64_t n, const long long *ends, int64_t m, uint32_t *res,
+                        unsigned int *err, cudaStream_t s)
+{
+  if(m <= 0) return;
+  k_gather_ends<<<grid_for(m), kBlock, 0, s>>>(scanned, ends, m, n, res, err);
 }
 
 // ---- backward child column on its own (gs_filter_backward)

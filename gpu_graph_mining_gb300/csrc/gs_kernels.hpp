@@ -13,6 +13,9 @@
 
 namespace gsgb {
 
+// SMs of device 0 (the library's device), read once; grid caps are per SM.
+int sm_count();
+
 // Extension records of the count pass, int4 {key field, x, y, graph rank}: the
 // key field holds the wave key in bits 0-26 and the counter copy the
 // extension was counted in in bits 27-30 (-1: an unused slot).  A forward
@@ -149,6 +152,18 @@ struct ListBuild {
   const int32_t *rowbase;
 };
 int64_t list_scan_scratch(int64_t n);
+
+// The reference's packed segmented scan (cuda_segmented_scan::scan,
+// src/reduction/cuda_segmented_scan.hpp): bit 31 of an element starts a new
+// segment, bits 0-30 are its value; out[i] = the sum of the values of i's
+// segment up to i (inclusive) or before i (exclusive), modulo 2^32.
+// scratch: segmented_scan_scratch(n) ints.  out may alias x.
+int64_t segmented_scan_scratch(int64_t n);
+void launch_segmented_scan(const uint32_t *x, int64_t n, int exclusive, int32_t *scratch, uint32_t *out,
+                           cudaStream_t s);
+// res[j] = scanned[ends[j]]; an index outside [0, n) sets bit 0 of *err.
+void launch_gather_ends(const uint32_t *scanned, int64_t n, const long long *ends, int64_t m, uint32_t *res,
+                        unsigned int *err, cudaStream_t s);
 
 // Backward child column on its own (gs_filter_backward; the reference's
 // filter_backward_embeddings, src/gspan_cuda/filter_backward.cpp:288-352):

@@ -440,7 +440,7 @@ template <int KMAX, bool MAT, bool MASK, bool JOIN> void launch_k(const WaveArgs
     configured = true;
   }
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
-  const long long cap = 152LL * GS_WAVE_GRID;
+  const long long cap = (long long)sm_count() * GS_WAVE_GRID;
   if(blocks > cap) blocks = cap;
   if(blocks < 1) blocks = 1;
   k_wave<KMAX, MAT, MASK, JOIN><<<(int)blocks, kWarps * 32, smem, s>>>(a);
@@ -463,21 +463,6 @@ template <bool MAT> void dispatch(int kmax, bool small_graphs, bool join, const 
     if(join) dispatch_k<MAT, false, true>(kmax, a, s);
     else dispatch_k<MAT, false, false>(kmax, a, s);
   }
-}
-
-// SMs of device 0 (the grid caps below are per SM)
-int sm_count()
-{
-  static int n = 0;
-  if(n == 0) {
-    int v = 0;
-    if(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess || v <= 0) {
-      cudaGetLastError();
-      v = 152;
-    }
-    n = v;
-  }
-  return n;
 }
 
 template <int KMAX, bool MASK, bool JOIN> KernelCall count_call_k(const WaveArgs &a, int grid_per_sm)
@@ -617,7 +602,7 @@ void launch_materialize_records(const int4 *rec, long long n, const int32_t *chi
 {
   if(n <= 0) return;
   long long blocks = ((n + 31) / 32 * 32 + 255) / 256;
-  if(blocks > 152LL * 16) blocks = 152LL * 16;
+  if(blocks > 16LL * sm_count()) blocks = 16LL * sm_count();
   const ListBuild lb = lists ? *lists : ListBuild{ nullptr, nullptr, nullptr };
   k_mat_records<<<(int)blocks, 256, 0, s>>>(rec, n, childmap, keyword, bm, bmx, cursor, cursor_stride, outs, bytes,
                                             err, lb, lists ? list_cnt : nullptr);

@@ -414,6 +414,27 @@ GS_API gs_status gs_support_count_noalloc(const int32_t *d_keys, const int32_t *
 GS_API gs_status gs_filter_backward(const int32_t *column, int64_t n_rows, const int32_t *records, int64_t n_records,
                                     const int32_t *dfs, int32_t *out, int64_t *n_out);
 
+/* The reference's segmented scan over packed uint32 values
+ * (cuda_segmented_scan::scan, src/reduction/cuda_segmented_scan.hpp:7-24;
+ * packed layout of src/reduction/segscanpacked.cu): bit 31 of an element
+ * starts a new segment (element 0 always starts one), bits 0-30 are its
+ * value.  out[i] (n values, unpacked) = the sum of the values of i's segment
+ * up to and including i, or before i when `exclusive` is set, modulo 2^32.
+ * Computed on the GPU by two plain scans (values, flags).  Host arrays; out
+ * may alias data.  GS_ERR_LIMIT beyond 2^31 - 2 elements. */
+GS_API gs_status gs_segmented_scan(const uint32_t *data, int64_t n, int32_t exclusive, uint32_t *out);
+
+/* The reference's segmented reduction (cuda_segmented_reduction::reduce,
+ * src/reduction/cuda_segmented_reduction.cpp:98-134): the segments are given
+ * as `groups` runs of segment_count[g] segments of segment_sizes[g] elements
+ * each; results[j] = the segmented scan (inclusive or exclusive) at the last
+ * element of segment j, i.e. the segment's sum (without its last value when
+ * exclusive).  *n_results receives the number of segments; results must hold
+ * that many.  GS_ERR_USAGE when the segments run past the array. */
+GS_API gs_status gs_segmented_reduce(const uint32_t *data, int64_t n, const uint32_t *segment_count,
+                                     const uint32_t *segment_sizes, int32_t groups, int32_t exclusive,
+                                     uint32_t *results, int64_t *n_results);
+
 /* Canonicality of a DFS code (n_edges tuples {from, to, fromlabel, elabel,
  * tolabel}, either label convention): 1 if minimal, 0 if not, -1 on bad
  * input.  Same semantics as the sequential reference's gSpan::is_min
