@@ -1,17 +1,20 @@
-"""Full benchmark sizes, checked through size-independent properties (the
-oracle cannot mine these sizes in test time):
-  * configuration 5 (1,000,000 graphs, 80 M adjacency entries) at minsup 0.5%:
-    repeat runs equal, the GPU and host canonicality checks equal, every
-    support >= minsup, every pattern's one-edge-shorter prefix present with
-    a support at least as large;
+"""Full benchmark sizes against the oracle's pins (tests/golden/fullsize*.tsv,
+made by tests/golden/make_fullsize.py with the oracle mining root-subtree
+shares in parallel), plus properties that need no oracle:
+  * configuration 5 (1,000,000 graphs, 80 M adjacency entries) at minsup
+    0.5%: its pin is checked in test_parity_gpu.py::test_full_size_checksums;
+    here repeat runs are equal, the GPU and host canonicality checks agree,
+    every support >= minsup and every pattern's one-edge-shorter prefix is
+    present with a support at least as large;
   * configuration 3 (64 databases, 916,553 graphs) at minsup 5%: mined as one
-    batch equals each database mined alone, and the oracle agrees on the
-    smallest databases."""
+    batch, every database's output equals the oracle's pinned count and
+    hash, and equals the same database mined alone."""
+import hashlib
 import os
 
 import pytest
 
-from conftest import run_oracle, to_lines
+from conftest import GOLDEN, read_lines, to_lines
 
 pytestmark = pytest.mark.gpu
 
@@ -33,25 +36,35 @@ def test_config5_full_size(gs):
     minsup = 5000
     a, sa = gs.mine_collect(db, minsup)
     b, _ = gs.mine_collect(db, minsup)
-    assert a == b and len(a) > 10000
+    assert a == b and len(a) == 36572
     c, sc = gs.mine_collect(db, minsup, min_check=1)
     assert c == a and sc["min_host_checks"] == sc["candidates"]
     _properties(gs, a, minsup)
     assert sa["min_host_checks"] * 100 <= sa["candidates"]
 
 
-def test_config3_full_batch(gs, oracle, tmp_path):
+def _batch_pins():
+    pins = {}
+    for line in read_lines(os.path.join(GOLDEN, "fullsize_batch.tsv")):
+        if line.startswith("#"):
+            continue
+        c, seed, scale, dbsha, s, n, sha, me = line.split("\t")
+        pins[int(seed)] = (int(s), int(n), sha)
+    return pins
+
+
+def test_config3_full_batch_against_oracle_pins(gs):
+    pins = _batch_pins()
+    assert sorted(pins) == list(range(1000, 1064))
     dbs = [gs.Database.generate(3, seed=1000 + i) for i in range(64)]
     sups = [max(1, int(round(0.05 * len(d)))) for d in dbs]
     batch, st = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ)
     assert st["patterns"] == sum(len(b) for b in batch)
-    for d, s, got in zip(dbs, sups, batch):
+    for i, (d, s, got) in enumerate(zip(dbs, sups, batch)):
+        ps, pn, psha = pins[1000 + i]
+        assert s == ps
+        lines = to_lines(got, gs)
+        assert len(lines) == pn, i
+        assert hashlib.sha256(("\n".join(lines) + "\n").encode()).hexdigest() == psha, i
         solo, _ = gs.mine_collect(d, s, label_style=gs.LABELS_SEQ)
         assert got == solo
-        _properties(gs, got, s)
-    # the oracle on the three smallest databases
-    order = sorted(range(64), key=lambda i: len(dbs[i]))[:3]
-    for i in order:
-        p = str(tmp_path / ("db%d.txt" % i))
-        dbs[i].write(p, "txt")
-        assert to_lines(batch[i], gs) == run_oracle(oracle, "txt", p, sups[i]), i

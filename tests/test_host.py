@@ -195,6 +195,32 @@ def test_oracle_generator_matches_pinned_checksums(oracle, tmp_path):
         assert hashlib.sha256(open(p, "rb").read()).hexdigest() == dbsha
 
 
+def _pin_rows():
+    rows = []
+    for name in ("fullsize.tsv", "fullsize_batch.tsv"):
+        for line in read_lines(os.path.join(GOLDEN, name)):
+            if not line.startswith("#"):
+                c, seed, scale, dbsha = line.split("\t")[:4]
+                rows.append((int(c), int(seed), float(scale), dbsha))
+    return sorted(set(rows))
+
+
+def test_pinned_databases_generated_identically(gs, tmp_path):
+    # the GPU tests regenerate the pinned full-size databases with the
+    # package's generator: the bytes must be the ones the oracle mined
+    rows = _pin_rows()
+    assert len(rows) >= 66  # configurations 2 and 5, the 64 batch databases, the serving databases
+    p = str(tmp_path / "db.txt")
+    for c, seed, scale, dbsha in rows:
+        gs.Database.generate(c, seed=seed, scale=scale).write(p)
+        h = hashlib.sha256()
+        with open(p, "rb") as f:
+            for blk in iter(lambda: f.read(1 << 24), b""):
+                h.update(blk)
+        assert h.hexdigest() == dbsha, (c, seed, scale)
+    os.remove(p)
+
+
 def test_oracle_gen_input_equals_txt_input(oracle, tmp_path):
     p = str(tmp_path / "d.txt")
     subprocess.check_call([oracle, "--write-gen", "2,4,0.01", p])

@@ -233,26 +233,30 @@ def test_filter_backward_random(gs):
         assert gs.filter_backward(col, recs, (4, 0, 9, 9, 9)) == []
 
 
-def _fullsize():
+def _fullsize(name="fullsize.tsv"):
+    """Rows of a pin table: (config, seed, scale, db sha256, minsup, count, output sha256, max edges)."""
     rows = []
-    for line in read_lines(os.path.join(GOLDEN, "fullsize.tsv")):
+    for line in read_lines(os.path.join(GOLDEN, name)):
         if line.startswith("#"):
             continue
-        c, seed, scale, dbsha, s, n, sha = line.split("\t")
-        rows.append((int(c), int(seed), float(scale), dbsha, int(s), int(n), sha))
+        c, seed, scale, dbsha, s, n, sha, me = line.split("\t")
+        rows.append((int(c), int(seed), float(scale), dbsha, int(s), int(n), sha, int(me)))
     return rows
 
 
-@pytest.mark.parametrize("row", _fullsize(), ids=lambda r: "cfg%d-s%d" % (r[0], r[4]))
-def test_full_size_checksums(gs, tmp_path, row):
-    config, seed, scale, dbsha, s, n, sha = row
+def _sha_lines(lines):
+    return hashlib.sha256(("\n".join(lines) + "\n").encode()).hexdigest()
+
+
+@pytest.mark.parametrize("row", _fullsize(), ids=lambda r: "cfg%d-seed%d-s%d-e%d" % (r[0], r[1], r[4], r[7]))
+def test_full_size_checksums(gs, row):
+    # the database bytes behind each pin are checked on the CPU
+    # (test_host.py::test_pinned_databases_generated_identically)
+    config, seed, scale, dbsha, s, n, sha, me = row
     db = gs.Database.generate(config, seed=seed, scale=scale)
-    p = str(tmp_path / "db.txt")
-    db.write(p, "txt")
-    assert hashlib.sha256(open(p, "rb").read()).hexdigest() == dbsha
-    lines, stats = _mine_lines(gs, db, s)
+    lines, stats = _mine_lines(gs, db, s, max_edges=me)
     assert len(lines) == n
-    assert hashlib.sha256(("\n".join(lines) + "\n").encode()).hexdigest() == sha
+    assert _sha_lines(lines) == sha
     # size-independent properties
     sup = {}
     for line in lines:
