@@ -19,6 +19,8 @@
 // Accepts exactly what gs_db_from_arrays accepts (same checks), and the
 // device database is identical to the one the host path uploads.
 #include <algorithm>
+#include <cstdint>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -413,6 +415,37 @@ struct ReadBack {
 
 // Process-wide ingest state: the ingest stream and a copy stream, the
 // scratch pool and the pinned read-back area.  Ingests are serialised by mu.
+// Copies an int32 host array to the device by a kernel that reads the host
+// memory in place: on a GPU that reaches pageable host memory through the
+// host's page tables (address translation services, as over a Grace C2C
+// link) this reads at the link's bandwidth with no driver staging through
+// pinned buffers, so it neither waits on host memcpy threads nor varies
+// with them.  16-byte loads when both ends are 16-byte aligned, 4-byte loads
+// otherwise; four loads in flight per thread.
+__global__ void __launch_bounds__(kThreads) k_pull(const int32_t *__restrict__ src, int32_t *__restrict__ dst,
+                                                   long long n, int vec)
+{
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long done = 0;
+  if(vec) {
+    const long long n4 = n / 4;
+    const int4 *s4 = reinterpret_cast<const int4 *>(src);
+    int4 *d4 = reinterpret_cast<int4 *>(dst);
+    long long i = tid;
+    for(; i + 3 * stride < n4; i += 4 * stride) {
+      const int4 a = s4[i], b = s4[i + stride], c = s4[i + 2 * stride], d = s4[i + 3 * stride];
+      d4[i] = a;
+      d4[i + stride] = b;
+      d4[i + 2 * stride] = c;
+      d4[i + 3 * stride] = d;
+    }
+    for(; i < n4; i += stride) d4[i] = s4[i];
+    done = n4 * 4;
+  }
+  for(long long i = done + tid; i < n; i += stride) dst[i] = src[i];
+}
+
 struct IngestCtx {
   std::mutex mu;
   cudaStream_t s = nullptr, s_copy = nullptr;
@@ -421,11 +454,22 @@ struct IngestCtx {
   ReadBack *rb = nullptr;
   int32_t *meta = nullptr;   // pinned: label values, root offsets and pair codes read back
   size_t meta_cap = 0;
+  bool direct = false;       // the GPU reads pageable host memory through the host's page tables
 
   void init()
   {
     if(s) return;
     CK(cudaSetDevice(0));
+    {
+      int pma = 0, ats = 0;
+      if(cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, 0) != cudaSuccess ||
+         cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, 0) != cudaSuccess) {
+        cudaGetLastError();
+        pma = ats = 0;
+      }
+      const char *env = std::getenv("GS_INGEST_MEMCPY");  // 1: always copy through cudaMemcpyAsync
+      direct = pma == 1 && ats == 1 && !(env && env[0] == '1');
+    }
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
     props.location.type = cudaMemLocationTypeDevice;
@@ -451,6 +495,23 @@ struct IngestCtx {
     return meta;
   }
 };
+
+// Host array -> device: the in-place read kernel where the GPU reaches
+// pageable host memory through the host's page tables, else cudaMemcpyAsync.
+void pull_to_device(const IngestCtx &cx, int32_t *dst, const int32_t *src, long long n, cudaStream_t st)
+{
+  if(n <= 0) return;
+  if(!cx.direct) {
+    CK(cudaMemcpyAsync(dst, src, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st));
+    return;
+  }
+  const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+  const long long per = vec ? 16 : 4;  // elements per thread per pass of four loads
+  long long b = (n + (long long)kThreads * per - 1) / ((long long)kThreads * per);
+  b = std::max(1ll, std::min(b, 4ll * gsgb::sm_count()));
+  k_pull<<<(unsigned)b, kThreads, 0, st>>>(src, dst, n, vec);
+  CK(cudaGetLastError());
+}
 
 IngestCtx &ingest_ctx()
 {
@@ -521,15 +582,16 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   } drain{ s, cx.s_copy };
   Scratch sc{ s, cx.pool, {} };
   const long long slots = (long long)G * maxv;
-  // raw arrays up (the reference's copy_to_device).  A copy from pageable
-  // memory returns only when it is done, so the vertex offsets go first and
-  // the per-graph pass is queued behind them before the other arrays are
-  // copied (on the copy stream): the GPU runs the pass while the host is in
-  // those copies.
+  // raw arrays up (the reference's copy_to_device).  The vertex offsets go
+  // first and the per-graph pass is queued behind them before the other
+  // arrays are copied (on the copy stream), so the pass runs during those
+  // copies: with cudaMemcpyAsync from pageable memory a copy returns only
+  // when it is done; with the in-place read kernel (pull_to_device) all of
+  // it is queued at once.
   int32_t *d_edges = sc.get<int32_t>(esz), *d_elab = sc.get<int32_t>(esz);
   int32_t *d_vlab = sc.get<int32_t>(slots), *d_voff = sc.get<int32_t>(slots + 1);
   CK(cudaEventRecord(cx.ev_alloc, s));
-  CK(cudaMemcpyAsync(d_voff, voff, sizeof(int32_t) * (slots + 1), cudaMemcpyHostToDevice, s));
+  pull_to_device(cx, d_voff, voff, slots + 1, s);
   unsigned *flags = sc.get<unsigned>(1);
   CK(cudaMemsetAsync(flags, 0, sizeof(unsigned), s));
 
@@ -544,10 +606,10 @@ void ingest_cudabin_device(Database &db, int32_t G, int32_t esz, int32_t maxv, c
   CK(cudaMemcpyAsync(&rb.flags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamWaitEvent(cx.s_copy, cx.ev_alloc, 0));
   if(esz) {
-    CK(cudaMemcpyAsync(d_edges, edges, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
-    CK(cudaMemcpyAsync(d_elab, elab, sizeof(int32_t) * esz, cudaMemcpyHostToDevice, cx.s_copy));
+    pull_to_device(cx, d_edges, edges, esz, cx.s_copy);
+    pull_to_device(cx, d_elab, elab, esz, cx.s_copy);
   }
-  if(slots) CK(cudaMemcpyAsync(d_vlab, vlab, sizeof(int32_t) * slots, cudaMemcpyHostToDevice, cx.s_copy));
+  if(slots) pull_to_device(cx, d_vlab, vlab, slots, cx.s_copy);
   CK(cudaEventRecord(cx.ev_copied, cx.s_copy));
   sc.after = cx.ev_copied;
   CK(cudaStreamSynchronize(s));
