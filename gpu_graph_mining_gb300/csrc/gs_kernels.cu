@@ -293,6 +293,32 @@ __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restri
   if(lane == 0 && bytes) atomicAdd(&counters[3], bytes);
 }
 
+// A listed key's support: its bitmap words popcounted, their exclusive
+// prefixes written (bmx), the total compared with minsup.  A key of at most
+// kBigWords words is taken by one warp, 4 words per lane per step; a larger
+// one (a key present in up to a million graphs has 31,250 words) by a whole
+// block, 8 words per thread per step, so that its words are not read by one
+// warp in a long chain of dependent steps.
+constexpr int kBigWords = 1024;
+
+__device__ __forceinline__ void listed_done(const int2 kn, const NodeDesc &nd, long long wbase, int running,
+                                            int32_t *cnt, long long *keyword, int4 *sel, int sel_cap,
+                                            unsigned long long *counters, int32_t *lnode)
+{
+  // algorithmic bytes: the listed entry, each bitmap word read and its
+  // prefix written, and for a selected key its word offset, result and counter
+  atomicAdd(&counters[3], 8ull + 8ull * (unsigned)nd.words + (running >= nd.minsup ? 32ull : 0ull));
+  if(running >= nd.minsup) {
+    keyword[kn.x] = wbase;
+    const unsigned long long at = atomicAdd(&counters[0], 1ull);
+    if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], 0);
+    // the total has been read: copy 0 turns into the cursor of copy 0's share
+    cnt[kn.x] = 0;
+    // lists strategy: a frequent forward key goes into its node's per-row lists
+    if(lnode && kn.x - nd.key_base < nd.nfwd) lnode[kn.x] = kn.y;
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restrict__ nodes,
                                                           const int2 *__restrict__ listed,
                                                           const uint32_t *__restrict__ bm,
@@ -301,37 +327,82 @@ __global__ void __launch_bounds__(kBlock) k_count_listed(const NodeDesc *__restr
                                                           unsigned long long *counters, int32_t *lnode)
 {
   const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long nlisted = (long long)counters[2];
+  // small keys: one warp each
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
   for(long long li = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < nlisted; li += warps) {
     const int2 kn = listed[li];
     const NodeDesc &nd = nodes[kn.y];
-    const long long wbase = nd.bm_base + (long long)(kn.x - nd.key_base) * nd.words;
+    const int words = nd.words;
+    if(words > kBigWords) continue;
+    const long long wbase = nd.bm_base + (long long)(kn.x - nd.key_base) * words;
     int running = 0;
-    for(int w0 = 0; w0 < nd.words; w0 += 32) {
-      const int w = w0 + lane;
-      const int pc = (w < nd.words) ? __popc(bm[wbase + w]) : 0;
-      int incl = pc;
-      for(int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(full, incl, o);
-        if(lane >= o) incl += t;
+    for(int w0 = 0; w0 < words; w0 += 128) {
+      const int w = w0 + 4 * lane;
+      int c[4], t = 0;
+#pragma unroll
+      for(int q = 0; q < 4; q++) {
+        c[q] = (w + q < words) ? __popc(bm[wbase + w + q]) : 0;
+        t += c[q];
       }
-      if(w < nd.words) bmx[wbase + w] = running + incl - pc;
+      int incl = t;
+      for(int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(full, incl, o);
+        if(lane >= o) incl += u;
+      }
+      int at = running + incl - t;
+#pragma unroll
+      for(int q = 0; q < 4; q++) {
+        if(w + q < words) bmx[wbase + w + q] = at;
+        at += c[q];
+      }
       running += __shfl_sync(full, incl, 31);
     }
-    // algorithmic bytes: the listed entry, each bitmap word read and its
-    // prefix written, and for a selected key its word offset, result and counter
-    if(lane == 0) atomicAdd(&counters[3], 8ull + 8ull * (unsigned)nd.words + (running >= nd.minsup ? 32ull : 0ull));
-    if(lane == 0 && running >= nd.minsup) {
-      keyword[kn.x] = wbase;
-      const unsigned long long at = atomicAdd(&counters[0], 1ull);
-      if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], 0);
-      // the total has been read: copy 0 turns into the cursor of copy 0's share
-      cnt[kn.x] = 0;
-      // lists strategy: a frequent forward key goes into its node's per-row lists
-      if(lnode && kn.x - nd.key_base < nd.nfwd) lnode[kn.x] = kn.y;
+    if(lane == 0) listed_done(kn, nd, wbase, running, cnt, keyword, sel, sel_cap, counters, lnode);
+  }
+  // large keys: one block each (the branch below is uniform over the block)
+  __shared__ int wtot[kBlock / 32];
+  constexpr int kPer = 8, kStep = kBlock * kPer;
+  for(long long li = blockIdx.x; li < nlisted; li += gridDim.x) {
+    const int2 kn = listed[li];
+    const NodeDesc &nd = nodes[kn.y];
+    const int words = nd.words;
+    if(words <= kBigWords) continue;
+    const long long wbase = nd.bm_base + (long long)(kn.x - nd.key_base) * words;
+    int running = 0;
+    for(int w0 = 0; w0 < words; w0 += kStep) {
+      const int w = w0 + kPer * threadIdx.x;
+      int c[kPer], t = 0;
+#pragma unroll
+      for(int q = 0; q < kPer; q++) {
+        c[q] = (w + q < words) ? __popc(bm[wbase + w + q]) : 0;
+        t += c[q];
+      }
+      int incl = t;
+      for(int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(full, incl, o);
+        if(lane >= o) incl += u;
+      }
+      if(lane == 31) wtot[warp] = incl;
+      __syncthreads();
+      int before = 0, total = 0;
+#pragma unroll
+      for(int x = 0; x < kBlock / 32; x++) {
+        const int v = wtot[x];
+        if(x < warp) before += v;
+        total += v;
+      }
+      int at = running + before + incl - t;
+#pragma unroll
+      for(int q = 0; q < kPer; q++) {
+        if(w + q < words) bmx[wbase + w + q] = at;
+        at += c[q];
+      }
+      running += total;
+      __syncthreads();  // wtot is rewritten by the next step
     }
+    if(threadIdx.x == 0) listed_done(kn, nd, wbase, running, cnt, keyword, sel, sel_cap, counters, lnode);
   }
 }
 

@@ -35,6 +35,7 @@
  *
  * Usage: gspan_oracle <txt|fsg|bin|cudabin> <file> <abs-minsup> [out|-] [--max-edges N]
  *        [--graph-limit G] [--time-limit SECONDS] [--roots i/n] [--repeat K] [--roots-once]
+ *        [--intervals K S]
  *        gspan_oracle gen <config[,seed[,scale]]> <abs-minsup> [same options]
  *        gspan_oracle --write-gen <config[,seed[,scale]]> <out.txt>
  *        gspan_oracle --gen-count <config[,seed[,scale]]>
@@ -43,7 +44,11 @@
  * mines only the frequent root edges whose index is i modulo n (independent
  * subtrees; the union over i = 0..n-1 is the full output).  --repeat K mines
  * K times over one load (timing samples); --roots-once builds the root map
- * (one pass over every graph and a sort of its edges) before them, untimed.  `gen` mines a generated database
+ * (one pass over every graph and a sort of its edges) before them, untimed.
+ * --intervals K S mines for K consecutive windows of S seconds (the
+ * traversal restarting whenever it completes) and reports the cumulative
+ * pattern count at the end of each window: a throughput sample of the whole
+ * traversal, not of its first seconds only.  `gen` mines a generated database
  * without a file; --write-gen writes one as txt; --gen-count prints its
  * graph count.
  * Output: one line per frequent pattern, "<code>\t<support>", in the
@@ -1123,6 +1128,13 @@ typedef struct {
   size_t line_cap;
   oextv roots;         /* the root edges of every graph in root-map order, built once */
   int have_roots;
+  /* interval sampling: patterns reported up to the end of each of nint
+   * consecutive windows of win seconds, counted over passes that restart
+   * when a traversal completes */
+  double win;
+  int nint, icur;
+  double done;         /* patterns of completed passes */
+  double *icount;
 } ominer;
 
 /* support (gspan.cpp:89-103): number of id changes along the projection */
@@ -1156,6 +1168,8 @@ static int out_of_time(ominer *m)
   struct timespec t;
   clock_gettime(CLOCK_MONOTONIC, &t);
   double s = (t.tv_sec - m->t0.tv_sec) + 1e-9 * (t.tv_nsec - m->t0.tv_nsec);
+  /* a window ends: the patterns so far (checked as each DFS-tree node starts) */
+  while(m->icur < m->nint && s >= (m->icur + 1) * m->win) m->icount[m->icur++] = m->done + m->count;
   if(s > m->time_limit) m->stopped = 1;
   return m->stopped;
 }
@@ -1326,7 +1340,8 @@ int main(int argc, char **argv)
   const char *ft = argv[1];
   if(ft[0] == '-') ft++;
   const char *outpath = 0;
-  int max_edges = 0, graph_limit = 0, repeat = 1, roots_once = 0;
+  int max_edges = 0, graph_limit = 0, repeat = 1, roots_once = 0, nint = 0;
+  double win = 0;
   double time_limit = 0;
   int root_part = 0, root_parts = 1;
   for(int i = 4; i < argc; i++) {
@@ -1335,6 +1350,10 @@ int main(int argc, char **argv)
     else if(strcmp(argv[i], "--time-limit") == 0 && i + 1 < argc) time_limit = atof(argv[++i]);
     else if(strcmp(argv[i], "--repeat") == 0 && i + 1 < argc) repeat = atoi(argv[++i]);
     else if(strcmp(argv[i], "--roots-once") == 0) roots_once = 1;
+    else if(strcmp(argv[i], "--intervals") == 0 && i + 2 < argc) {
+      nint = atoi(argv[++i]);
+      win = atof(argv[++i]);
+    }
     else if(strcmp(argv[i], "--roots") == 0 && i + 1 < argc) {
       if(sscanf(argv[++i], "%d/%d", &root_part, &root_parts) != 2 || root_parts < 1 || root_part < 0 ||
          root_part >= root_parts) { fprintf(stderr, "bad --roots i/n\n"); return 1; }
@@ -1395,6 +1414,34 @@ int main(int argc, char **argv)
     build_roots(&m);
     clock_gettime(CLOCK_MONOTONIC, &r1);
     fprintf(stderr, "roots_time=%.6f root_edges=%d\n", elapsed_s(&r0, &r1), m.roots.n);
+  }
+  if(nint > 0) {
+    /* --intervals K S: mine for K windows of S seconds, restarting the
+     * traversal whenever it completes; report the patterns found up to the
+     * end of each window ("intervals=c1,c2,...", cumulative) */
+    if(win <= 0 || nint > 100000) { fprintf(stderr, "bad --intervals\n"); return 1; }
+    m.win = win;
+    m.nint = nint;
+    m.icount = xmalloc(sizeof(double) * nint);
+    m.time_limit = nint * win;
+    m.out = 0;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    m.t0 = t0;
+    int passes = 0;
+    while(!m.stopped) {
+      m.count = 0;
+      run(&m);
+      if(!m.stopped) { m.done += m.count; passes++; }
+      out_of_time(&m);
+      if(!m.stopped && m.count == 0 && passes > 0) break;  /* nothing frequent: no work to sample */
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    for(; m.icur < nint; m.icur++) m.icount[m.icur] = m.done + m.count;
+    fprintf(stderr, "sample_time=%.6f passes_completed=%d intervals=", elapsed_s(&t0, &t1), passes);
+    for(int j = 0; j < nint; j++) fprintf(stderr, "%s%.0f", j ? "," : "", m.icount[j]);
+    fprintf(stderr, "\n");
+    return 0;
   }
   /* --repeat K mines the database K times (one timing line each, output
    * written on the first pass only), so that timed samples share one load */
