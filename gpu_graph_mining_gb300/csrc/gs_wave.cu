@@ -181,7 +181,11 @@ k_wave(const WaveArgs a)
       S.clen[t] = a.collen[nd.col_off + t];
     }
     // ---- phase 1: this lane's row
-    const int i = (int)((tile - nd.tile_begin) * 32) + lane;
+    // the tile's first row within the node (kept in a register: the emission
+    // below stores to global memory, so a reload from the node would not be
+    // hoisted out of the item loop)
+    const int row0 = (int)((tile - nd.tile_begin) * 32);
+    const int i = row0 + lane;
     bool valid = i < nd.nrows;
     int W = 0, g = 0, last_prev = 0;
     // the graph rank is loaded now and checked after the walk, so that the
@@ -390,7 +394,7 @@ k_wave(const WaveArgs a)
             chunk_fill = cntx - room;
           }
           if(key >= 0 && dst >= 0 && dst < a.rec_cap) {
-            const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
+            const int i_o = row0 + o;
             a.rec[dst] = bwd ? make_int4((key_base + key) | rec_tag, S.phi[k - 1][o], S.lp[o], g_o)
                              : make_int4((key_base + key) | rec_tag, w, i_o, g_o);
           }
@@ -409,7 +413,7 @@ k_wave(const WaveArgs a)
           const int rank = a.bmx[wi] + __popc(a.bm[wi] & ((1u << (g_o & 31)) - 1u));
           const ChildOut out = a.outs[c];
           if(pos < out.cap) {
-            const int i_o = (int)((tile - nd.tile_begin) * 32) + o;
+            const int i_o = row0 + o;
             out.col[pos] = bwd ? make_int2(S.phi[k - 1][o], S.lp[o]) : make_int2(w, i_o);
             out.gord[pos] = rank;
           } else {
