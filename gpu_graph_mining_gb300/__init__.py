@@ -52,7 +52,8 @@ class MineOpts(ctypes.Structure):
                 ("wave_rows", ctypes.c_int64), ("wave_words", ctypes.c_int64),
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
                 ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
-                ("count_grid", ctypes.c_int32), ("extension", ctypes.c_int32)]
+                ("count_grid", ctypes.c_int32), ("extension", ctypes.c_int32),
+                ("deep_nodes", ctypes.c_int32)]
 
 
 # extension strategies (gs_mine_opts.extension)
@@ -67,11 +68,11 @@ class ConvertInfo(ctypes.Structure):
 
 class TuneReport(ctypes.Structure):
     _fields_ = [("trials", ctypes.c_int32), ("wave_nodes", ctypes.c_int32), ("wave_rows", ctypes.c_int64),
-                ("count_grid", ctypes.c_int32), ("reserved", ctypes.c_int32), ("base_ms", ctypes.c_double),
+                ("count_grid", ctypes.c_int32), ("deep_nodes", ctypes.c_int32), ("base_ms", ctypes.c_double),
                 ("best_ms", ctypes.c_double)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class MineStats(ctypes.Structure):
@@ -324,7 +325,8 @@ def _extension(x):
 
 
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
-          root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0, extension=EXTENSION_RMPATH):
+          root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0, extension=EXTENSION_RMPATH,
+          deep_nodes=0):
     o = MineOpts()
     lib().gs_mine_opts_default(ctypes.byref(o))
     o.max_edges = int(max_edges)
@@ -343,12 +345,14 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
     o.launch_mode = int(launch_mode)
     o.count_grid = int(count_grid)
     o.extension = _extension(extension)
+    if deep_nodes:
+        o.deep_nodes = int(deep_nodes)
     return o
 
 
 def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
          wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0,
-         extension=EXTENSION_RMPATH):
+         extension=EXTENSION_RMPATH, deep_nodes=0):
     """Mines db at absolute support minsup.
 
     Returns (patterns, stats): patterns is a list of (code, support) with code a
@@ -367,7 +371,7 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
 
     fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
     o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check,
-              launch_mode, count_grid, extension)
+              launch_mode, count_grid, extension, deep_nodes)
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()
@@ -421,7 +425,8 @@ def autotune(dbs, minsups, **kw):
     ms = (ctypes.c_int32 * len(dbs))(*[int(m) for m in minsups])
     r = TuneReport()
     _check(lib().gs_autotune(hs, len(dbs), ms, ctypes.byref(o), ctypes.byref(r)))
-    return {"wave_nodes": o.wave_nodes, "wave_rows": o.wave_rows, "count_grid": o.count_grid}, r.as_dict()
+    return ({"wave_nodes": o.wave_nodes, "wave_rows": o.wave_rows, "count_grid": o.count_grid,
+             "deep_nodes": o.deep_nodes}, r.as_dict())
 
 
 def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True,

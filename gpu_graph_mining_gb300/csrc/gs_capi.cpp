@@ -52,6 +52,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   m.launch_mode = o->launch_mode == 1 ? 1 : 0;
   if(o->count_grid > 0 && o->count_grid <= 1024) m.count_grid = o->count_grid;
   m.extension = o->extension == GS_EXTENSION_LISTS ? 1 : 0;
+  if(o->deep_nodes > 0) m.deep_nodes = o->deep_nodes;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -268,6 +269,7 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->min_check = m.min_check;
   o->launch_mode = m.launch_mode;
   o->count_grid = m.count_grid;
+  o->deep_nodes = m.deep_nodes;
   o->extension = m.extension;
 }
 
@@ -373,16 +375,18 @@ gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, 
   opts->wave_nodes = best.wave_nodes;
   opts->wave_rows = best.wave_rows;
   opts->count_grid = best.count_grid;
+  opts->deep_nodes = best.deep_nodes;
   if(report) {
     report->trials = (int32_t)trials.size();
     report->wave_nodes = best.wave_nodes;
     report->wave_rows = best.wave_rows;
     report->count_grid = best.count_grid;
-    report->reserved = 0;
+    report->deep_nodes = best.deep_nodes;
     report->base_ms = trials.front().ms;
     double b = trials.front().ms;
     for(const auto &t : trials)
-      if(t.wave_nodes == best.wave_nodes && t.wave_rows == best.wave_rows && t.count_grid == best.count_grid)
+      if(t.wave_nodes == best.wave_nodes && t.wave_rows == best.wave_rows && t.count_grid == best.count_grid &&
+         t.deep_nodes == best.deep_nodes)
         b = t.ms;
     report->best_ms = b;
   }

@@ -1081,7 +1081,7 @@ public:
   {
     for(int c = 0; c < nctx_; c++)
       if(!fl_[c].busy) {
-        const bool deep = stacked_ >= std::max(1, wo_.wave_nodes);
+        const bool deep = stacked_ >= (wo_.deep_nodes > 0 ? wo_.deep_nodes : std::max(1, wo_.wave_nodes));
         if(c >= 2 && !deep) continue;
         int idle = 0;
         for(int d = 0; d < nctx_; d++) idle += (!fl_[d].busy && (d < 2 || deep)) ? 1 : 0;
@@ -2155,7 +2155,7 @@ int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptio
       b = std::min(b, st.wall_ms);
     }
     ms = b;
-    trials.push_back(TuneTrial{ o.wave_nodes, o.wave_rows, o.count_grid, ms });
+    trials.push_back(TuneTrial{ o.wave_nodes, o.wave_rows, o.count_grid, o.deep_nodes, ms });
     return ST_OK;
   };
   MineOptions cur = base;
@@ -2189,6 +2189,12 @@ int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptio
     if(cg == cur.count_grid || (cur.count_grid == 0 && cg == 64)) continue;
     MineOptions o = cur;
     o.count_grid = cg;
+    if((rc = consider(o))) return rc;
+  }
+  for(int32_t dn : { 1, 256, 1024 }) {
+    if(dn == cur.deep_nodes) continue;
+    MineOptions o = cur;
+    o.deep_nodes = dn;
     if((rc = consider(o))) return rc;
   }
   best = cur;

@@ -128,6 +128,7 @@ struct MineOptions {
                               // scanned; 1 lists: forward children join their parent's per-row
                               // lists of frequent forward extensions and scan only their new
                               // right-most vertex (the reference's gspan_cuda_lists)
+  int32_t deep_nodes = 0;     // a third wave context launches while this many nodes are queued (0 = wave_nodes)
 };
 
 struct MineStats {
@@ -239,6 +240,7 @@ struct TuneTrial {
   int32_t wave_nodes;
   int64_t wave_rows;
   int32_t count_grid;
+  int32_t deep_nodes;
   double ms;
 };
 int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptions &best,

@@ -187,6 +187,10 @@ typedef struct gs_mine_opts {
                           vertices by joining its parent's frequent forward extensions at the same
                           parent row (extend_embeddings.cpp:206-330, intersection_fwd_fwd) and
                           scans only its new right-most vertex.  Same patterns and supports. */
+  int32_t deep_nodes;  /* a third wave may be in flight (besides two) while at least this many DFS-tree
+                          nodes are queued; 0 = wave_nodes (default), 1 = always.  More waves in flight
+                          hide more of the host's work per wave when a workload has many small nodes;
+                          a short queue split three ways makes smaller waves. */
 } gs_mine_opts;
 
 #define GS_EXTENSION_RMPATH 0
@@ -332,8 +336,8 @@ GS_API void gs_server_destroy(gs_server *srv);
 
 /* Autotuner: picks the wave options for a workload (the databases mined
  * together at their minsups, as gs_mine_batch would).  Coordinate descent
- * over wave_nodes (1024..16384), wave_rows (2^22..2^25) and count_grid
- * (16..96 blocks per SM); every trial is a complete mining pass with the
+ * over wave_nodes (1024..16384), wave_rows (2^22..2^25), count_grid
+ * (16..96 blocks per SM) and deep_nodes (1, 256, 1024); every trial is a complete mining pass with the
  * patterns counted, not emitted, best of two on the host clock, and a value
  * is taken only when it is 2% faster.  opts: in, the starting options (other
  * fields are kept); out, the tuned ones.  No counterpart in the reference,
@@ -343,7 +347,7 @@ typedef struct gs_tune_report {
   int32_t wave_nodes;
   int64_t wave_rows;
   int32_t count_grid;
-  int32_t reserved;
+  int32_t deep_nodes;
   double base_ms;  /* the starting options */
   double best_ms;  /* the tuned options */
 } gs_tune_report;

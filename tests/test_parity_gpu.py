@@ -292,6 +292,19 @@ def test_direct_launches_equal_graph_replay(gs):
     assert a == b and sa["waves"] == sb["waves"]
 
 
+def test_deep_wave_contexts_keep_results(gs):
+    # a third wave in flight whenever anything is queued (deep_nodes=1) changes
+    # how the queue is split into waves, not the patterns
+    dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.03) for i in range(4)]
+    sups = [max(2, int(0.05 * len(d))) for d in dbs]
+    a, sa = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ)
+    b, sb = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, deep_nodes=1, wave_nodes=64)
+    assert a == b and sa["patterns"] == sb["patterns"]
+    lines, _ = _mine_lines(gs, gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt"), 10, deep_nodes=1,
+                           wave_nodes=16)
+    assert lines == read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s10.txt"))
+
+
 def test_autotune_keeps_results(gs):
     dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.05) for i in range(3)]
     sups = [max(2, int(0.05 * len(d))) for d in dbs]
