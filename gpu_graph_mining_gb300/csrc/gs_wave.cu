@@ -153,6 +153,16 @@ k_wave(const WaveArgs a)
     const unsigned long long *__restrict__ adj = dbr.adj;
     const int32_t *__restrict__ adj_off = dbr.adj_off;
     const int32_t *__restrict__ adj_pair = dbr.adj_pair;
+    // The forward key needs the entry's pair index.  When the wave's
+    // adjacency is larger than L2 (no rule skip), the per-entry pair array is
+    // a second random DRAM access per entry (a 32-byte sector for 4 useful
+    // bytes); a small label alphabet's pair table (VL * EL * VL entries) stays
+    // in L1 instead, looked up from the entry's labels for the entries that
+    // become forward extensions.  On configuration 5 this cut the kernel's
+    // DRAM traffic from 1.62 to 1.17 times its algorithmic bytes.
+    const int32_t *__restrict__ ptab =
+        !JOIN && !a.rule_skip && (long long)dbr.VL * dbr.EL * dbr.VL <= 16384 ? dbr.pair_idx : nullptr;
+    const int pEL = dbr.EL, pVL = dbr.VL;
     const int nv = dbr.n_vertices;
     if(k > KMAX || nslot > KMAX || k < 1 || nslot < 1) {
       if(lane == 0) atomicOr(a.err, 2u);
@@ -306,7 +316,7 @@ k_wave(const WaveArgs a)
         } else {
           s_n = s0 + sl;
           ent_n = __ldg(&adj[e]);
-          pr_n = __ldg(&adj_pair[e]);
+          if(!ptab) pr_n = __ldg(&adj_pair[e]);
         }
       }
     };
@@ -346,7 +356,7 @@ k_wave(const WaveArgs a)
           for(int t = 0; t < k; ++t) in_emb |= (S.phi[t][o] == w);
         }
         if(fwd_rules && !in_emb) {
-          key = fko + pr;
+          key = fko + (ptab ? __ldg(&ptab[(S.slot[s].vlab * pEL + (hi >> 16)) * pVL + wl]) : pr);
         } else if(is_r && in_emb) {
           // backward edge from the right-most vertex to a right-most-path vertex
           int jv = -1;
