@@ -615,6 +615,7 @@ def main():
     times, stats_all, pats_local = mine_timed(g, tm, db, minsup, a.steps, 0, kw)
     clk = clocks.stop()
     ms = sum(times) / len(times)
+    config_ms_range = [min(times), max(times)]
     if dist:
         t = torch.tensor([ms, float(pats_local)], device=dev)
         mx = t.clone()
@@ -650,9 +651,10 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": WORLD, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_job, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic", "config": config,
-        "patterns_per_step": pats_job,
+        "patterns_per_step": pats_job, "ms_per_step_range": config_ms_range,
         "e2e": {"value": e2e, "unit": UNIT, "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "steps": len(e2e_times)},
+                "d2h_bytes_per_step": d2h, "steps": len(e2e_times),
+                "ms_min": min(e2e_times), "ms_max": max(e2e_times)},
         "roofline": roof,
         "cpu_baseline": None,
         "clocks": clk,
