@@ -690,6 +690,8 @@ struct WaveCtx {
   HBuf<long long> h_keyword;
   HBuf<unsigned long long> h_misc;  // [0] records written, [1] consistency flags, [2..3] = d_selc
   // 0/1 count, 1/6 selection, 6/2 canonicality, 3 results copied, 4/5 materialise
+  // (root contexts: 0/1 count and support, 3 read back, 5 first embeddings; the
+  // first root context's 6 follows a group of jobs' read-backs)
   cudaEvent_t ev[7] = {};
   bool have_events = false;
   std::vector<WaveGraph> graphs;
@@ -762,7 +764,10 @@ struct Engine {
   DBuf<DevDB> d_dbs;
   DBuf<unsigned long long> d_bytes;   // [0] count bytes, [1] materialise bytes, [2] root bytes, [3] flags
   WaveCtx ctx[kWaveCtx];
-  WaveCtx rootc;
+  // root phases: up to kRootCtx jobs of a batch are counted together, with one
+  // host wait for all of them, each in its own context
+  static constexpr int kRootCtx = 16;
+  WaveCtx rootc[kRootCtx];
   bool ready = false;
 
   void init(int threads)
@@ -775,7 +780,7 @@ struct Engine {
       d_dbs.ensure(kMaxDbSlots);
       CK(cudaMemsetAsync(d_bytes.p, 0, sizeof(unsigned long long) * 4, stream));
       for(auto &c : ctx) c.init();
-      rootc.init();
+      for(auto &r : rootc) r.init();
       ready = true;
     }
     pool.set_limit(pool_limit);
@@ -793,7 +798,7 @@ struct Engine {
     d_dbs.free();
     d_bytes.free();
     for(auto &c : ctx) c.free();
-    rootc.free();
+    for(auto &r : rootc) r.free();
     cudaStreamSynchronize(aux);
     cudaStreamDestroy(aux);
     cudaStreamDestroy(stream);
@@ -1036,6 +1041,26 @@ public:
   // queues its root nodes.  Returns the job id.
   int32_t add(const MineJob &j)
   {
+    const int32_t id = enter(j);
+    root_phase(std::vector<int32_t>{ id });
+    if(jobs_[id]->pending == 0) complete(id);
+    return id;
+  }
+
+  // Several jobs at once: their root levels are counted together.
+  void add_all(const std::vector<MineJob> &js)
+  {
+    std::vector<int32_t> ids;
+    ids.reserve(js.size());
+    for(const MineJob &j : js) ids.push_back(enter(j));
+    root_phase(ids);
+    for(int32_t id : ids)
+      if(jobs_[id]->pending == 0) complete(id);
+  }
+
+  // A job's checks, its database resident and in the device table, its state.
+  int32_t enter(const MineJob &j)
+  {
     if(!j.db) throw Error(ST_ERR_USAGE, "null database");
     if(j.minsup < 1) throw Error(ST_ERR_MINSUP_TOO_SMALL, "error: absolute_min_support < 1");
     if(j.minsup >= j.db->host.n_graphs)
@@ -1070,8 +1095,6 @@ public:
     S.db_slot = slot;
     active_++;
     order_.push_back(id);
-    root_phase(id);
-    if(S.pending == 0) complete(id);
     return id;
   }
 
@@ -1237,11 +1260,32 @@ private:
   }
 
   // ---- root level: all frequent 1-edge codes of one job
-  void root_phase(int32_t id)
+  // The root level of jobs: every root triple's support and embedding count
+  // (one count and one support launch per job), the frequent roots in the
+  // reference's order, and their first embeddings.  The jobs' counts are
+  // queued together and read back after one host wait.
+  void root_phase(const std::vector<int32_t> &ids)
+  {
+    for(size_t i0 = 0; i0 < ids.size(); i0 += Engine::kRootCtx) {
+      const size_t i1 = std::min(ids.size(), i0 + (size_t)Engine::kRootCtx);
+      for(size_t i = i0; i < i1; i++) root_count(ids[i], E.rootc[i - i0]);
+      {
+        // one event behind every job's read-back (a job without root keys
+        // queues nothing, so no job's own event can stand for the others)
+        CK(cudaEventRecord(E.rootc[0].ev[6], E.stream));
+        const clk::time_point t0 = clk::now();
+        CK(cudaEventSynchronize(E.rootc[0].ev[6]));
+        st_.host_wait_ms += ms_since(t0);
+      }
+      CK(cudaGetLastError());
+      for(size_t i = i0; i < i1; i++) root_children(ids[i], E.rootc[i - i0]);
+    }
+  }
+
+  void root_count(int32_t id, WaveCtx &X)
   {
     JobState &S = *jobs_[id];
     Database &db = *S.job.db;
-    WaveCtx &X = E.rootc;
     const int32_t words = words_for(db.host.n_graphs);
     const int32_t R = db.root_keys;
     if(R == 0) return;
@@ -1276,12 +1320,17 @@ private:
     d2h(X.h_cnt.p, X.d_cnt.p, (size_t)R * 4);
     d2h(X.h_misc.p + 1, E.d_bytes.p + 3, sizeof(unsigned long long));
     CK(cudaEventRecord(X.ev[3], E.stream));
-    {
-      const clk::time_point t0 = clk::now();
-      CK(cudaEventSynchronize(X.ev[3]));
-      st_.host_wait_ms += ms_since(t0);
-    }
-    CK(cudaGetLastError());
+  }
+
+  // after root_count's results are on the host (ev[3] reached)
+  void root_children(int32_t id, WaveCtx &X)
+  {
+    JobState &S = *jobs_[id];
+    Database &db = *S.job.db;
+    const int32_t words = words_for(db.host.n_graphs);
+    const int32_t R = db.root_keys;
+    if(R == 0) return;
+    const int32_t rcopies = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)1 << 20) / R));
     check_flags(X.h_misc.p[1]);
     st_.root_ms += ms_between(X.ev[0], X.ev[1]);
 
@@ -2063,7 +2112,7 @@ int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats 
     const clk::time_point t0 = clk::now();
     g_engine.init(wave_opt.threads);
     Sched s(g_engine, wave_opt, st);
-    for(auto &j : jobs) s.add(j);
+    s.add_all(jobs);
     while(!s.idle()) s.step();
     s.sync_stats();
     st.wall_ms += ms_since(t0);
