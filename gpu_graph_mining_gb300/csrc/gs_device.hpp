@@ -42,6 +42,21 @@ struct DevDB {
   const int32_t *pair_code;  // [root_off[VL]] (elabel << 16) | tolabel of each pair
 };
 
+// Per job of a root phase (the root level of a group of jobs, one launch per
+// kernel): its vertices as 32-vertex warp tiles in the group's tile space, its
+// bitmaps, counter copies and keys at their offsets in the group's buffers.
+struct RootJob {
+  long long tile_begin;  // first warp tile of the job (its vertex 0)
+  long long bm_base;     // first bitmap word of the job's key 0
+  long long cnt_base;    // first counter of the job's copy 0 (copy q at cnt_base + q * R)
+  int32_t db;            // index into the resident-database table
+  int32_t words;         // bitmap words per key = ceil(graphs / 32)
+  int32_t R;             // root keys of the job's database
+  int32_t copies;        // counter copies
+  int32_t key_base;      // first key of the job in the group's key space
+  int32_t pad;
+};
+
 // Per DFS-tree node of a wave (a batch of nodes extended together).
 struct NodeDesc {
   long long row_begin;   // first row in the wave's concatenated row space

@@ -764,10 +764,10 @@ struct Engine {
   DBuf<DevDB> d_dbs;
   DBuf<unsigned long long> d_bytes;   // [0] count bytes, [1] materialise bytes, [2] root bytes, [3] flags
   WaveCtx ctx[kWaveCtx];
-  // root phases: up to kRootCtx jobs of a batch are counted together, with one
-  // host wait for all of them, each in its own context
-  static constexpr int kRootCtx = 16;
-  WaveCtx rootc[kRootCtx];
+  // root phases: the root level of a group of jobs, one launch per kernel
+  WaveCtx rootx;
+  static constexpr int kRootGroup = 64;                    // jobs
+  static constexpr int64_t kRootGroupBytes = 1LL << 30;   // bitmap bytes (one job at least)
   bool ready = false;
 
   void init(int threads)
@@ -780,7 +780,7 @@ struct Engine {
       d_dbs.ensure(kMaxDbSlots);
       CK(cudaMemsetAsync(d_bytes.p, 0, sizeof(unsigned long long) * 4, stream));
       for(auto &c : ctx) c.init();
-      for(auto &r : rootc) r.init();
+      rootx.init();
       ready = true;
     }
     pool.set_limit(pool_limit);
@@ -798,7 +798,7 @@ struct Engine {
     d_dbs.free();
     d_bytes.free();
     for(auto &c : ctx) c.free();
-    for(auto &r : rootc) r.free();
+    rootx.free();
     cudaStreamSynchronize(aux);
     cudaStreamDestroy(aux);
     cudaStreamDestroy(stream);
@@ -1260,112 +1260,141 @@ private:
   }
 
   // ---- root level: all frequent 1-edge codes of one job
-  // The root level of jobs: every root triple's support and embedding count
-  // (one count and one support launch per job), the frequent roots in the
-  // reference's order, and their first embeddings.  The jobs' counts are
-  // queued together and read back after one host wait.
+  // The root level of jobs, in groups: every root triple's support and
+  // embedding count for all jobs of a group (one launch of each kernel), read
+  // back after one host wait; the frequent roots of each job in the
+  // reference's order; their first embeddings (one launch for the group).
+  static int32_t root_copies(int32_t R)
+  {
+    // copies of the root counters: every vertex adds into a few hundred counters
+    return (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)1 << 20) / R));
+  }
+
   void root_phase(const std::vector<int32_t> &ids)
   {
-    for(size_t i0 = 0; i0 < ids.size(); i0 += Engine::kRootCtx) {
-      const size_t i1 = std::min(ids.size(), i0 + (size_t)Engine::kRootCtx);
-      for(size_t i = i0; i < i1; i++) root_count(ids[i], E.rootc[i - i0]);
-      {
-        // one event behind every job's read-back (a job without root keys
-        // queues nothing, so no job's own event can stand for the others)
-        CK(cudaEventRecord(E.rootc[0].ev[6], E.stream));
-        const clk::time_point t0 = clk::now();
-        CK(cudaEventSynchronize(E.rootc[0].ev[6]));
-        st_.host_wait_ms += ms_since(t0);
+    size_t i = 0;
+    while(i < ids.size()) {
+      std::vector<RootJob> rj;
+      std::vector<int32_t> gid;
+      int64_t bmw = 0, cntn = 0;
+      int32_t keys = 0;
+      long long tiles = 0;
+      for(; i < ids.size() && (int)rj.size() < Engine::kRootGroup; i++) {
+        JobState &S = *jobs_[ids[i]];
+        Database &db = *S.job.db;
+        const int32_t R = db.root_keys;
+        if(R == 0) continue;
+        const int32_t words = words_for(db.host.n_graphs);
+        const int64_t nw = (int64_t)R * words;
+        if(!rj.empty() && (bmw + nw) * 4 > Engine::kRootGroupBytes) break;
+        RootJob J{};
+        J.tile_begin = tiles;
+        J.bm_base = bmw;
+        J.cnt_base = cntn;
+        J.db = S.db_slot;
+        J.words = words;
+        J.R = R;
+        J.copies = root_copies(R);
+        J.key_base = keys;
+        rj.push_back(J);
+        gid.push_back(ids[i]);
+        tiles += ((long long)db.dev.n_vertices + 31) / 32;
+        bmw += nw;
+        cntn += (int64_t)R * J.copies;
+        keys += R;
       }
-      CK(cudaGetLastError());
-      for(size_t i = i0; i < i1; i++) root_children(ids[i], E.rootc[i - i0]);
+      if(!rj.empty()) root_group(rj, gid, tiles, bmw, cntn, keys);
     }
   }
 
-  void root_count(int32_t id, WaveCtx &X)
+  void root_group(const std::vector<RootJob> &rj, const std::vector<int32_t> &gid, long long tiles, int64_t bmw,
+                  int64_t cntn, int32_t keys)
   {
-    JobState &S = *jobs_[id];
-    Database &db = *S.job.db;
-    const int32_t words = words_for(db.host.n_graphs);
-    const int32_t R = db.root_keys;
-    if(R == 0) return;
-    // the pinned mirrors below were last read by the previous root phase's copies
+    WaveCtx &X = E.rootx;
+    const int32_t n = (int32_t)rj.size();
+    // the pinned mirrors below were last read by the previous group's copies
     CK(cudaEventSynchronize(X.ev[5]));
-    const size_t nw = (size_t)R * words;
-    X.d_bm.ensure(nw);
-    X.d_bmx.ensure(nw);
-    // copies of the root counters: every vertex adds into a few hundred counters
-    const int32_t rcopies = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)1 << 20) / R));
-    X.d_cnt.ensure((size_t)R * rcopies);
-    X.d_sup.ensure(R);
-    X.d_childmap.ensure(R);
-    // pseudo node spanning the root keys, for the support kernel
-    NodeDesc nd{};
-    nd.words = words;
-    nd.nkeys = R;
-    X.d_desc.ensure(sizeof(NodeDesc));
-    X.h_desc.ensure(sizeof(NodeDesc));
-    std::memcpy(X.h_desc.p, &nd, sizeof(nd));
-    h2d(X.d_desc.p, X.h_desc.p, sizeof(nd));
-    CK(cudaMemsetAsync(X.d_bm.p, 0, nw * 4, E.stream));
-    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)R * rcopies * 4, E.stream));
+    X.d_bm.ensure(bmw);
+    X.d_bmx.ensure(bmw);
+    X.d_cnt.ensure(cntn);
+    X.d_sup.ensure(2 * (size_t)keys);  // supports, then embeddings
+    X.d_childmap.ensure(keys);
+    // pseudo nodes spanning each job's root keys (for the support kernel), then the job table
+    const size_t nd_bytes = sizeof(NodeDesc) * n, tab_bytes = nd_bytes + sizeof(RootJob) * n;
+    X.d_desc.ensure(tab_bytes);
+    X.h_desc.ensure(tab_bytes);
+    NodeDesc *hn = (NodeDesc *)X.h_desc.p;
+    for(int32_t q = 0; q < n; q++) {
+      NodeDesc nd{};
+      nd.words = rj[q].words;
+      nd.nkeys = rj[q].R;
+      nd.key_base = rj[q].key_base;
+      nd.bm_base = rj[q].bm_base;
+      hn[q] = nd;
+    }
+    std::memcpy(X.h_desc.p + nd_bytes, rj.data(), sizeof(RootJob) * n);
+    h2d(X.d_desc.p, X.h_desc.p, tab_bytes);
+    const NodeDesc *d_nd = (const NodeDesc *)X.d_desc.p;
+    const RootJob *d_rj = (const RootJob *)(X.d_desc.p + nd_bytes);
+    CK(cudaMemsetAsync(X.d_bm.p, 0, (size_t)bmw * 4, E.stream));
+    CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)cntn * 4, E.stream));
     CK(cudaEventRecord(X.ev[0], E.stream));
-    launch_root_count(db.dev, db.d_root_off, X.d_bm.p, X.d_cnt.p, words, R, rcopies, E.d_bytes.p + 2, E.stream);
-    launch_support((const NodeDesc *)X.d_desc.p, 1, R, X.d_bm.p, X.d_bmx.p, X.d_sup.p, E.stream);
+    launch_root_count(d_rj, n, tiles, E.d_dbs.p, X.d_bm.p, X.d_cnt.p, X.d_sup.p + keys, keys, E.d_bytes.p + 2,
+                      E.stream);
+    launch_support(d_nd, n, keys, X.d_bm.p, X.d_bmx.p, X.d_sup.p, E.stream);
     CK(cudaEventRecord(X.ev[1], E.stream));
-    st_.launches += 2;
-    X.h_sup.ensure(R);
-    X.h_cnt.ensure(R);
-    d2h(X.h_sup.p, X.d_sup.p, (size_t)R * 4);
-    d2h(X.h_cnt.p, X.d_cnt.p, (size_t)R * 4);
+    st_.launches += 3;
+    X.h_sup.ensure(2 * (size_t)keys);
+    d2h(X.h_sup.p, X.d_sup.p, (size_t)keys * 8);
     d2h(X.h_misc.p + 1, E.d_bytes.p + 3, sizeof(unsigned long long));
     CK(cudaEventRecord(X.ev[3], E.stream));
-  }
-
-  // after root_count's results are on the host (ev[3] reached)
-  void root_children(int32_t id, WaveCtx &X)
-  {
-    JobState &S = *jobs_[id];
-    Database &db = *S.job.db;
-    const int32_t words = words_for(db.host.n_graphs);
-    const int32_t R = db.root_keys;
-    if(R == 0) return;
-    const int32_t rcopies = (int32_t)std::max<int64_t>(1, std::min<int64_t>(64, ((int64_t)1 << 20) / R));
+    {
+      const clk::time_point t0 = clk::now();
+      CK(cudaEventSynchronize(X.ev[3]));
+      st_.host_wait_ms += ms_since(t0);
+    }
+    CK(cudaGetLastError());
     check_flags(X.h_misc.p[1]);
     st_.root_ms += ms_between(X.ev[0], X.ev[1]);
 
-    const bool extend = S.job.opt.max_edges != 1;
     std::vector<ChildOut> outs;
-    std::vector<int32_t> made;
-    X.h_childmap.ensure(R);
-    for(int32_t i = 0; i < R; i++) X.h_childmap.p[i] = -1;
-    // frequent roots of this job (and partition), in the reference's order
-    struct Sel { int32_t key, pid; DFS d; int32_t sup; int64_t n; };
-    std::vector<Sel> sel;
-    int32_t root_index = 0;
-    size_t bytes = 0;
-    for(int32_t fl = 0; fl < db.VL; fl++) {
-      for(size_t p = 0; p < db.pairs[fl].size(); p++) {
-        const int32_t el = db.pairs[fl][p].first, tl = db.pairs[fl][p].second;
-        if(tl < fl) continue;
-        const int32_t key = db.root_off[fl] + (int32_t)p;
-        const int32_t sup = X.h_sup.p[key];
-        if(sup < S.job.minsup) continue;
-        // root-subtree partition: independent subtrees, no exchange between parts
-        const int32_t ri = root_index++;
-        if(S.job.opt.root_parts > 1 && ri % S.job.opt.root_parts != S.job.opt.root_part) continue;
-        PatternRec pr{ -1, DFS{ 0, 1, fl, el, tl }, sup };
-        S.pats.push_back(pr);
-        const int32_t pid = (int32_t)S.pats.size() - 1;
-        S.roots.push_back(pid);
-        if(!extend) continue;
-        const int64_t n = X.h_cnt.p[key];
-        sel.push_back(Sel{ key, pid, pr.edge, sup, n });
-        bytes += 2 * Carver::round((size_t)n * 8) + Carver::round((size_t)n * 4);
+    std::vector<std::vector<int32_t>> made(n);
+    X.h_childmap.ensure(keys);
+    for(int32_t k = 0; k < keys; k++) X.h_childmap.p[k] = -1;
+    const int32_t *hsup = X.h_sup.p, *hcnt = X.h_sup.p + keys;
+    for(int32_t q = 0; q < n; q++) {
+      const int32_t id = gid[q];
+      JobState &S = *jobs_[id];
+      Database &db = *S.job.db;
+      const int32_t kb = rj[q].key_base;
+      const bool extend = S.job.opt.max_edges != 1;
+      // frequent roots of this job (and partition), in the reference's order
+      struct Sel { int32_t key, pid; DFS d; int32_t sup; int64_t n; };
+      std::vector<Sel> sel;
+      int32_t root_index = 0;
+      size_t bytes = 0;
+      for(int32_t fl = 0; fl < db.VL; fl++) {
+        for(size_t p = 0; p < db.pairs[fl].size(); p++) {
+          const int32_t el = db.pairs[fl][p].first, tl = db.pairs[fl][p].second;
+          if(tl < fl) continue;
+          const int32_t key = kb + db.root_off[fl] + (int32_t)p;
+          const int32_t sup = hsup[key];
+          if(sup < S.job.minsup) continue;
+          // root-subtree partition: independent subtrees, no exchange between parts
+          const int32_t ri = root_index++;
+          if(S.job.opt.root_parts > 1 && ri % S.job.opt.root_parts != S.job.opt.root_part) continue;
+          PatternRec pr{ -1, DFS{ 0, 1, fl, el, tl }, sup };
+          S.pats.push_back(pr);
+          const int32_t pid = (int32_t)S.pats.size() - 1;
+          S.roots.push_back(pid);
+          if(!extend) continue;
+          const int64_t rows = hcnt[key];
+          sel.push_back(Sel{ key, pid, pr.edge, sup, rows });
+          bytes += 2 * Carver::round((size_t)rows * 8) + Carver::round((size_t)rows * 4);
+        }
       }
-    }
-    if(!sel.empty()) {
-      // all root columns and ranks in one pool block
+      if(sel.empty()) continue;
+      // all root columns and ranks of the job in one pool block
       const int32_t blk = E.new_block(bytes);
       Carver cv{ (char *)E.blocks[blk].base };
       for(const Sel &s : sel) {
@@ -1388,28 +1417,28 @@ private:
         nn.nrows = s.n;
         nn.support = s.sup;
         S.live_bytes += s.n * (int64_t)(2 * sizeof(int2) + sizeof(int32_t));
-        made.push_back(nid);
+        made[q].push_back(nid);
       }
       S.peak_bytes = std::max(S.peak_bytes, S.live_bytes);
     }
     if(!outs.empty()) {
       X.d_outs.ensure(outs.size());
-      X.d_cursor.ensure(outs.size());
       X.h_outs.ensure(outs.size());
       std::memcpy(X.h_outs.p, outs.data(), sizeof(ChildOut) * outs.size());
       h2d(X.d_outs.p, X.h_outs.p, sizeof(ChildOut) * outs.size());
-      h2d(X.d_childmap.p, X.h_childmap.p, (size_t)R * 4);
-      // cursors: the root counter copies hold each copy's offset; copy 0 (the
-      // totals, already copied back) starts at 0
-      CK(cudaMemsetAsync(X.d_cnt.p, 0, (size_t)R * 4, E.stream));
-      launch_root_materialize(db.dev, db.d_root_off, X.d_bm.p, X.d_bmx.p, words, X.d_childmap.p, X.d_cnt.p, R, rcopies,
-                              X.d_outs.p, err_flag(), E.stream);
+      h2d(X.d_childmap.p, X.h_childmap.p, (size_t)keys * 4);
+      // cursors: the counter copies hold each copy's offset (copy 0 at 0)
+      launch_root_materialize(d_rj, n, tiles, E.d_dbs.p, X.d_bm.p, X.d_bmx.p, X.d_cnt.p, X.d_childmap.p, X.d_outs.p,
+                              err_flag(), E.stream);
       st_.launches++;
     }
     CK(cudaEventRecord(X.ev[5], E.stream));
-    S.pending += (int64_t)made.size();
-    stacked_ += (int64_t)made.size();
-    for(auto it = made.rbegin(); it != made.rend(); ++it) S.stack.push_back(*it);
+    for(int32_t q = 0; q < n; q++) {
+      JobState &S = *jobs_[gid[q]];
+      S.pending += (int64_t)made[q].size();
+      stacked_ += (int64_t)made[q].size();
+      for(auto it = made[q].rbegin(); it != made[q].rend(); ++it) S.stack.push_back(*it);
+    }
   }
 
   // Queues a wave's device work: replayed from the context's CUDA graph for

@@ -58,30 +58,47 @@ __device__ __forceinline__ unsigned lanemask_lt()
 // (coalesced 8-byte loads) and find their source vertex by a 5-step shuffle
 // search over the lanes' adjacency starts.  The warp stays converged, so the
 // embedding counters and child cursors take one atomic per distinct key.
+// The root level of a group of jobs in one launch: the jobs' vertex tiles
+// laid end to end (a warp finds its tile's job in the table), each job's
+// bitmaps, counter copies and keys at its own offsets.  The materialise pass
+// runs the same grid over the same tiles, so a warp uses the same counter copy
+// in both passes.
 template <bool MAT>
-__device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__restrict__ root_off, uint32_t *bm,
-                                           const int32_t *__restrict__ bmx, int32_t *cnt, int32_t words,
-                                           int32_t R, int32_t cnt_copies,
-                                           const int32_t *__restrict__ childmap, int32_t *cursor,
-                                           const ChildOut *__restrict__ outs, unsigned long long *bytes,
-                                           unsigned int *err)
+__device__ __forceinline__ void root_tiles(const RootJob *__restrict__ jobs, int njobs, long long tiles,
+                                           const DevDB *__restrict__ dbs, uint32_t *bm,
+                                           const int32_t *__restrict__ bmx, int32_t *cnt,
+                                           const int32_t *__restrict__ childmap, const ChildOut *__restrict__ outs,
+                                           unsigned long long *bytes, unsigned int *err)
 {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const long long tiles = ((long long)db.n_vertices + 31) / 32;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   unsigned long long mine = 0;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  // this warp's copy of the root counters (copies spread the hot counters over L2 slices)
-  const int cnt_copy_idx = (int)(gw % (cnt_copies > 0 ? cnt_copies : 1));
-  int32_t *const cnt_copy = MAT ? nullptr : cnt + cnt_copy_idx * (long long)R;
+  int jn = 0;  // a warp's tiles ascend, so its job index only moves forward
   for(long long tile = gw; tile < tiles; tile += nwarps) {
-    const long long v = tile * 32 + lane;
-    const bool valid = v < db.n_vertices;
-    const int a0 = valid ? __ldg(&db.adj_off[v]) : 0;
-    const int a1 = valid ? __ldg(&db.adj_off[v + 1]) : 0;
-    const int fl = valid ? __ldg(&db.vlabel[v]) : 0;
-    const int g = valid ? __ldg(&db.vgraph[v]) : 0;
+    while(jn + 1 < njobs && jobs[jn + 1].tile_begin <= tile) jn++;
+    const RootJob J = jobs[jn];
+    // the job's database: pointers into registers (the atomics below would
+    // otherwise make the compiler re-read the table)
+    const unsigned long long *__restrict__ adj = dbs[J.db].adj;
+    const int32_t *__restrict__ adj_off = dbs[J.db].adj_off;
+    const int32_t *__restrict__ vlabel = dbs[J.db].vlabel;
+    const int32_t *__restrict__ vgraph = dbs[J.db].vgraph;
+    const int32_t *__restrict__ adj_pair = dbs[J.db].adj_pair;
+    const int32_t *__restrict__ root_off = dbs[J.db].root_off;
+    const int n_vertices = dbs[J.db].n_vertices;
+    // this warp's copy of the job's root counters (copies spread the hot
+    // counters over L2 slices)
+    const int cnt_copy_idx = (int)(gw % (J.copies > 0 ? J.copies : 1));
+    int32_t *const cnt_copy = cnt + J.cnt_base + (long long)cnt_copy_idx * J.R;
+    const long long vt = (tile - J.tile_begin) * 32;
+    const long long v = vt + lane;
+    const bool valid = v < n_vertices;
+    const int a0 = valid ? __ldg(&adj_off[v]) : 0;
+    const int a1 = valid ? __ldg(&adj_off[v + 1]) : 0;
+    const int fl = valid ? __ldg(&vlabel[v]) : 0;
+    const int g = valid ? __ldg(&vgraph[v]) : 0;
     const int W = a1 - a0;
     int incl = W;
     for(int o = 1; o < 32; o <<= 1) {
@@ -106,8 +123,8 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
       int key = -1, w = 0;
       if(has) {
         // entry, pair index and the label's first key: independent loads, in flight together
-        const unsigned long long ent = __ldg(&db.adj[e]);
-        const int pr = __ldg(&db.adj_pair[e]);
+        const unsigned long long ent = __ldg(&adj[e]);
+        const int pr = __ldg(&adj_pair[e]);
         const int ro = __ldg(&root_off[fl_o]);
         w = (int)(unsigned)(ent & 0xffffffffull);
         const unsigned hi = (unsigned)(ent >> 32);
@@ -117,26 +134,26 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
       }
       if(!MAT) {
         if(key >= 0) {
-          atomicOr(&bm[(long long)key * words + (g_o >> 5)], 1u << (g_o & 31));
+          atomicOr(&bm[J.bm_base + (long long)key * J.words + (g_o >> 5)], 1u << (g_o & 31));
           mine += 8;
         }
         const unsigned peers = __match_any_sync(full, key);
         if(key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt_copy[key], __popc(peers));
       } else {
-        const int c = key >= 0 ? childmap[key] : -1;
+        const int c = key >= 0 ? childmap[J.key_base + key] : -1;
         const unsigned peers = __match_any_sync(full, c);
         const int leader = __ffs(peers) - 1;
         int pos = 0;
         // the cursor of this warp's counter copy of the key: the same warp
         // counted the same entries in the count pass (same grid, same tiles)
-        if(c >= 0 && lane == leader) pos = atomicAdd(&cursor[cnt_copy_idx * (long long)R + key], __popc(peers));
+        if(c >= 0 && lane == leader) pos = atomicAdd(&cnt_copy[key], __popc(peers));
         pos = __shfl_sync(full, pos, leader) + __popc(peers & lanemask_lt());
         if(c >= 0) {
-          const long long wi = (long long)key * words + (g_o >> 5);
+          const long long wi = J.bm_base + (long long)key * J.words + (g_o >> 5);
           const int rank = bmx[wi] + __popc(bm[wi] & ((1u << (g_o & 31)) - 1u));
           const ChildOut out = outs[c];
           if(pos < out.cap) {
-            out.col0[pos] = make_int2((int)(tile * 32 + o), -1);
+            out.col0[pos] = make_int2((int)(vt + o), -1);
             out.col[pos] = make_int2(w, pos);
             out.gord[pos] = rank;
           } else {
@@ -149,36 +166,46 @@ __device__ __forceinline__ void root_tiles(const DevDB &db, const int32_t *__res
   if(!MAT) add_bytes(bytes, mine);
 }
 
-__global__ void __launch_bounds__(kBlock) k_root_count(DevDB db, const int32_t *__restrict__ root_off, uint32_t *bm,
-                                                        int32_t *cnt, int32_t words, int32_t R, int32_t cnt_copies,
+__global__ void __launch_bounds__(kBlock) k_root_count(const RootJob *__restrict__ jobs, int njobs, long long tiles,
+                                                        const DevDB *__restrict__ dbs, uint32_t *bm, int32_t *cnt,
                                                         unsigned long long *bytes)
 {
-  root_tiles<false>(db, root_off, bm, nullptr, cnt, words, R, cnt_copies, nullptr, nullptr, nullptr, bytes, nullptr);
+  root_tiles<false>(jobs, njobs, tiles, dbs, bm, nullptr, cnt, nullptr, nullptr, bytes, nullptr);
 }
 
-// copies -> copy 0 the total, copy q >= 1 the count of copies 0..q-1
-__global__ void __launch_bounds__(kBlock) k_sum_copies(int32_t *cnt, int32_t n, int32_t copies)
+// Per key of the group: the job's counter copies turn into the offsets of
+// each copy's share (copy q >= 1: the count of copies 0..q-1), the total goes
+// to tot[key], and copy 0 starts at 0 as the materialise pass's cursor.
+__global__ void __launch_bounds__(kBlock) k_sum_copies(const RootJob *__restrict__ jobs, int njobs, int total_keys,
+                                                        int32_t *cnt, int32_t *tot)
 {
-  for(int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    int c = cnt[k];
-    for(int q = 1; q < copies; q++) {
-      const int x = cnt[(long long)q * n + k];
-      cnt[(long long)q * n + k] = c;
+  for(int kg = blockIdx.x * blockDim.x + threadIdx.x; kg < total_keys; kg += gridDim.x * blockDim.x) {
+    int lo = 0, hi = njobs - 1;
+    while(lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if(jobs[mid].key_base <= kg) lo = mid; else hi = mid - 1;
+    }
+    const RootJob &J = jobs[lo];
+    int32_t *c0 = cnt + J.cnt_base + (kg - J.key_base);
+    int c = c0[0];
+    for(int q = 1; q < J.copies; q++) {
+      const int x = c0[(long long)q * J.R];
+      c0[(long long)q * J.R] = c;
       c += x;
     }
-    cnt[k] = c;
+    tot[kg] = c;
+    c0[0] = 0;
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_root_materialize(DevDB db, const int32_t *__restrict__ root_off,
+__global__ void __launch_bounds__(kBlock) k_root_materialize(const RootJob *__restrict__ jobs, int njobs,
+                                                              long long tiles, const DevDB *__restrict__ dbs,
                                                               const uint32_t *__restrict__ bm,
-                                                              const int32_t *__restrict__ bmx, int32_t words,
-                                                              const int32_t *__restrict__ childmap, int32_t *cursor,
-                                                              int32_t R, int32_t cnt_copies,
+                                                              const int32_t *__restrict__ bmx, int32_t *cursor,
+                                                              const int32_t *__restrict__ childmap,
                                                               const ChildOut *__restrict__ outs, unsigned int *err)
 {
-  root_tiles<true>(db, root_off, const_cast<uint32_t *>(bm), bmx, nullptr, words, R, cnt_copies, childmap, cursor,
-                   outs, nullptr, err);
+  root_tiles<true>(jobs, njobs, tiles, dbs, const_cast<uint32_t *>(bm), bmx, cursor, childmap, outs, nullptr, err);
 }
 
 __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__ nodes, int nnodes, int total_keys,
@@ -531,22 +558,22 @@ inline int grid_for(long long n)
 
 }  // namespace
 
-void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
-                       int32_t R, int32_t cnt_copies, unsigned long long *bytes, cudaStream_t s)
+void launch_root_count(const RootJob *jobs, int32_t njobs, long long tiles, const DevDB *dbs, uint32_t *bm,
+                       int32_t *cnt, int32_t *tot, int32_t total_keys, unsigned long long *bytes, cudaStream_t s)
 {
-  k_root_count<<<grid_for((long long)db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, cnt, words, R, cnt_copies,
-                                                                      bytes);
-  if(cnt_copies > 1) k_sum_copies<<<grid_for(R), kBlock, 0, s>>>(cnt, R, cnt_copies);
+  if(tiles > 0) k_root_count<<<grid_for(tiles * 32), kBlock, 0, s>>>(jobs, njobs, tiles, dbs, bm, cnt, bytes);
+  if(total_keys > 0) k_sum_copies<<<grid_for(total_keys), kBlock, 0, s>>>(jobs, njobs, total_keys, cnt, tot);
 }
 
-void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
-                             int32_t words, const int32_t *childmap, int32_t *cursor, int32_t R, int32_t cnt_copies,
+void launch_root_materialize(const RootJob *jobs, int32_t njobs, long long tiles, const DevDB *dbs,
+                             const uint32_t *bm, const int32_t *bmx, int32_t *cursor, const int32_t *childmap,
                              const ChildOut *outs, unsigned int *err, cudaStream_t s)
 {
   // the same grid as the count pass: warp w processes the same tiles and uses
   // the same counter copy
-  k_root_materialize<<<grid_for(db.n_vertices), kBlock, 0, s>>>(db, root_off, bm, bmx, words, childmap, cursor, R,
-                                                                 cnt_copies, outs, err);
+  if(tiles > 0)
+    k_root_materialize<<<grid_for(tiles * 32), kBlock, 0, s>>>(jobs, njobs, tiles, dbs, bm, bmx, cursor, childmap,
+                                                                outs, err);
 }
 
 void launch_records_bitmap(const int32_t *keys, const int32_t *gids, long long n, int32_t words, uint32_t *bm,

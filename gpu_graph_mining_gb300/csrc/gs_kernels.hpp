@@ -55,19 +55,19 @@ private:
   size_t used_ = 0;
 };
 
-// Root level: one thread per vertex walks its adjacency; every directed
-// entry (v -> w) with label(v) <= label(w) is a 1-edge embedding
-// (get_forward_root, src/globals/graph_types.cpp:365-375).
-// Sets support-bitmap bit [key][graph] and counts embeddings per key.
-// cnt holds cnt_copies copies of the R root counters, R apart (summed into the
-// first copy before the call returns on the stream).
-void launch_root_count(const DevDB &db, const int32_t *root_off, uint32_t *bm, int32_t *cnt, int32_t words,
-                       int32_t R, int32_t cnt_copies, unsigned long long *bytes, cudaStream_t s);
-// Writes the two columns and graph ranks of every selected root key.  cursor
-// holds cnt_copies copies of R cursors: copy q of a key starts at the count
-// of copies 0..q-1 (as the root count leaves them, with copy 0 reset to 0).
-void launch_root_materialize(const DevDB &db, const int32_t *root_off, const uint32_t *bm, const int32_t *bmx,
-                             int32_t words, const int32_t *childmap, int32_t *cursor, int32_t R, int32_t cnt_copies,
+// Root level of a group of jobs: a warp per 32 vertices of a job walks their
+// adjacency; every directed entry (v -> w) with label(v) <= label(w) is a
+// 1-edge embedding (get_forward_root, src/globals/graph_types.cpp:365-375).
+// Sets support-bitmap bit [key][graph] and counts embeddings per key in the
+// warp's counter copy; then per key of the group: tot[key] = its embeddings,
+// copy q >= 1 = the count of copies 0..q-1 and copy 0 = 0 (the materialise
+// pass's cursors).  tiles = the group's warp tiles; total_keys = its keys.
+void launch_root_count(const RootJob *jobs, int32_t njobs, long long tiles, const DevDB *dbs, uint32_t *bm,
+                       int32_t *cnt, int32_t *tot, int32_t total_keys, unsigned long long *bytes, cudaStream_t s);
+// Writes the two columns and graph ranks of every selected root key of the
+// group (childmap over the group's keys), with the counter copies as cursors.
+void launch_root_materialize(const RootJob *jobs, int32_t njobs, long long tiles, const DevDB *dbs,
+                             const uint32_t *bm, const int32_t *bmx, int32_t *cursor, const int32_t *childmap,
                              const ChildOut *outs, unsigned int *err, cudaStream_t s);
 
 // Wave level (gs_wave.cu): a warp per 32 embedding rows of the wave's nodes.
