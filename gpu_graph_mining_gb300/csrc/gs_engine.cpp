@@ -225,13 +225,15 @@ namespace {
 
 // -------------------------------------------------------------- device pool
 
-// First-fit sub-allocator over a few large cudaMalloc chunks.  All work is
-// issued on one stream, so memory freed here may be handed out again
-// immediately: later kernels are ordered after the ones still reading it.
+// First-fit sub-allocator over a few large cudaMalloc chunks.  Memory freed
+// here is handed out again at once: the engine returns a block only after
+// every stream has passed the work queued before the block's last reference
+// was dropped (Engine::fence / reap).
 class Pool {
 public:
   void set_limit(int64_t b) { limit_ = b; }
-  void *alloc(size_t n)
+  // a piece of the chunks there are, or nullptr
+  void *try_alloc(size_t n)
   {
     n = (n + 255) & ~(size_t)255;
     if(n == 0) n = 256;
@@ -239,6 +241,13 @@ public:
       void *p = take(c, n);
       if(p) return p;
     }
+    return nullptr;
+  }
+  void *alloc(size_t n)
+  {
+    if(void *p = try_alloc(n)) return p;
+    n = (n + 255) & ~(size_t)255;
+    if(n == 0) n = 256;
     grow(n);
     void *p = take(chunks_.size() - 1, n);
     if(!p) throw Error(ST_ERR_NOMEM, "device pool exhausted");
@@ -674,7 +683,7 @@ struct WaveCtx {
   DBuf<int32_t> d_lnode;   // lists strategy: the node of each frequent forward key
   // A wave's results, copied back in one piece: a 64-byte header (kHead*
   // slots) followed by the selected candidates {key, support, embeddings,
-  // verdict}.  The zeroed region holds the embedding counts and the support
+  // node << 2 | verdict}.  The zeroed region holds the embedding counts and the support
   // bitmaps (one memset).  The child table holds the children's outputs and
   // (key, child) pairs (one upload).
   DBuf<char> d_head, d_zero, d_mat;
@@ -695,13 +704,16 @@ struct WaveCtx {
   cudaEvent_t ev[7] = {};
   bool have_events = false;
   std::vector<WaveGraph> graphs;
+  // the context's stream (wave contexts; the root context uses the engine's)
+  cudaStream_t stream = nullptr;
 
-  void init()
+  void init(bool own_stream)
   {
     if(!have_events) {
       for(auto &e : ev) CK(cudaEventCreate(&e));
       have_events = true;
     }
+    if(own_stream && !stream) CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     h_misc.ensure(4);
   }
   void free()
@@ -719,6 +731,11 @@ struct WaveCtx {
     if(have_events)
       for(auto &e : ev) cudaEventDestroy(e);
     have_events = false;
+    if(stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+    stream = nullptr;
     rec_enabled = true;
     wanted_rec = 0;
   }
@@ -751,8 +768,13 @@ int64_t rule_skip_adj_bytes()
 constexpr int kWaveCtx = GS_WAVE_CTX;   // databases one scheduler keeps in its device table before it grows
 
 struct Engine {
+  // Streams: the engine's (database table, root phases) and one per wave
+  // context, so that one wave's selection and materialise passes run beside
+  // another's count kernel.  A wave waits (events) for the engine's stream
+  // and for every other context's last materialise pass before its count.
   cudaStream_t stream = nullptr;
   cudaStream_t aux = nullptr;   // catch-up copies that must not wait for queued waves
+  cudaEvent_t ev_main = nullptr;  // the engine's stream after the last jobs joined
   Pool pool;
   std::unique_ptr<Workers> workers;
   std::vector<MinChecker> checkers;
@@ -769,6 +791,17 @@ struct Engine {
   static constexpr int kRootGroup = 64;                    // jobs
   static constexpr int64_t kRootGroupBytes = 1LL << 30;   // bitmap bytes (one job at least)
   bool ready = false;
+  // Pool blocks whose last reference was dropped go back to the pool only
+  // after every stream has passed the work queued until then (a fence: one
+  // event per stream), since a pass queued on another stream may still read
+  // them.
+  struct Fence {
+    std::vector<cudaEvent_t> ev;
+    std::vector<void *> blocks;
+  };
+  std::vector<void *> released;
+  std::deque<Fence> fences;
+  std::vector<cudaEvent_t> spare_ev;
 
   void init(int threads)
   {
@@ -776,11 +809,12 @@ struct Engine {
       CK(cudaSetDevice(0));
       CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
       CK(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming));
       d_bytes.ensure(4);
       d_dbs.ensure(kMaxDbSlots);
       CK(cudaMemsetAsync(d_bytes.p, 0, sizeof(unsigned long long) * 4, stream));
-      for(auto &c : ctx) c.init();
-      rootx.init();
+      for(auto &c : ctx) c.init(true);
+      rootx.init(false);
       ready = true;
     }
     pool.set_limit(pool_limit);
@@ -793,7 +827,15 @@ struct Engine {
   void destroy()
   {
     if(!ready) return;
-    cudaStreamSynchronize(stream);
+    sync_all();
+    for(Fence &f : fences)
+      for(cudaEvent_t e : f.ev) cudaEventDestroy(e);
+    fences.clear();
+    released.clear();
+    for(cudaEvent_t e : spare_ev) cudaEventDestroy(e);
+    spare_ev.clear();
+    if(ev_main) cudaEventDestroy(ev_main);
+    ev_main = nullptr;
     pool.destroy();
     d_dbs.free();
     d_bytes.free();
@@ -815,15 +857,77 @@ struct Engine {
     int32_t id;
     if(!free_blocks.empty()) { id = free_blocks.back(); free_blocks.pop_back(); }
     else { id = (int32_t)blocks.size(); blocks.emplace_back(); }
-    blocks[id].base = pool.alloc(bytes);
+    blocks[id].base = take_pool(bytes);
     blocks[id].refs = 0;
     return id;
+  }
+  // every stream's work done
+  void sync_all()
+  {
+    if(stream) cudaStreamSynchronize(stream);
+    for(auto &c : ctx)
+      if(c.stream) cudaStreamSynchronize(c.stream);
+  }
+  // a fence over the blocks released since the last one
+  void fence()
+  {
+    if(released.empty()) return;
+    Fence f;
+    auto rec = [&](cudaStream_t s) {
+      cudaEvent_t e;
+      if(!spare_ev.empty()) { e = spare_ev.back(); spare_ev.pop_back(); }
+      else CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      CK(cudaEventRecord(e, s));
+      f.ev.push_back(e);
+    };
+    rec(stream);
+    for(auto &c : ctx)
+      if(c.stream) rec(c.stream);
+    f.blocks.swap(released);
+    fences.push_back(std::move(f));
+  }
+  // returns fenced blocks to the pool: the passed fences (wait: also the
+  // oldest one not passed yet).  Returns false when no fence was left.
+  bool reap(bool wait)
+  {
+    bool any = false;
+    while(!fences.empty()) {
+      Fence &f = fences.front();
+      bool passed = true;
+      for(cudaEvent_t e : f.ev) {
+        const cudaError_t q = cudaEventQuery(e);
+        if(q == cudaErrorNotReady) { passed = false; break; }
+        CK(q);
+      }
+      if(!passed) {
+        if(!wait) break;
+        for(cudaEvent_t e : f.ev) CK(cudaEventSynchronize(e));
+        wait = false;
+      }
+      for(void *b : f.blocks) pool.release(b);
+      for(cudaEvent_t e : f.ev) spare_ev.push_back(e);
+      fences.pop_front();
+      any = true;
+    }
+    return any;
+  }
+  void *take_pool(size_t bytes)
+  {
+    fence();
+    reap(false);
+    for(;;) {
+      if(void *p = pool.try_alloc(bytes)) return p;
+      // fenced blocks first, the pool grows only when none is left
+      if(fences.empty()) break;
+      reap(true);
+    }
+    return pool.alloc(bytes);
   }
   void block_ref(int32_t b) { blocks[b].refs++; }
   void block_unref(int32_t b)
   {
     if(--blocks[b].refs == 0) {
-      pool.release(blocks[b].base);
+      released.push_back(blocks[b].base);
       blocks[b].base = nullptr;
       free_blocks.push_back(b);
     }
@@ -1018,16 +1122,19 @@ struct Flight {
   uint32_t *bm = nullptr;    // the wave's support bitmaps (in the zeroed region)
   int32_t *cnt = nullptr;    // its counter copies, cstride apart (cursors of the records materialise)
   long long cstride = 0;
+  std::vector<int32_t> sel_at, sel_order;  // the candidates' counting sort by node
 };
 
 // The wave scheduler.  Jobs join at any time (add) and leave when their last
 // DFS-tree node is done; each step launches waves into the idle contexts and
 // completes the oldest wave in flight.  With two contexts the host decodes
 // one wave's candidates, checks canonicality and lays out its children while
-// the GPU counts the other wave.  All device work is issued on the engine's
-// one stream, so a wave's children are materialised before any later wave
-// reads them, and pool memory released on the host is only reused by work
-// queued after its last reader.
+// the GPU counts the other wave.  Each context issues its waves on its own
+// stream: a wave's count waits for the engine's stream (database table, root
+// levels) and for every other context's last materialise pass, so that its
+// nodes' columns are written before it reads them; pool memory released on
+// the host is reused only after every stream has passed its last reader
+// (Engine::fence).
 class Sched {
 public:
   Sched(Engine &e, const MineOptions &wo, MineStats &st) : E(e), wo_(wo), st_(st)
@@ -1043,6 +1150,7 @@ public:
   {
     const int32_t id = enter(j);
     root_phase(std::vector<int32_t>{ id });
+    CK(cudaEventRecord(E.ev_main, E.stream));
     if(jobs_[id]->pending == 0) complete(id);
     return id;
   }
@@ -1054,6 +1162,7 @@ public:
     ids.reserve(js.size());
     for(const MineJob &j : js) ids.push_back(enter(j));
     root_phase(ids);
+    CK(cudaEventRecord(E.ev_main, E.stream));
     for(int32_t id : ids)
       if(jobs_[id]->pending == 0) complete(id);
   }
@@ -1081,7 +1190,7 @@ public:
       tab_.push_back(db->dev);
       if(tab_.size() > E.d_dbs.cap) {
         // the table is read by waves in flight: let them finish before it moves
-        CK(cudaStreamSynchronize(E.stream));
+        E.sync_all();
         E.d_dbs.ensure(tab_.size());
         h2d(E.d_dbs.p, tab_.data(), sizeof(DevDB) * tab_.size());
       } else {
@@ -1156,9 +1265,13 @@ public:
         fl_[c].mat_pending = false;
       }
     }
+    // every context's passes done before the counters are read
+    for(auto &c : E.ctx) CK(cudaStreamSynchronize(c.stream));
     unsigned long long bytes[4] = { 0, 0, 0, 0 };
     d2h(bytes, E.d_bytes.p, sizeof(bytes));
     CK(cudaStreamSynchronize(E.stream));
+    E.fence();
+    E.reap(false);
     CK(cudaGetLastError());
     check_flags(bytes[3]);
     st_.count_bytes += (int64_t)bytes[0] - seen_bytes_[0];
@@ -1189,14 +1302,14 @@ private:
   int64_t stacked_ = 0;          // nodes on all jobs' stacks
   int64_t seen_bytes_[2] = { 0, 0 };
 
-  void h2d(void *dst, const void *src, size_t n)
+  void h2d(void *dst, const void *src, size_t n, cudaStream_t s = nullptr)
   {
-    CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, E.stream));
+    CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s ? s : E.stream));
     st_.h2d_bytes += (int64_t)n;
   }
-  void d2h(void *dst, const void *src, size_t n)
+  void d2h(void *dst, const void *src, size_t n, cudaStream_t s = nullptr)
   {
-    CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, E.stream));
+    CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, s ? s : E.stream));
     st_.d2h_bytes += (int64_t)n;
   }
   // device consistency flags (slot 3 of the counters)
@@ -1448,19 +1561,19 @@ private:
     st_.h2d_bytes += (int64_t)q.desc_bytes;
     st_.d2h_bytes += (int64_t)q.d2h_bytes;
     if(wo_.launch_mode != 0) {
-      CK(cudaMemcpyAsync(q.desc_dst, q.desc_src, q.desc_bytes, cudaMemcpyHostToDevice, E.stream));
-      CK(cudaMemsetAsync(q.zero, 0, q.zero_bytes, E.stream));
-      CK(cudaMemsetAsync(q.head, 0, kHeadBytes, E.stream));
-      CK(cudaEventRecord(X.ev[0], E.stream));
-      CK(q.count.run(E.stream));
-      CK(cudaEventRecord(X.ev[1], E.stream));
-      CK(q.screen.run(E.stream));
-      CK(q.listed.run(E.stream));
-      CK(cudaEventRecord(X.ev[6], E.stream));
-      if(q.with_min) CK(q.ismin.run(E.stream));
-      CK(cudaEventRecord(X.ev[2], E.stream));
-      CK(cudaMemcpyAsync(q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost, E.stream));
-      CK(cudaEventRecord(X.ev[3], E.stream));
+      CK(cudaMemcpyAsync(q.desc_dst, q.desc_src, q.desc_bytes, cudaMemcpyHostToDevice, X.stream));
+      CK(cudaMemsetAsync(q.zero, 0, q.zero_bytes, X.stream));
+      CK(cudaMemsetAsync(q.head, 0, kHeadBytes, X.stream));
+      CK(cudaEventRecord(X.ev[0], X.stream));
+      CK(q.count.run(X.stream));
+      CK(cudaEventRecord(X.ev[1], X.stream));
+      CK(q.screen.run(X.stream));
+      CK(q.listed.run(X.stream));
+      CK(cudaEventRecord(X.ev[6], X.stream));
+      if(q.with_min) CK(q.ismin.run(X.stream));
+      CK(cudaEventRecord(X.ev[2], X.stream));
+      CK(cudaMemcpyAsync(q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost, X.stream));
+      CK(cudaEventRecord(X.ev[3], X.stream));
       return;
     }
     WaveGraph *G = nullptr;
@@ -1509,7 +1622,7 @@ private:
       if(q.with_min) CK(cudaGraphExecKernelNodeSetParams(G->x, G->ismin, &km));
       CK(cudaGraphExecMemcpyNodeSetParams1D(G->x, G->d2h, q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost));
     }
-    CK(cudaGraphLaunch(G->x, E.stream));
+    CK(cudaGraphLaunch(G->x, X.stream));
   }
 
   // ---- launch one wave into context c: descriptors, count, support, results copy
@@ -1744,6 +1857,12 @@ private:
                                  head + kHeadSelected, lnode);
     q.with_min = wo_.min_check == 0;
     if(q.with_min) q.ismin = is_min_call(f.dn, W, f.ds, E.d_dbs.p, dcode, sel, kb, head + kHeadSelected);
+    // the wave's nodes were made by the root phases (engine stream) or by
+    // other contexts' materialise passes (their last ones cover every node
+    // made so far; this context's own are ahead on its stream)
+    CK(cudaStreamWaitEvent(X.stream, E.ev_main, 0));
+    for(int d = 0; d < kWaveCtx; d++)
+      if(d != c) CK(cudaStreamWaitEvent(X.stream, E.ctx[d].ev[5], 0));
     issue(X, q);
     st_.launches += q.with_min ? 4 : 3;
     f.busy = true;
@@ -1799,15 +1918,26 @@ private:
       CK(cudaStreamSynchronize(E.aux));
       st_.d2h_bytes += (int64_t)(kHeadBytes + sizeof(int4) * nsel);
     }
-    int4 *hsel = (int4 *)(X.h_head.p + kHeadBytes);
+    const int4 *hsel = (const int4 *)(X.h_head.p + kHeadBytes);
     X.sel_hint = std::max<int64_t>(X.sel_hint, 2 * nsel);
-    std::sort(hsel, hsel + nsel, [](const int4 &a, const int4 &b) { return a.x < b.x; });
+    // the candidates grouped by node (the selection records each one's node):
+    // a counting sort, each node's in any order (children are ordered below)
+    std::vector<int32_t> &at = f.sel_at;
+    at.assign((size_t)W + 1, 0);
+    for(int64_t i = 0; i < nsel; i++) {
+      const int32_t n = hsel[i].w >> 2;
+      if(n < 0 || n >= W) throw Error(ST_ERR_STATE, "selected key outside the wave's nodes");
+      at[n + 1]++;
+    }
+    for(int32_t n = 0; n < W; n++) at[n + 1] += at[n];
+    std::vector<int32_t> &order = f.sel_order;
+    order.resize((size_t)nsel);
+    for(int64_t i = 0; i < nsel; i++) order[at[hsel[i].w >> 2]++] = (int32_t)i;
     std::vector<Candidate> cands;
     cands.reserve((size_t)nsel);
-    int32_t n = 0;
-    for(int64_t i = 0; i < nsel; i++) {
-      const int4 e = hsel[i];
-      while(n + 1 < W && hn[n + 1].key_base <= e.x) n++;
+    for(int64_t oi = 0; oi < nsel; oi++) {
+      const int4 e = hsel[order[oi]];
+      const int32_t n = e.w >> 2;
       const JobState &S = *jobs_[pn_[nodes[n]].job];
       if(S.cancelled) continue;
       Candidate cd;
@@ -1815,7 +1945,7 @@ private:
       cd.key = e.x - hn[n].key_base;
       cd.support = e.y;
       cd.cnt = e.z;
-      cd.verdict = wo_.min_check == 0 ? e.w : 2;
+      cd.verdict = wo_.min_check == 0 ? (e.w & 3) : 2;
       cd.ok = cd.verdict == 1;
       if(cd.key < 0 || cd.key >= hn[n].nkeys) throw Error(ST_ERR_STATE, "selected key outside its node");
       // the kernels emit keys of valid extensions only: one that does not
@@ -1868,7 +1998,7 @@ private:
     int64_t list_rows = 0, list_n = 0;
     std::vector<int32_t> list_rb;  // per node: its first list row, or -1
     {
-      // accepted candidates; cands is in key order, so each node's are contiguous
+      // accepted candidates; cands is grouped by node, so each node's are contiguous
       std::vector<int32_t> acc;
       acc.reserve(cands.size());
       for(int32_t i = 0; i < (int32_t)cands.size(); i++)
@@ -2005,33 +2135,33 @@ private:
       std::memcpy(X.h_mat.p, outs.data(), sizeof(ChildOut) * outs.size());
       std::memcpy(X.h_mat.p + outs_bytes, pairs.data(), sizeof(int2) * pairs.size());
       if(list_blk >= 0) std::memcpy(X.h_mat.p + outs_bytes + pairs_bytes, list_rb.data(), sizeof(int32_t) * W);
-      h2d(X.d_mat.p, X.h_mat.p, mat_bytes);
+      h2d(X.d_mat.p, X.h_mat.p, mat_bytes, X.stream);
       const ChildOut *douts = (const ChildOut *)X.d_mat.p;
       X.d_cursor.ensure(outs.size());
-      CK(cudaEventRecord(X.ev[4], E.stream));
+      CK(cudaEventRecord(X.ev[4], X.stream));
       launch_scatter_childmap((const int2 *)(X.d_mat.p + outs_bytes), (int32_t)pairs.size(), X.d_childmap.p,
-                              X.d_cursor.p, (int32_t)outs.size(), E.stream);
+                              X.d_cursor.p, (int32_t)outs.size(), X.stream);
       // lists strategy: the records pass also counts the list rows
       ListBuild lb{ X.d_lnode.p, f.dn, (const int32_t *)(X.d_mat.p + outs_bytes + pairs_bytes) };
-      if(list_blk >= 0) CK(cudaMemsetAsync(list_off, 0, sizeof(int32_t) * (size_t)(list_rows + 1), E.stream));
+      if(list_blk >= 0) CK(cudaMemsetAsync(list_off, 0, sizeof(int32_t) * (size_t)(list_rows + 1), X.stream));
       if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
         launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, f.bm, X.d_bmx.p, f.cnt, f.cstride,
                                    douts, E.d_bytes.p + 1, err_flag(), list_blk >= 0 ? &lb : nullptr,
-                                   list_off + 1, E.stream);
+                                   list_off + 1, X.stream);
       } else {
         // records overflowed (or are disabled): enumerate again
         launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, X.d_bmx.p,
                                 X.d_childmap.p, X.d_cursor.p, douts, E.d_bytes.p + 1, err_flag(), f.join,
-                                f.rule_skip, E.stream);
+                                f.rule_skip, X.stream);
         if(f.rec) X.wanted_rec = std::max<long long>(X.wanted_rec, nrec + nrec / 4);
       }
       if(list_blk >= 0) {
-        launch_fill_lists(f.rec, nrec, lb, list_off, list_rows, list_ent, list_n, list_scr, err_flag(), E.stream);
+        launch_fill_lists(f.rec, nrec, lb, list_off, list_rows, list_ent, list_n, list_scr, err_flag(), X.stream);
         st_.list_entries += list_n;
         st_.launches += 2;
       }
-      CK(cudaEventRecord(X.ev[5], E.stream));
+      CK(cudaEventRecord(X.ev[5], X.stream));
       st_.launches += 2;
       f.mat_pending = true;
     }
@@ -2053,6 +2183,7 @@ private:
     }
     nodes.clear();
     f.busy = false;
+    E.fence();
     st_.host_select_ms += ms_since(t_ready) - (st_.host_min_ms - min_before);
     std::sort(touched.begin(), touched.end());
     touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
@@ -2116,7 +2247,7 @@ private:
 void engine_fail(Engine &e)
 {
   if(e.ready) {
-    cudaStreamSynchronize(e.stream);
+    e.sync_all();
     cudaGetLastError();
     e.destroy();
   }

@@ -349,7 +349,11 @@ __global__ void __launch_bounds__(kMinWarps * 32) k_is_min(const NodeDesc *__res
   const long long nwarps = (long long)gridDim.x * kMinWarps;
   for(long long i = (long long)blockIdx.x * kMinWarps + warp; i < nsel; i += nwarps) {
     const int4 x = sel[i];
-    const NodeDesc &nd = nodes[node_of_key(nodes, nnodes, x.x)];
+    // the node the selection recorded, or (out of range) the search by key
+    int ni = x.w >> 2;
+    if(ni < 0 || ni >= nnodes || x.x < nodes[ni].key_base || x.x >= nodes[ni].key_base + nodes[ni].nkeys)
+      ni = node_of_key(nodes, nnodes, x.x);
+    const NodeDesc &nd = nodes[ni];
     const int len = nd.code_len, n = len + 1;
     int verdict = 2;
     if(n <= kMinE) {
@@ -395,7 +399,7 @@ __global__ void __launch_bounds__(kMinWarps * 32) k_is_min(const NodeDesc *__res
       if(nd.k + 1 <= kMinV) verdict = warp_is_min(S, n, lane);
       __syncwarp();
     }
-    if(lane == 0) sel[i].w = verdict;
+    if(lane == 0) sel[i].w = (x.w & ~3) | verdict;
   }
 }
 

@@ -240,7 +240,8 @@ __global__ void __launch_bounds__(kBlock) k_support(const NodeDesc *__restrict__
 // (overwritten afterwards for the children that are materialised).
 // Counting, one warp per listed key: popcount of its bitmap with prefix
 // counts for the materialise pass; the frequent keys are appended to sel as
-// {key, support, embeddings, 0} (order unspecified) and get keyword = their
+// {key, support, embeddings, node << 2} (order unspecified; the low two bits
+// take the canonicality verdict) and get keyword = their
 // first bitmap word.  counters: [0] selected, [1] embeddings of all keys,
 // [2] listed keys.
 __global__ void __launch_bounds__(kBlock) k_screen_keys(const NodeDesc *__restrict__ nodes, int nnodes,
@@ -338,7 +339,7 @@ __device__ __forceinline__ void listed_done(const int2 kn, const NodeDesc &nd, l
   if(running >= nd.minsup) {
     keyword[kn.x] = wbase;
     const unsigned long long at = atomicAdd(&counters[0], 1ull);
-    if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], 0);
+    if(at < (unsigned long long)sel_cap) sel[at] = make_int4(kn.x, running, cnt[kn.x], kn.y << 2);
     // the total has been read: copy 0 turns into the cursor of copy 0's share
     cnt[kn.x] = 0;
     // lists strategy: a frequent forward key goes into its node's per-row lists

@@ -126,8 +126,9 @@ KernelCall screen_keys_call(const NodeDesc *nodes, int32_t nnodes, int32_t total
 KernelCall count_listed_call(const NodeDesc *nodes, const int2 *listed, const uint32_t *bm, int32_t *cnt,
                              int32_t *bmx, long long *keyword, int4 *sel, int32_t sel_cap,
                              unsigned long long *counters, int32_t *lnode);
-// Canonicality of the selected candidates (gs_ismin.cu): sel[i].w = 1 minimal,
-// 0 not minimal, 2 left to the host.  codes = the wave's code table.
+// Canonicality of the selected candidates (gs_ismin.cu): the low two bits of
+// sel[i].w (above them the candidate's node) = 1 minimal, 0 not minimal, 2
+// left to the host.  codes = the wave's code table.
 KernelCall is_min_call(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *slots, const DevDB *dbs,
                        const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters);
 // childmap[pairs[i].x] = pairs[i].y, and cursor[0..ncursor) = 0
