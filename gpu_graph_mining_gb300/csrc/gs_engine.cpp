@@ -460,11 +460,23 @@ struct Block {
   int32_t refs = 0;
 };
 
+// A column of embedding rows.  Columns form chains: a node's columns are its
+// last column and that column's ancestors (parent), and a column holds one
+// reference on its parent, so that a node needs one reference (its last
+// column) for all of them.
 struct Column {
   int2 *ptr = nullptr;
   int64_t n = 0;
   int32_t refs = 0;
   int32_t blk = -1;
+  int32_t parent = -1;
+};
+
+// A node's view of one of its columns (kept in the node, so that wave
+// descriptors are filled without visiting the column table).
+struct ColRef {
+  const int2 *ptr;
+  int64_t n;
 };
 
 // One frequent pattern of a job's output tree; children in traversal order
@@ -562,7 +574,8 @@ struct PNode {
   int32_t job;
   int32_t pattern;
   SmallVec<DFS, 12> code;
-  SmallVec<int32_t, 12> cols;
+  SmallVec<ColRef, 12> cols;  // column c = pattern vertex c
+  int32_t last_col = -1;      // the node's reference: its last column (the rest by parent links)
   int32_t *gord;
   int32_t gord_blk;
   int64_t nrows;
@@ -932,7 +945,9 @@ struct Engine {
       free_blocks.push_back(b);
     }
   }
-  int32_t new_col(int2 *p, int64_t n, int32_t blk)
+  // a column with one reference (its creator's); it takes a reference on its
+  // parent column, unless adopt (the parent's creator hands its own over)
+  int32_t new_col(int2 *p, int64_t n, int32_t blk, int32_t parent, bool adopt = false)
   {
     int32_t id;
     if(!free_cols.empty()) { id = free_cols.back(); free_cols.pop_back(); }
@@ -941,20 +956,24 @@ struct Engine {
     cols[id].n = n;
     cols[id].refs = 1;
     cols[id].blk = blk;
+    cols[id].parent = parent;
     block_ref(blk);
+    if(parent >= 0 && !adopt) cols[parent].refs++;
     return id;
   }
-  void ref(int32_t id) { cols[id].refs++; }
-  // drops one reference; returns the column's bytes when it was the last
+  // drops one reference, and a released column's reference on its parent;
+  // returns the bytes of the columns released
   int64_t unref(int32_t id)
   {
-    if(--cols[id].refs == 0) {
+    int64_t freed = 0;
+    while(id >= 0 && --cols[id].refs == 0) {
       block_unref(cols[id].blk);
       cols[id].ptr = nullptr;
       free_cols.push_back(id);
-      return cols[id].n * (int64_t)sizeof(int2);
+      freed += cols[id].n * (int64_t)sizeof(int2);
+      id = cols[id].parent;
     }
-    return 0;
+    return freed;
   }
 };
 
@@ -1301,6 +1320,13 @@ private:
   int64_t active_ = 0;
   int64_t stacked_ = 0;          // nodes on all jobs' stacks
   int64_t seen_bytes_[2] = { 0, 0 };
+  // per-wave scratch of finish(), reused
+  struct Mat { int32_t node, cand, pid; };
+  std::vector<Candidate> w_cands_;
+  std::vector<int32_t> w_todo_, w_made_, w_made_at_, w_acc_, w_touched_;
+  std::vector<ChildOut> w_outs_;
+  std::vector<int2> w_pairs_;
+  std::vector<Mat> w_mats_;
 
   void h2d(void *dst, const void *src, size_t n, cudaStream_t s = nullptr)
   {
@@ -1335,6 +1361,7 @@ private:
     PNode &p = pn_[id];
     p.code.assign(nullptr, 0);
     p.cols.assign(nullptr, 0);
+    p.last_col = -1;
     p.list_blk = -1;
     p.list_off = nullptr;
     p.list_ent = nullptr;
@@ -1347,7 +1374,8 @@ private:
   // releases a node's columns and graph ranks
   void drop_node(JobState &S, PNode &p)
   {
-    for(int32_t id : p.cols) S.live_bytes -= E.unref(id);
+    S.live_bytes -= E.unref(p.last_col);
+    p.last_col = -1;
     S.live_bytes -= p.nrows * (int64_t)sizeof(int32_t);
     E.block_unref(p.gord_blk);
     if(p.list_blk >= 0) E.block_unref(p.list_blk);
@@ -1522,8 +1550,10 @@ private:
         nn.job = id;
         nn.pattern = s.pid;
         nn.code.push_back(s.d);
-        nn.cols.push_back(E.new_col(c0, s.n, blk));
-        nn.cols.push_back(E.new_col(c1, s.n, blk));
+        const int32_t id0 = E.new_col(c0, s.n, blk, -1);
+        nn.last_col = E.new_col(c1, s.n, blk, id0, true);
+        nn.cols.push_back(ColRef{ c0, s.n });
+        nn.cols.push_back(ColRef{ c1, s.n });
         nn.gord = gord;
         nn.gord_blk = blk;
         E.block_ref(blk);
@@ -1748,8 +1778,8 @@ private:
         c[4] = e.tolabel;
       }
       for(size_t cc = 0; cc < p.cols.size(); cc++) {
-        hc[co + cc] = E.cols[p.cols[cc]].ptr;
-        hl[co + cc] = (int32_t)E.cols[p.cols[cc]].n;
+        hc[co + cc] = p.cols[cc].ptr;
+        hl[co + cc] = (int32_t)p.cols[cc].n;
         hv[co + cc] = -1;
       }
       for(size_t s = 0; s < L.slots.size(); s++) {
@@ -1933,7 +1963,8 @@ private:
     std::vector<int32_t> &order = f.sel_order;
     order.resize((size_t)nsel);
     for(int64_t i = 0; i < nsel; i++) order[at[hsel[i].w >> 2]++] = (int32_t)i;
-    std::vector<Candidate> cands;
+    std::vector<Candidate> &cands = w_cands_;
+    cands.clear();
     cands.reserve((size_t)nsel);
     for(int64_t oi = 0; oi < nsel; oi++) {
       const int4 e = hsel[order[oi]];
@@ -1966,7 +1997,8 @@ private:
     // canonicality: the GPU's verdicts; the rest on the host, in parallel
     {
       const clk::time_point t0 = clk::now();
-      std::vector<int32_t> todo;
+      std::vector<int32_t> &todo = w_todo_;
+      todo.clear();
       for(int32_t i = 0; i < (int32_t)cands.size(); i++)
         if(cands[i].verdict != 0 && cands[i].verdict != 1) todo.push_back(i);
       st_.min_host += (int64_t)todo.size();
@@ -1984,11 +2016,15 @@ private:
     }
 
     // accepted children: output tree, materialisation slots
-    std::vector<ChildOut> outs;
-    std::vector<int2> pairs;
+    std::vector<ChildOut> &outs = w_outs_;
+    std::vector<int2> &pairs = w_pairs_;
+    outs.clear();
+    pairs.clear();
     // children in node order (a node's children are contiguous, from made_at[n])
-    std::vector<int32_t> made;
-    std::vector<int32_t> made_at(W + 1, 0);
+    std::vector<int32_t> &made = w_made_;
+    std::vector<int32_t> &made_at = w_made_at_;
+    made.clear();
+    made_at.assign((size_t)W + 1, 0);
     // lists strategy: every node with a forward child to materialise keeps
     // per-row lists of its frequent forward extensions (built from this
     // wave's records) for those children's joins
@@ -1999,13 +2035,14 @@ private:
     std::vector<int32_t> list_rb;  // per node: its first list row, or -1
     {
       // accepted candidates; cands is grouped by node, so each node's are contiguous
-      std::vector<int32_t> acc;
+      std::vector<int32_t> &acc = w_acc_;
+      acc.clear();
       acc.reserve(cands.size());
       for(int32_t i = 0; i < (int32_t)cands.size(); i++)
         if(cands[i].ok) acc.push_back(i);
       // pass 1: output tree (reference order) and which children to materialise
-      struct Mat { int32_t node, cand, pid; };
-      std::vector<Mat> mats;
+      std::vector<Mat> &mats = w_mats_;
+      mats.clear();
       mats.reserve(acc.size());
       size_t bytes = 0;
       for(size_t a0 = 0; a0 < acc.size();) {
@@ -2089,8 +2126,8 @@ private:
           const size_t keep = cd.dfs.is_forward() ? p.cols.size() : p.cols.size() - 1;
           nn.cols.reserve(keep + 1);
           nn.cols.assign(p.cols.data(), keep);
-          for(int32_t id : nn.cols) E.ref(id);
-          nn.cols.push_back(E.new_col(col, rowsn, blk));
+          nn.cols.push_back(ColRef{ col, rowsn });
+          nn.last_col = E.new_col(col, rowsn, blk, cd.dfs.is_forward() ? p.last_col : E.cols[p.last_col].parent);
           nn.gord = gord;
           nn.gord_blk = blk;
           E.block_ref(blk);
@@ -2167,7 +2204,8 @@ private:
     }
     // the parents are done: drop their column references and graph ranks
     // (stream order keeps the materialise kernel ahead of any reuse)
-    std::vector<int32_t> touched;
+    std::vector<int32_t> &touched = w_touched_;
+    touched.clear();
     for(int32_t n = W - 1; n >= 0; n--) {
       JobState &S = *jobs_[pn_[nodes[n]].job];
       for(int32_t i = made_at[n + 1] - 1; i >= made_at[n]; i--) S.stack.push_back(made[i]);
