@@ -311,10 +311,15 @@ class Timer:
         return r, e0.elapsed_time(e1)
 
 
-def roofline(stats_all, peak, peak_kind, traffic, traffic_note):
+def roofline(stats_all, peak, peak_kind, traffic, traffic_note, serial_stats=None):
     """Achieved GB/s of the count, materialise and selection kernels: their
     algorithmic bytes (counted inside the kernels) / their device time (CUDA
-    events on the engine's stream), averaged over the timed steps."""
+    events on the wave contexts' streams), averaged over the timed steps.
+    In the timed steps the contexts' streams overlap: one wave's selection and
+    materialise passes share the GPU with another wave's count, so their event
+    spans include time spent sharing it.  serial_stats (untimed passes with
+    every context on one stream, gs_mine_opts.serial) give each kernel's
+    exclusive time: "kernels_one_stream"."""
     n = len(stats_all)
 
     def avg(k):
@@ -335,7 +340,10 @@ def roofline(stats_all, peak, peak_kind, traffic, traffic_note):
             "kernel_ms_per_step": count["kernel_ms_per_step"], "launches_per_step": waves,
             "kernels": {"k_wave count": count, "materialise (k_mat_records, k_wave materialise)": mat,
                         "selection (k_screen_keys + k_count_listed)": sel,
-                        "k_is_min": {"kernel_ms_per_step": avg("min_ms"), "note": "shared memory only"}}}
+                        "k_is_min": {"kernel_ms_per_step": avg("min_ms"), "note": "shared memory only"}},
+            "kernels_note": "event spans on overlapping streams (a pass sharing the GPU with another wave's count)",
+            "kernels_one_stream": roofline(serial_stats, peak, peak_kind, None, None)["kernels"] if serial_stats
+            else None}
 
 
 def mine_timed(g, tm, db, minsup, steps, warmup, kw):
@@ -631,7 +639,9 @@ def main():
     waves = sum(s["waves"] for s in stats_all) / len(stats_all)
     tag = "config%d" % a.config if a.scale == 1.0 and a.extension == "rmpath" else "none"
     traffic, traffic_note = count_traffic(tag, cb, waves)
-    roof = roofline(stats_all, peak, peak_kind, traffic, traffic_note)
+    # each kernel's exclusive time: untimed passes with the wave contexts on one stream
+    _, serial_stats, _ = mine_timed(g, tm, db, minsup, 2, 1, dict(kw, serial=1))
+    roof = roofline(stats_all, peak, peak_kind, traffic, traffic_note, serial_stats)
     launches_per_step = sum(s["launches"] for s in stats_all) / len(stats_all)
 
     # ---- end to end through the C ABI from host arrays

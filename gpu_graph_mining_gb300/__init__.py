@@ -53,7 +53,7 @@ class MineOpts(ctypes.Structure):
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
                 ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
                 ("count_grid", ctypes.c_int32), ("extension", ctypes.c_int32),
-                ("deep_nodes", ctypes.c_int32)]
+                ("deep_nodes", ctypes.c_int32), ("serial", ctypes.c_int32)]
 
 
 # extension strategies (gs_mine_opts.extension)
@@ -326,7 +326,7 @@ def _extension(x):
 
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
           root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0, extension=EXTENSION_RMPATH,
-          deep_nodes=0):
+          deep_nodes=0, serial=0):
     o = MineOpts()
     lib().gs_mine_opts_default(ctypes.byref(o))
     o.max_edges = int(max_edges)
@@ -347,12 +347,13 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
     o.extension = _extension(extension)
     if deep_nodes:
         o.deep_nodes = int(deep_nodes)
+    o.serial = 1 if serial else 0
     return o
 
 
 def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
          wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0,
-         extension=EXTENSION_RMPATH, deep_nodes=0):
+         extension=EXTENSION_RMPATH, deep_nodes=0, serial=0):
     """Mines db at absolute support minsup.
 
     Returns (patterns, stats): patterns is a list of (code, support) with code a
@@ -371,7 +372,7 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
 
     fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
     o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check,
-              launch_mode, count_grid, extension, deep_nodes)
+              launch_mode, count_grid, extension, deep_nodes, serial)
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()

@@ -53,6 +53,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   if(o->count_grid > 0 && o->count_grid <= 1024) m.count_grid = o->count_grid;
   m.extension = o->extension == GS_EXTENSION_LISTS ? 1 : 0;
   if(o->deep_nodes > 0) m.deep_nodes = o->deep_nodes;
+  m.serial = o->serial == 1 ? 1 : 0;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -271,6 +272,7 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->count_grid = m.count_grid;
   o->deep_nodes = m.deep_nodes;
   o->extension = m.extension;
+  o->serial = m.serial;
 }
 
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,

@@ -1328,6 +1328,8 @@ private:
   std::vector<int2> w_pairs_;
   std::vector<Mat> w_mats_;
 
+  // a wave context's stream (all on the engine's with the serial option)
+  cudaStream_t cs(const WaveCtx &X) const { return wo_.serial ? E.stream : X.stream; }
   void h2d(void *dst, const void *src, size_t n, cudaStream_t s = nullptr)
   {
     CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s ? s : E.stream));
@@ -1588,22 +1590,23 @@ private:
   // its count-kernel variant (node parameters updated), or launched directly.
   void issue(WaveCtx &X, WaveSeq &q)
   {
+    const cudaStream_t st = cs(X);
     st_.h2d_bytes += (int64_t)q.desc_bytes;
     st_.d2h_bytes += (int64_t)q.d2h_bytes;
     if(wo_.launch_mode != 0) {
-      CK(cudaMemcpyAsync(q.desc_dst, q.desc_src, q.desc_bytes, cudaMemcpyHostToDevice, X.stream));
-      CK(cudaMemsetAsync(q.zero, 0, q.zero_bytes, X.stream));
-      CK(cudaMemsetAsync(q.head, 0, kHeadBytes, X.stream));
-      CK(cudaEventRecord(X.ev[0], X.stream));
-      CK(q.count.run(X.stream));
-      CK(cudaEventRecord(X.ev[1], X.stream));
-      CK(q.screen.run(X.stream));
-      CK(q.listed.run(X.stream));
-      CK(cudaEventRecord(X.ev[6], X.stream));
-      if(q.with_min) CK(q.ismin.run(X.stream));
-      CK(cudaEventRecord(X.ev[2], X.stream));
-      CK(cudaMemcpyAsync(q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost, X.stream));
-      CK(cudaEventRecord(X.ev[3], X.stream));
+      CK(cudaMemcpyAsync(q.desc_dst, q.desc_src, q.desc_bytes, cudaMemcpyHostToDevice, st));
+      CK(cudaMemsetAsync(q.zero, 0, q.zero_bytes, st));
+      CK(cudaMemsetAsync(q.head, 0, kHeadBytes, st));
+      CK(cudaEventRecord(X.ev[0], st));
+      CK(q.count.run(st));
+      CK(cudaEventRecord(X.ev[1], st));
+      CK(q.screen.run(st));
+      CK(q.listed.run(st));
+      CK(cudaEventRecord(X.ev[6], st));
+      if(q.with_min) CK(q.ismin.run(st));
+      CK(cudaEventRecord(X.ev[2], st));
+      CK(cudaMemcpyAsync(q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost, st));
+      CK(cudaEventRecord(X.ev[3], st));
       return;
     }
     WaveGraph *G = nullptr;
@@ -1652,7 +1655,7 @@ private:
       if(q.with_min) CK(cudaGraphExecKernelNodeSetParams(G->x, G->ismin, &km));
       CK(cudaGraphExecMemcpyNodeSetParams1D(G->x, G->d2h, q.head_host, q.head, q.d2h_bytes, cudaMemcpyDeviceToHost));
     }
-    CK(cudaGraphLaunch(G->x, X.stream));
+    CK(cudaGraphLaunch(G->x, st));
   }
 
   // ---- launch one wave into context c: descriptors, count, support, results copy
@@ -1890,9 +1893,11 @@ private:
     // the wave's nodes were made by the root phases (engine stream) or by
     // other contexts' materialise passes (their last ones cover every node
     // made so far; this context's own are ahead on its stream)
-    CK(cudaStreamWaitEvent(X.stream, E.ev_main, 0));
-    for(int d = 0; d < kWaveCtx; d++)
-      if(d != c) CK(cudaStreamWaitEvent(X.stream, E.ctx[d].ev[5], 0));
+    if(!wo_.serial) {
+      CK(cudaStreamWaitEvent(X.stream, E.ev_main, 0));
+      for(int d = 0; d < kWaveCtx; d++)
+        if(d != c) CK(cudaStreamWaitEvent(X.stream, E.ctx[d].ev[5], 0));
+    }
     issue(X, q);
     st_.launches += q.with_min ? 4 : 3;
     f.busy = true;
@@ -1904,6 +1909,7 @@ private:
   void finish(int c)
   {
     WaveCtx &X = E.ctx[c];
+    const cudaStream_t st = cs(X);
     Flight &f = fl_[c];
     {
       const clk::time_point t0 = clk::now();
@@ -2172,33 +2178,33 @@ private:
       std::memcpy(X.h_mat.p, outs.data(), sizeof(ChildOut) * outs.size());
       std::memcpy(X.h_mat.p + outs_bytes, pairs.data(), sizeof(int2) * pairs.size());
       if(list_blk >= 0) std::memcpy(X.h_mat.p + outs_bytes + pairs_bytes, list_rb.data(), sizeof(int32_t) * W);
-      h2d(X.d_mat.p, X.h_mat.p, mat_bytes, X.stream);
+      h2d(X.d_mat.p, X.h_mat.p, mat_bytes, st);
       const ChildOut *douts = (const ChildOut *)X.d_mat.p;
       X.d_cursor.ensure(outs.size());
-      CK(cudaEventRecord(X.ev[4], X.stream));
+      CK(cudaEventRecord(X.ev[4], st));
       launch_scatter_childmap((const int2 *)(X.d_mat.p + outs_bytes), (int32_t)pairs.size(), X.d_childmap.p,
-                              X.d_cursor.p, (int32_t)outs.size(), X.stream);
+                              X.d_cursor.p, (int32_t)outs.size(), st);
       // lists strategy: the records pass also counts the list rows
       ListBuild lb{ X.d_lnode.p, f.dn, (const int32_t *)(X.d_mat.p + outs_bytes + pairs_bytes) };
-      if(list_blk >= 0) CK(cudaMemsetAsync(list_off, 0, sizeof(int32_t) * (size_t)(list_rows + 1), X.stream));
+      if(list_blk >= 0) CK(cudaMemsetAsync(list_off, 0, sizeof(int32_t) * (size_t)(list_rows + 1), st));
       if(f.rec && nrec <= f.rec_cap) {
         // record-driven: one thread per extension record, no graph access
         launch_materialize_records(f.rec, nrec, X.d_childmap.p, X.d_keyword.p, f.bm, X.d_bmx.p, f.cnt, f.cstride,
                                    douts, E.d_bytes.p + 1, err_flag(), list_blk >= 0 ? &lb : nullptr,
-                                   list_off + 1, X.stream);
+                                   list_off + 1, st);
       } else {
         // records overflowed (or are disabled): enumerate again
         launch_wave_materialize(f.dn, W, f.tb, f.kmax, f.small, f.dc, f.dl, f.ds, f.dv, E.d_dbs.p, f.bm, X.d_bmx.p,
                                 X.d_childmap.p, X.d_cursor.p, douts, E.d_bytes.p + 1, err_flag(), f.join,
-                                f.rule_skip, X.stream);
+                                f.rule_skip, st);
         if(f.rec) X.wanted_rec = std::max<long long>(X.wanted_rec, nrec + nrec / 4);
       }
       if(list_blk >= 0) {
-        launch_fill_lists(f.rec, nrec, lb, list_off, list_rows, list_ent, list_n, list_scr, err_flag(), X.stream);
+        launch_fill_lists(f.rec, nrec, lb, list_off, list_rows, list_ent, list_n, list_scr, err_flag(), st);
         st_.list_entries += list_n;
         st_.launches += 2;
       }
-      CK(cudaEventRecord(X.ev[5], X.stream));
+      CK(cudaEventRecord(X.ev[5], st));
       st_.launches += 2;
       f.mat_pending = true;
     }

@@ -129,6 +129,7 @@ struct MineOptions {
                               // lists of frequent forward extensions and scan only their new
                               // right-most vertex (the reference's gspan_cuda_lists)
   int32_t deep_nodes = 0;     // a third wave context launches while this many nodes are queued (0 = wave_nodes)
+  int32_t serial = 0;         // 1: every wave context issues on the engine's stream (no kernels overlap)
 };
 
 struct MineStats {

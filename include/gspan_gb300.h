@@ -191,6 +191,10 @@ typedef struct gs_mine_opts {
                           nodes are queued; 0 = wave_nodes (default), 1 = always.  More waves in flight
                           hide more of the host's work per wave when a workload has many small nodes;
                           a short queue split three ways makes smaller waves. */
+  int32_t serial;      /* 0 = each wave context issues on its own stream, so that one wave's selection and
+                          materialise passes run beside another wave's count (default); 1 = all on one
+                          stream: no two kernels overlap, so per-kernel times in gs_mine_stats are
+                          exclusive.  Same patterns and supports. */
 } gs_mine_opts;
 
 #define GS_EXTENSION_RMPATH 0

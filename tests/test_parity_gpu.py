@@ -305,6 +305,38 @@ def test_deep_wave_contexts_keep_results(gs):
     assert lines == read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s10.txt"))
 
 
+def test_one_stream_equals_context_streams(gs):
+    # every wave context on the engine's one stream (serial) or each on its
+    # own (default): the same waves, patterns and supports
+    db = gs.Database.generate(2, scale=0.05)
+    s = max(2, int(0.01 * len(db)))
+    a, sa = gs.mine(db, s)
+    b, sb = gs.mine(db, s, serial=1)
+    assert a == b and sa["waves"] == sb["waves"]
+    dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.03) for i in range(4)]
+    sups = [max(2, int(0.05 * len(d))) for d in dbs]
+    c, sc = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, deep_nodes=1, wave_nodes=64)
+    d, sd = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, deep_nodes=1, wave_nodes=64, serial=1)
+    assert c == d and sc["waves"] == sd["waves"]
+
+
+def test_tight_pool_reuses_fenced_blocks(gs):
+    # with the device pool capped near the run's peak, blocks released on the
+    # host are handed out again only after every stream has passed their last
+    # reader (waiting on the fences instead of growing the pool)
+    db = gs.Database.generate(2, scale=0.1)
+    s = max(2, int(0.01 * len(db)))
+    a, sa = gs.mine(db, s)
+    try:
+        gs.engine_reset()
+        gs.set_pool_bytes(max(2 * sa["peak_pool_bytes"], 32 << 20))
+        b, sb = gs.mine(db, s)
+    finally:
+        gs.set_pool_bytes(0)
+        gs.engine_reset()
+    assert a == b and sb["peak_pool_bytes"] <= max(2 * sa["peak_pool_bytes"], 32 << 20)
+
+
 def test_autotune_keeps_results(gs):
     dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.05) for i in range(3)]
     sups = [max(2, int(0.05 * len(d))) for d in dbs]
