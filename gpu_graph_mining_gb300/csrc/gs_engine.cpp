@@ -712,8 +712,8 @@ struct WaveCtx {
   HBuf<long long> h_keyword;
   HBuf<unsigned long long> h_misc;  // [0] records written, [1] consistency flags, [2..3] = d_selc
   // 0/1 count, 1/6 selection, 6/2 canonicality, 3 results copied, 4/5 materialise
-  // (root contexts: 0/1 count and support, 3 read back, 5 first embeddings; the
-  // first root context's 6 follows a group of jobs' read-backs)
+  // (the root context: 0/1 a group's count and support, 3 read back, 5 first
+  // embeddings)
   cudaEvent_t ev[7] = {};
   bool have_events = false;
   std::vector<WaveGraph> graphs;
