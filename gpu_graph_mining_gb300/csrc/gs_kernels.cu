@@ -173,13 +173,17 @@ __global__ void __launch_bounds__(kBlock) k_root_count(const RootJob *__restrict
   root_tiles<false>(jobs, njobs, tiles, dbs, bm, nullptr, cnt, nullptr, nullptr, bytes, nullptr);
 }
 
-// Per key of the group: the job's counter copies turn into the offsets of
-// each copy's share (copy q >= 1: the count of copies 0..q-1), the total goes
-// to tot[key], and copy 0 starts at 0 as the materialise pass's cursor.
+// Per key of the group, one warp: the job's counter copies turn into the
+// offsets of each copy's share (copy q: the count of copies 0..q-1, a warp
+// scan over the copies; copy 0 starts at 0 as the materialise pass's cursor)
+// and the total goes to tot[key].
 __global__ void __launch_bounds__(kBlock) k_sum_copies(const RootJob *__restrict__ jobs, int njobs, int total_keys,
                                                         int32_t *cnt, int32_t *tot)
 {
-  for(int kg = blockIdx.x * blockDim.x + threadIdx.x; kg < total_keys; kg += gridDim.x * blockDim.x) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for(int kg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; kg < total_keys; kg += warps) {
     int lo = 0, hi = njobs - 1;
     while(lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -187,14 +191,19 @@ __global__ void __launch_bounds__(kBlock) k_sum_copies(const RootJob *__restrict
     }
     const RootJob &J = jobs[lo];
     int32_t *c0 = cnt + J.cnt_base + (kg - J.key_base);
-    int c = c0[0];
-    for(int q = 1; q < J.copies; q++) {
-      const int x = c0[(long long)q * J.R];
-      c0[(long long)q * J.R] = c;
-      c += x;
+    int run = 0;
+    for(int q0 = 0; q0 < J.copies; q0 += 32) {
+      const int q = q0 + lane;
+      const int x = q < J.copies ? c0[(long long)q * J.R] : 0;
+      int incl = x;
+      for(int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(full, incl, o);
+        if(lane >= o) incl += t;
+      }
+      if(q < J.copies) c0[(long long)q * J.R] = run + incl - x;
+      run += __shfl_sync(full, incl, 31);
     }
-    tot[kg] = c;
-    c0[0] = 0;
+    if(lane == 0) tot[kg] = run;
   }
 }
 
@@ -563,7 +572,8 @@ void launch_root_count(const RootJob *jobs, int32_t njobs, long long tiles, cons
                        int32_t *cnt, int32_t *tot, int32_t total_keys, unsigned long long *bytes, cudaStream_t s)
 {
   if(tiles > 0) k_root_count<<<grid_for(tiles * 32), kBlock, 0, s>>>(jobs, njobs, tiles, dbs, bm, cnt, bytes);
-  if(total_keys > 0) k_sum_copies<<<grid_for(total_keys), kBlock, 0, s>>>(jobs, njobs, total_keys, cnt, tot);
+  if(total_keys > 0)
+    k_sum_copies<<<grid_for((long long)total_keys * 32), kBlock, 0, s>>>(jobs, njobs, total_keys, cnt, tot);
 }
 
 void launch_root_materialize(const RootJob *jobs, int32_t njobs, long long tiles, const DevDB *dbs,
