@@ -227,8 +227,7 @@ namespace {
 
 // First-fit sub-allocator over a few large cudaMalloc chunks.  Memory freed
 // here is handed out again at once: the engine returns a block only after
-// every stream has passed the work queued before the block's last reference
-// was dropped (Engine::fence / reap).
+// the last passes that may read it have completed (Engine::reap).
 class Pool {
 public:
   void set_limit(int64_t b) { limit_ = b; }
@@ -719,6 +718,10 @@ struct WaveCtx {
   std::vector<WaveGraph> graphs;
   // the context's stream (wave contexts; the root context uses the engine's)
   cudaStream_t stream = nullptr;
+  // records of ev[5] (materialise passes), and the records of the engine's
+  // ev_main and of the other contexts' ev[5] this context's stream already waits for
+  uint64_t mat_gen = 0, seen_main = 0;
+  uint64_t seen_mat[8] = {};
 
   void init(bool own_stream)
   {
@@ -754,7 +757,7 @@ struct WaveCtx {
   }
 };
 
-constexpr int kMaxDbSlots = 256;
+constexpr int kMaxDbSlots = 256;  // databases one scheduler keeps in its device table before it grows
 // Waves whose databases hold at most three quarters of the L2 in adjacency
 // bytes (12 per entry) skip the entries below a forward rule (sorted
 // adjacency): about 97 MiB on a GB300.
@@ -778,7 +781,8 @@ int64_t rule_skip_adj_bytes()
 #ifndef GS_WAVE_CTX
 #define GS_WAVE_CTX 3
 #endif
-constexpr int kWaveCtx = GS_WAVE_CTX;   // databases one scheduler keeps in its device table before it grows
+constexpr int kWaveCtx = GS_WAVE_CTX;
+static_assert(kWaveCtx <= 8, "WaveCtx::seen_mat holds 8 contexts");
 
 struct Engine {
   // Streams: the engine's (database table, root phases) and one per wave
@@ -805,16 +809,16 @@ struct Engine {
   static constexpr int64_t kRootGroupBytes = 1LL << 30;   // bitmap bytes (one job at least)
   bool ready = false;
   // Pool blocks whose last reference was dropped go back to the pool only
-  // after every stream has passed the work queued until then (a fence: one
-  // event per stream), since a pass queued on another stream may still read
-  // them.
-  struct Fence {
-    std::vector<cudaEvent_t> ev;
-    std::vector<void *> blocks;
-  };
+  // after every wave context's last materialise pass has completed: the
+  // only passes that read a node's memory after the host dropped the node
+  // are the materialise passes queued for its wave (the record-driven pass
+  // reads records, the enumerating fallback the wave's columns); counts read
+  // live nodes only, root phases write new blocks only.  Each context's
+  // event 5 follows its latest materialise pass, so when every context's
+  // event 5 has completed, every block released so far is free (a later
+  // record of an event only makes the wait longer).
   std::vector<void *> released;
-  std::deque<Fence> fences;
-  std::vector<cudaEvent_t> spare_ev;
+  uint64_t main_gen = 0;          // records of ev_main
 
   void init(int threads)
   {
@@ -841,12 +845,7 @@ struct Engine {
   {
     if(!ready) return;
     sync_all();
-    for(Fence &f : fences)
-      for(cudaEvent_t e : f.ev) cudaEventDestroy(e);
-    fences.clear();
     released.clear();
-    for(cudaEvent_t e : spare_ev) cudaEventDestroy(e);
-    spare_ev.clear();
     if(ev_main) cudaEventDestroy(ev_main);
     ev_main = nullptr;
     pool.destroy();
@@ -881,59 +880,33 @@ struct Engine {
     for(auto &c : ctx)
       if(c.stream) cudaStreamSynchronize(c.stream);
   }
-  // a fence over the blocks released since the last one
-  void fence()
-  {
-    if(released.empty()) return;
-    Fence f;
-    auto rec = [&](cudaStream_t s) {
-      cudaEvent_t e;
-      if(!spare_ev.empty()) { e = spare_ev.back(); spare_ev.pop_back(); }
-      else CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      CK(cudaEventRecord(e, s));
-      f.ev.push_back(e);
-    };
-    rec(stream);
-    for(auto &c : ctx)
-      if(c.stream) rec(c.stream);
-    f.blocks.swap(released);
-    fences.push_back(std::move(f));
-  }
-  // returns fenced blocks to the pool: the passed fences (wait: also the
-  // oldest one not passed yet).  Returns false when no fence was left.
+  // returns the released blocks to the pool once every context's last
+  // materialise pass has completed (wait: waits for them).  Returns false
+  // when nothing was released.
   bool reap(bool wait)
   {
-    bool any = false;
-    while(!fences.empty()) {
-      Fence &f = fences.front();
-      bool passed = true;
-      for(cudaEvent_t e : f.ev) {
-        const cudaError_t q = cudaEventQuery(e);
-        if(q == cudaErrorNotReady) { passed = false; break; }
+    if(released.empty()) return false;
+    for(auto &c : ctx) {
+      if(!c.have_events) continue;
+      const cudaError_t q = cudaEventQuery(c.ev[5]);
+      if(q == cudaErrorNotReady) {
+        if(!wait) return false;
+        CK(cudaEventSynchronize(c.ev[5]));
+      } else {
         CK(q);
       }
-      if(!passed) {
-        if(!wait) break;
-        for(cudaEvent_t e : f.ev) CK(cudaEventSynchronize(e));
-        wait = false;
-      }
-      for(void *b : f.blocks) pool.release(b);
-      for(cudaEvent_t e : f.ev) spare_ev.push_back(e);
-      fences.pop_front();
-      any = true;
     }
-    return any;
+    for(void *b : released) pool.release(b);
+    released.clear();
+    return true;
   }
   void *take_pool(size_t bytes)
   {
-    fence();
     reap(false);
-    for(;;) {
+    if(void *p = pool.try_alloc(bytes)) return p;
+    // released blocks first, the pool grows only when none is left
+    if(reap(true))
       if(void *p = pool.try_alloc(bytes)) return p;
-      // fenced blocks first, the pool grows only when none is left
-      if(fences.empty()) break;
-      reap(true);
-    }
     return pool.alloc(bytes);
   }
   void block_ref(int32_t b) { blocks[b].refs++; }
@@ -1152,8 +1125,8 @@ struct Flight {
 // stream: a wave's count waits for the engine's stream (database table, root
 // levels) and for every other context's last materialise pass, so that its
 // nodes' columns are written before it reads them; pool memory released on
-// the host is reused only after every stream has passed its last reader
-// (Engine::fence).
+// the host is reused only after every context's last materialise pass has
+// completed (Engine::reap).
 class Sched {
 public:
   Sched(Engine &e, const MineOptions &wo, MineStats &st) : E(e), wo_(wo), st_(st)
@@ -1170,6 +1143,7 @@ public:
     const int32_t id = enter(j);
     root_phase(std::vector<int32_t>{ id });
     CK(cudaEventRecord(E.ev_main, E.stream));
+    E.main_gen++;
     if(jobs_[id]->pending == 0) complete(id);
     return id;
   }
@@ -1182,6 +1156,7 @@ public:
     for(const MineJob &j : js) ids.push_back(enter(j));
     root_phase(ids);
     CK(cudaEventRecord(E.ev_main, E.stream));
+    E.main_gen++;
     for(int32_t id : ids)
       if(jobs_[id]->pending == 0) complete(id);
   }
@@ -1289,7 +1264,6 @@ public:
     unsigned long long bytes[4] = { 0, 0, 0, 0 };
     d2h(bytes, E.d_bytes.p, sizeof(bytes));
     CK(cudaStreamSynchronize(E.stream));
-    E.fence();
     E.reap(false);
     CK(cudaGetLastError());
     check_flags(bytes[3]);
@@ -1894,9 +1868,15 @@ private:
     // other contexts' materialise passes (their last ones cover every node
     // made so far; this context's own are ahead on its stream)
     if(!wo_.serial) {
-      CK(cudaStreamWaitEvent(X.stream, E.ev_main, 0));
+      if(X.seen_main != E.main_gen) {
+        CK(cudaStreamWaitEvent(X.stream, E.ev_main, 0));
+        X.seen_main = E.main_gen;
+      }
       for(int d = 0; d < kWaveCtx; d++)
-        if(d != c) CK(cudaStreamWaitEvent(X.stream, E.ctx[d].ev[5], 0));
+        if(d != c && X.seen_mat[d] != E.ctx[d].mat_gen) {
+          CK(cudaStreamWaitEvent(X.stream, E.ctx[d].ev[5], 0));
+          X.seen_mat[d] = E.ctx[d].mat_gen;
+        }
     }
     issue(X, q);
     st_.launches += q.with_min ? 4 : 3;
@@ -2205,6 +2185,7 @@ private:
         st_.launches += 2;
       }
       CK(cudaEventRecord(X.ev[5], st));
+      X.mat_gen++;
       st_.launches += 2;
       f.mat_pending = true;
     }
@@ -2227,7 +2208,6 @@ private:
     }
     nodes.clear();
     f.busy = false;
-    E.fence();
     st_.host_select_ms += ms_since(t_ready) - (st_.host_min_ms - min_before);
     std::sort(touched.begin(), touched.end());
     touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
