@@ -475,7 +475,8 @@ def bench_batch(a, g, tm, steps):
             "steps": steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": "batch: 64 databases of generator configuration 3 (seeds 1000-1063), minsup 5%, "
-                                   "one gs_mine_batch call with autotuned wave options",
+                                   "one gs_mine_batch call with autotuned wave options (the batch split over "
+                                   "the autotuned number of schedulers, each on its own host thread)",
                        "graphs": sum(len(d) for d in dbs),
                        "l2": "flushed between steps (256 MiB write)"},
             "patterns_per_step": pats,

@@ -53,7 +53,7 @@ class MineOpts(ctypes.Structure):
                 ("root_part", ctypes.c_int32), ("root_parts", ctypes.c_int32),
                 ("min_check", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
                 ("count_grid", ctypes.c_int32), ("extension", ctypes.c_int32),
-                ("deep_nodes", ctypes.c_int32), ("serial", ctypes.c_int32)]
+                ("deep_nodes", ctypes.c_int32), ("serial", ctypes.c_int32), ("schedulers", ctypes.c_int32)]
 
 
 # extension strategies (gs_mine_opts.extension)
@@ -69,7 +69,7 @@ class ConvertInfo(ctypes.Structure):
 class TuneReport(ctypes.Structure):
     _fields_ = [("trials", ctypes.c_int32), ("wave_nodes", ctypes.c_int32), ("wave_rows", ctypes.c_int64),
                 ("count_grid", ctypes.c_int32), ("deep_nodes", ctypes.c_int32), ("base_ms", ctypes.c_double),
-                ("best_ms", ctypes.c_double)]
+                ("best_ms", ctypes.c_double), ("schedulers", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -326,7 +326,7 @@ def _extension(x):
 
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
           root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0, extension=EXTENSION_RMPATH,
-          deep_nodes=0, serial=0):
+          deep_nodes=0, serial=0, schedulers=0):
     o = MineOpts()
     lib().gs_mine_opts_default(ctypes.byref(o))
     o.max_edges = int(max_edges)
@@ -348,6 +348,7 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
     if deep_nodes:
         o.deep_nodes = int(deep_nodes)
     o.serial = 1 if serial else 0
+    o.schedulers = int(schedulers)
     return o
 
 
@@ -427,7 +428,7 @@ def autotune(dbs, minsups, **kw):
     r = TuneReport()
     _check(lib().gs_autotune(hs, len(dbs), ms, ctypes.byref(o), ctypes.byref(r)))
     return ({"wave_nodes": o.wave_nodes, "wave_rows": o.wave_rows, "count_grid": o.count_grid,
-             "deep_nodes": o.deep_nodes}, r.as_dict())
+             "deep_nodes": o.deep_nodes, "schedulers": o.schedulers}, r.as_dict())
 
 
 def mine_batch(dbs, minsups, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True,

@@ -54,6 +54,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   m.extension = o->extension == GS_EXTENSION_LISTS ? 1 : 0;
   if(o->deep_nodes > 0) m.deep_nodes = o->deep_nodes;
   m.serial = o->serial == 1 ? 1 : 0;
+  if(o->schedulers > 0 && o->schedulers <= 64) m.schedulers = o->schedulers;
   if(o->root_parts > 1 && o->root_part >= 0 && o->root_part < o->root_parts) {
     m.root_parts = o->root_parts;
     m.root_part = o->root_part;
@@ -273,6 +274,7 @@ void gs_mine_opts_default(gs_mine_opts *o)
   o->deep_nodes = m.deep_nodes;
   o->extension = m.extension;
   o->serial = m.serial;
+  o->schedulers = m.schedulers;
 }
 
 gs_status gs_mine_ex(gs_db *db, int32_t abs_minsup, const gs_mine_opts *opts, gs_emit_fn emit, void *user,
@@ -378,17 +380,19 @@ gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, 
   opts->wave_rows = best.wave_rows;
   opts->count_grid = best.count_grid;
   opts->deep_nodes = best.deep_nodes;
+  opts->schedulers = best.schedulers;
   if(report) {
     report->trials = (int32_t)trials.size();
     report->wave_nodes = best.wave_nodes;
     report->wave_rows = best.wave_rows;
     report->count_grid = best.count_grid;
     report->deep_nodes = best.deep_nodes;
+    report->schedulers = best.schedulers;
     report->base_ms = trials.front().ms;
     double b = trials.front().ms;
     for(const auto &t : trials)
       if(t.wave_nodes == best.wave_nodes && t.wave_rows == best.wave_rows && t.count_grid == best.count_grid &&
-         t.deep_nodes == best.deep_nodes)
+         t.deep_nodes == best.deep_nodes && t.schedulers == best.schedulers)
         b = t.ms;
     report->best_ms = b;
   }

@@ -966,6 +966,10 @@ struct Carver {
 
 std::mutex g_mu;
 Engine g_engine;
+// engines of the extra schedulers of a batch split over host threads
+constexpr int kMaxSchedulers = 4;
+Engine g_extra[kMaxSchedulers - 1];
+int64_t g_pool_limit = 0;
 
 inline int32_t words_for(int64_t support) { return (int32_t)((support + 31) / 32); }
 
@@ -1149,7 +1153,8 @@ public:
   }
 
   // Several jobs at once: their root levels are counted together.
-  void add_all(const std::vector<MineJob> &js)
+  void add_all(const std::vector<MineJob> &js) { add_all_ids(js); }
+  std::vector<int32_t> add_all_ids(const std::vector<MineJob> &js)
   {
     std::vector<int32_t> ids;
     ids.reserve(js.size());
@@ -1159,6 +1164,7 @@ public:
     E.main_gen++;
     for(int32_t id : ids)
       if(jobs_[id]->pending == 0) complete(id);
+    return ids;
   }
 
   // A job's checks, its database resident and in the device table, its state.
@@ -1294,6 +1300,7 @@ private:
   int64_t active_ = 0;
   int64_t stacked_ = 0;          // nodes on all jobs' stacks
   int64_t seen_bytes_[2] = { 0, 0 };
+  bool defer_emit_ = false;
   // per-wave scratch of finish(), reused
   struct Mat { int32_t node, cand, pid; };
   std::vector<Candidate> w_cands_;
@@ -1367,14 +1374,33 @@ private:
     order_.erase(std::find(order_.begin(), order_.end(), id));
     done_.push_back(id);
     if(!S.cancelled) {
-      ScopeMs t(st_.host_emit_ms);
       S.patterns = (int64_t)S.pats.size();
       st_.patterns += S.patterns;
+      if(defer_emit_) return;  // emitted later by emit_deferred, on the caller's thread
+      ScopeMs t(st_.host_emit_ms);
       emit(S);
     }
     std::vector<PatternRec>().swap(S.pats);
     std::vector<int32_t>().swap(S.roots);
   }
+
+public:
+  // Schedulers run on worker threads keep the finished jobs' pattern trees
+  // and emit them when the caller asks (the callbacks stay on its thread).
+  void set_defer_emit(bool v) { defer_emit_ = v; }
+  void emit_deferred(int32_t id)
+  {
+    JobState &S = *jobs_[id];
+    if(!S.done || S.cancelled) return;
+    {
+      ScopeMs t(st_.host_emit_ms);
+      emit(S);
+    }
+    std::vector<PatternRec>().swap(S.pats);
+    std::vector<int32_t>().swap(S.roots);
+  }
+
+private:
 
   // ---- root level: all frequent 1-edge codes of one job
   // The root level of jobs, in groups: every root triple's support and
@@ -2279,6 +2305,107 @@ void engine_fail(Engine &e)
 
 }  // namespace
 
+namespace {
+
+void add_stats(MineStats &a, const MineStats &b)
+{
+  a.patterns += b.patterns; a.waves += b.waves; a.launches += b.launches; a.nodes += b.nodes; a.rows += b.rows;
+  a.extensions += b.extensions; a.candidates += b.candidates; a.count_bytes += b.count_bytes;
+  a.mat_bytes += b.mat_bytes; a.count_ms += b.count_ms; a.mat_ms += b.mat_ms; a.support_ms += b.support_ms;
+  a.root_ms += b.root_ms; a.host_min_ms += b.host_min_ms; a.peak_pool_bytes += b.peak_pool_bytes;
+  a.h2d_bytes += b.h2d_bytes; a.d2h_bytes += b.d2h_bytes; a.host_build_ms += b.host_build_ms;
+  a.host_wait_ms += b.host_wait_ms; a.host_select_ms += b.host_select_ms; a.host_emit_ms += b.host_emit_ms;
+  a.min_host += b.min_host; a.list_entries += b.list_entries; a.join_nodes += b.join_nodes;
+  a.sel_bytes += b.sel_bytes; a.sel_ms += b.sel_ms; a.min_ms += b.min_ms;
+}
+
+// A batch split over P schedulers, each with its own engine (pool, wave
+// contexts, streams) on its own host thread: the host's per-node work, which
+// bounds a batch of many small databases, runs on P cores while the GPU runs
+// the P schedulers' waves side by side.  Jobs go to the scheduler with the
+// fewest graphs so far (largest first); each scheduler mines its jobs as one
+// batch.  Patterns are emitted afterwards on the calling thread, job by job
+// in batch order.
+int run_jobs_split(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats &st, std::string &err,
+                   int P)
+{
+  const clk::time_point t0 = clk::now();
+  // databases resident before the threads start (a database may appear twice)
+  for(auto &j : jobs)
+    if(!j.db->resident) {
+      j.db->upload();
+      st.h2d_bytes += (int64_t)j.db->d_bytes;
+    }
+  std::vector<int32_t> order(jobs.size());
+  for(size_t i = 0; i < jobs.size(); i++) order[i] = (int32_t)i;
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return jobs[a].db->host.n_graphs > jobs[b].db->host.n_graphs;
+  });
+  std::vector<std::vector<int32_t>> part(P);
+  std::vector<int64_t> load(P, 0);
+  for(int32_t i : order) {
+    const int p = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    part[p].push_back(i);
+    load[p] += jobs[i].db->host.n_graphs;
+  }
+  for(auto &v : part) std::sort(v.begin(), v.end());
+  std::vector<MineStats> pst(P);
+  std::vector<std::unique_ptr<Sched>> sch(P);
+  std::vector<std::vector<int32_t>> ids(P);
+  std::vector<int> prc(P, ST_OK);
+  std::vector<std::string> perr(P);
+  auto engine = [](int p) -> Engine & { return p == 0 ? g_engine : g_extra[p - 1]; };
+  auto work = [&](int p) {
+    try {
+      CK(cudaSetDevice(0));
+      Engine &E = engine(p);
+      E.pool_limit = g_pool_limit;
+      E.init(wave_opt.threads);
+      sch[p].reset(new Sched(E, wave_opt, pst[p]));
+      sch[p]->set_defer_emit(true);
+      std::vector<MineJob> js;
+      for(int32_t i : part[p]) js.push_back(jobs[i]);
+      ids[p] = sch[p]->add_all_ids(js);
+      while(!sch[p]->idle()) sch[p]->step();
+      sch[p]->sync_stats();
+    } catch(const Error &e) {
+      prc[p] = e.code;
+      perr[p] = e.what();
+    } catch(const std::exception &e) {
+      prc[p] = ST_ERR_STATE;
+      perr[p] = e.what();
+    }
+  };
+  std::vector<std::thread> th;
+  for(int p = 1; p < P; p++)
+    if(!part[p].empty()) th.emplace_back(work, p);
+  if(!part[0].empty()) work(0);
+  for(auto &t : th) t.join();
+  for(int p = 0; p < P; p++)
+    if(prc[p] != ST_OK) {
+      err = perr[p];
+      const int rc = prc[p];
+      for(int q = 0; q < P; q++) {
+        sch[q].reset();
+        if(prc[q] != ST_OK) engine_fail(engine(q));
+      }
+      return rc;
+    }
+  // patterns in batch order, on this thread
+  std::vector<std::pair<int, int32_t>> where(jobs.size());
+  for(int p = 0; p < P; p++)
+    for(size_t k = 0; k < part[p].size(); k++) where[part[p][k]] = { p, ids[p][k] };
+  for(size_t i = 0; i < jobs.size(); i++) sch[where[i].first]->emit_deferred(where[i].second);
+  for(int p = 0; p < P; p++) {
+    add_stats(st, pst[p]);
+    sch[p].reset();
+  }
+  st.wall_ms += ms_since(t0);
+  return ST_OK;
+}
+
+}  // namespace
+
 int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats *stats, std::string &err)
 {
   std::lock_guard<std::mutex> g(g_mu);
@@ -2293,7 +2420,11 @@ int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats 
                                                  " is greater then the database size " +
                                                  std::to_string(j.db->host.n_graphs));
     }
+    int P = wave_opt.schedulers > 0 ? wave_opt.schedulers : (jobs.size() >= 16 ? (int)(jobs.size() / 8) : 1);
+    P = std::max(1, std::min<int>({ P, kMaxSchedulers, (int)jobs.size() }));
+    if(P > 1) return run_jobs_split(jobs, wave_opt, st, err, P);
     const clk::time_point t0 = clk::now();
+    g_engine.pool_limit = g_pool_limit;
     g_engine.init(wave_opt.threads);
     Sched s(g_engine, wave_opt, st);
     s.add_all(jobs);
@@ -2388,7 +2519,7 @@ int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptio
       b = std::min(b, st.wall_ms);
     }
     ms = b;
-    trials.push_back(TuneTrial{ o.wave_nodes, o.wave_rows, o.count_grid, o.deep_nodes, ms });
+    trials.push_back(TuneTrial{ o.wave_nodes, o.wave_rows, o.count_grid, o.deep_nodes, o.schedulers, ms });
     return ST_OK;
   };
   MineOptions cur = base;
@@ -2430,6 +2561,14 @@ int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptio
     o.deep_nodes = dn;
     if((rc = consider(o))) return rc;
   }
+  // a batch: the number of schedulers it is split over
+  if(jobs.size() >= 2)
+    for(int32_t sc : { 1, 2, 3, 4 }) {
+      if(sc == cur.schedulers || sc > (int32_t)jobs.size()) continue;
+      MineOptions o = cur;
+      o.schedulers = sc;
+      if((rc = consider(o))) return rc;
+    }
   best = cur;
   return ST_OK;
 }
@@ -2617,6 +2756,7 @@ void engine_reset()
   {
     std::lock_guard<std::mutex> g(g_mu);
     g_engine.destroy();
+    for(auto &e : g_extra) e.destroy();
   }
   ingest_release();
 }
@@ -2624,7 +2764,7 @@ void engine_reset()
 void engine_set_pool_bytes(int64_t bytes)
 {
   std::lock_guard<std::mutex> g(g_mu);
-  g_engine.pool_limit = bytes;
+  g_pool_limit = bytes;
 }
 
 }  // namespace gsgb

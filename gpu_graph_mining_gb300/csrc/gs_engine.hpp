@@ -130,6 +130,8 @@ struct MineOptions {
                               // right-most vertex (the reference's gspan_cuda_lists)
   int32_t deep_nodes = 0;     // a third wave context launches while this many nodes are queued (0 = wave_nodes)
   int32_t serial = 0;         // 1: every wave context issues on the engine's stream (no kernels overlap)
+  int32_t schedulers = 0;     // batches: jobs split over this many schedulers, each with its own engine and
+                              // host thread (0 = one per 8 jobs from 16 jobs on, at most 4; else 1)
 };
 
 struct MineStats {
@@ -242,6 +244,7 @@ struct TuneTrial {
   int64_t wave_rows;
   int32_t count_grid;
   int32_t deep_nodes;
+  int32_t schedulers;
   double ms;
 };
 int autotune_jobs(std::vector<MineJob> &jobs, const MineOptions &base, MineOptions &best,

@@ -409,11 +409,11 @@ KernelCall is_min_call(const NodeDesc *nodes, int32_t nnodes, const SlotDesc *sl
                        const int32_t *codes, int4 *sel, int32_t sel_cap, const unsigned long long *counters)
 {
   const size_t smem = sizeof(MinSmem) * kMinWarps;
-  static bool configured = false;
-  if(!configured) {
+  static const bool configured = [smem] {
     cudaFuncSetAttribute(k_is_min, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
-  }
+    return true;
+  }();
+  (void)configured;
   KernelCall c;
   c.func = (const void *)k_is_min;
   c.grid = dim3((unsigned)(2 * sm_count()));

@@ -448,11 +448,12 @@ k_wave(const WaveArgs a)
 template <int KMAX, bool MAT, bool MASK, bool JOIN> void launch_k(const WaveArgs &a, cudaStream_t s)
 {
   const size_t smem = sizeof(Smem<KMAX>) * kWarps;
-  static bool configured = false;
-  if(!configured) {
+  // once per instance (a thread-safe static: schedulers may launch from several threads)
+  static const bool configured = [smem] {
     cudaFuncSetAttribute(k_wave<KMAX, MAT, MASK, JOIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
-  }
+    return true;
+  }();
+  (void)configured;
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
   const long long cap = (long long)sm_count() * GS_WAVE_GRID;
   if(blocks > cap) blocks = cap;
@@ -482,11 +483,11 @@ template <bool MAT> void dispatch(int kmax, bool small_graphs, bool join, const 
 template <int KMAX, bool MASK, bool JOIN> KernelCall count_call_k(const WaveArgs &a, int grid_per_sm)
 {
   const size_t smem = sizeof(Smem<KMAX>) * kWarps;
-  static bool configured = false;
-  if(!configured) {
+  static const bool configured = [smem] {
     cudaFuncSetAttribute(k_wave<KMAX, false, MASK, JOIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = true;
-  }
+    return true;
+  }();
+  (void)configured;
   long long blocks = (a.total_tiles + kWarps - 1) / kWarps;
   const long long cap = (long long)sm_count() * (grid_per_sm > 0 ? grid_per_sm : GS_WAVE_GRID);
   if(blocks > cap) blocks = cap;

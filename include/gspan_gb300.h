@@ -195,6 +195,13 @@ typedef struct gs_mine_opts {
                           materialise passes run beside another wave's count (default); 1 = all on one
                           stream: no two kernels overlap, so per-kernel times in gs_mine_stats are
                           exclusive.  Same patterns and supports. */
+  int32_t schedulers;  /* gs_mine_batch: the databases split over this many schedulers, each with its own
+                          device pool, wave contexts and streams, run on their own host threads (the
+                          host's per-node work then uses that many cores while the GPU runs their waves
+                          side by side); 0 = one per 8 databases for batches of 16 or more, at most 4,
+                          else 1.  Patterns are
+                          emitted on the calling thread after all are mined, database by database in batch
+                          order.  Same patterns and supports. */
 } gs_mine_opts;
 
 #define GS_EXTENSION_RMPATH 0
@@ -354,6 +361,7 @@ typedef struct gs_tune_report {
   int32_t deep_nodes;
   double base_ms;  /* the starting options */
   double best_ms;  /* the tuned options */
+  int32_t schedulers;
 } gs_tune_report;
 GS_API gs_status gs_autotune(gs_db *const *dbs, int32_t n, const int32_t *abs_minsups, gs_mine_opts *opts,
                              gs_tune_report *report);

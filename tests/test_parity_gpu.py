@@ -320,6 +320,22 @@ def test_one_stream_equals_context_streams(gs):
     assert c == d and sc["waves"] == sd["waves"]
 
 
+def test_batch_split_over_schedulers_keeps_results(gs):
+    # the batch split over 1, 2 or 3 schedulers (own engines, own host
+    # threads): the same patterns for every database, in batch order
+    dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.03) for i in range(7)]
+    dbs.append(dbs[2])  # a database twice in one batch
+    sups = [max(2, int(0.05 * len(d))) for d in dbs]
+    a, sa = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, schedulers=1)
+    for p in (2, 3):
+        b, sb = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, schedulers=p)
+        assert a == b and sa["patterns"] == sb["patterns"]
+    assert a[2] == a[7]
+    for d, s, pats in zip(dbs, sups, a):
+        one, _ = gs.mine(d, s, label_style=gs.LABELS_SEQ)
+        assert one == pats
+
+
 def test_tight_pool_reuses_fenced_blocks(gs):
     # with the device pool capped near the run's peak, blocks released on the
     # host are handed out again only after every stream has passed their last
