@@ -354,7 +354,7 @@ def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave
 
 def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, collect=True, sink=None,
          wave_rows=0, wave_words=0, root_part=0, root_parts=1, min_check=0, launch_mode=0, count_grid=0,
-         extension=EXTENSION_RMPATH, deep_nodes=0, serial=0):
+         extension=EXTENSION_RMPATH, deep_nodes=0, serial=0, schedulers=0):
     """Mines db at absolute support minsup.
 
     Returns (patterns, stats): patterns is a list of (code, support) with code a
@@ -373,7 +373,7 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
 
     fn = EMIT_FN(cb) if (collect or sink is not None) else ctypes.cast(None, EMIT_FN)
     o = _opts(max_edges, label_style, wave_nodes, threads, wave_rows, wave_words, root_part, root_parts, min_check,
-              launch_mode, count_grid, extension, deep_nodes, serial)
+              launch_mode, count_grid, extension, deep_nodes, serial, schedulers)
     st = MineStats()
     _check(lib().gs_mine_ex(db.handle, int(minsup), ctypes.byref(o), fn, None, ctypes.byref(st)))
     return out, st.as_dict()

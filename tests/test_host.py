@@ -432,6 +432,15 @@ def test_option_structs_match_the_header(gs):
     assert gs._opts(extension="rmpath").extension == gs.EXTENSION_RMPATH
     with pytest.raises(ValueError):
         gs._opts(extension="bogus")
+    # gs_tune_report too, and every option the autotuner returns is a keyword
+    # of mine() (the bench passes the tuned options to single-database calls)
+    body = re.search(r"typedef struct gs_tune_report \{(.*?)\} gs_tune_report;", hdr, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    assert re.findall(r"\b(?:int32_t|int64_t|double)\s+(\w+);", body) == [f for f, _ in gs.TuneReport._fields_]
+    import inspect
+    params = set(inspect.signature(gs.mine).parameters) & set(inspect.signature(gs._opts).parameters)
+    for f, _ in gs.MineOpts._fields_:
+        assert f in params, f
 
 
 def test_drop_in_shim_compiles_against_the_reference(tmp_path):
