@@ -595,6 +595,7 @@ struct JobState {
   int32_t db_slot = 0;
   std::vector<PatternRec> pats;
   std::vector<int32_t> roots;
+  std::vector<int32_t> root_keys;  // each root's key (root_off[fl] + pair): the reference's root order
   std::vector<int32_t> stack;  // DFS-tree nodes waiting for a wave (top = back), as node pool ids
   int64_t pending = 0;         // nodes on the stack or in a wave in flight
   int64_t live_bytes = 0;      // embedding-store bytes held by the job's nodes
@@ -1382,6 +1383,7 @@ private:
     }
     std::vector<PatternRec>().swap(S.pats);
     std::vector<int32_t>().swap(S.roots);
+    std::vector<int32_t>().swap(S.root_keys);
   }
 
 public:
@@ -1396,8 +1398,24 @@ public:
       ScopeMs t(st_.host_emit_ms);
       emit(S);
     }
+    release_patterns(id);
+  }
+  // a job split by root subtrees: its parts' roots are merged in the
+  // reference's root order (root keys), one root subtree at a time
+  const std::vector<int32_t> &root_keys(int32_t id) const { return jobs_[id]->root_keys; }
+  void emit_root(int32_t id, size_t r)
+  {
+    JobState &S = *jobs_[id];
+    if(!S.done || S.cancelled) return;
+    ScopeMs t(st_.host_emit_ms);
+    emit(S, r, r + 1);
+  }
+  void release_patterns(int32_t id)
+  {
+    JobState &S = *jobs_[id];
     std::vector<PatternRec>().swap(S.pats);
     std::vector<int32_t>().swap(S.roots);
+    std::vector<int32_t>().swap(S.root_keys);
   }
 
 private:
@@ -1530,6 +1548,7 @@ private:
           S.pats.push_back(pr);
           const int32_t pid = (int32_t)S.pats.size() - 1;
           S.roots.push_back(pid);
+          S.root_keys.push_back(key - kb);
           if(!extend) continue;
           const int64_t rows = hcnt[key];
           sel.push_back(Sel{ key, pid, pr.edge, sup, rows });
@@ -2242,10 +2261,12 @@ private:
   }
 
   // pre-order traversal of a job's pattern tree, codes in the caller's labels
-  void emit(JobState &S)
+  // the patterns of roots r0..r1-1 (all by default), each root's subtree in pre-order
+  void emit(JobState &S, size_t r0 = 0, size_t r1 = SIZE_MAX)
   {
     const MineJob &j = S.job;
     if(!j.emit) return;
+    r1 = std::min(r1, S.roots.size());
     const LabelMap &lm = j.db->labels;
     std::vector<DFS> path, styled, orig;
     std::vector<int32_t> flat;
@@ -2272,7 +2293,8 @@ private:
       }
       j.emit(flat.data(), (int32_t)n, S.pats[pid].support, j.user);
     };
-    for(int32_t r : S.roots) {
+    for(size_t ri = r0; ri < r1; ri++) {
+      const int32_t r = S.roots[ri];
       path.assign(1, S.pats[r].edge);
       out(r);
       st.assign(1, Frame{ r, S.pats[r].first_child });
@@ -2326,10 +2348,29 @@ void add_stats(MineStats &a, const MineStats &b)
 // fewest graphs so far (largest first); each scheduler mines its jobs as one
 // batch.  Patterns are emitted afterwards on the calling thread, job by job
 // in batch order.
-int run_jobs_split(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats &st, std::string &err,
+int run_jobs_split(std::vector<MineJob> &batch, const MineOptions &wave_opt, MineStats &st, std::string &err,
                    int P)
 {
   const clk::time_point t0 = clk::now();
+  // the schedulers' jobs: a batch's jobs as they are, or one job split into P
+  // parts by root subtrees (part p mines the roots whose index in the
+  // reference's order is its own residue, within the job's own partition)
+  std::vector<MineJob> jobs;
+  std::vector<int32_t> orig;
+  if(batch.size() == 1) {
+    const MineJob &j0 = batch[0];
+    const int32_t RP = j0.opt.root_parts > 1 ? j0.opt.root_parts : 1, rp = RP > 1 ? j0.opt.root_part : 0;
+    for(int p = 0; p < P; p++) {
+      MineJob j = j0;
+      j.opt.root_parts = RP * P;
+      j.opt.root_part = rp + RP * p;
+      jobs.push_back(j);
+      orig.push_back(0);
+    }
+  } else {
+    jobs = batch;
+    for(size_t i = 0; i < batch.size(); i++) orig.push_back((int32_t)i);
+  }
   // databases resident before the threads start (a database may appear twice)
   for(auto &j : jobs)
     if(!j.db->resident) {
@@ -2343,10 +2384,14 @@ int run_jobs_split(std::vector<MineJob> &jobs, const MineOptions &wave_opt, Mine
   });
   std::vector<std::vector<int32_t>> part(P);
   std::vector<int64_t> load(P, 0);
-  for(int32_t i : order) {
-    const int p = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    part[p].push_back(i);
-    load[p] += jobs[i].db->host.n_graphs;
+  if(batch.size() == 1) {
+    for(int p = 0; p < P; p++) part[p].push_back(p);
+  } else {
+    for(int32_t i : order) {
+      const int p = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      part[p].push_back(i);
+      load[p] += jobs[i].db->host.n_graphs;
+    }
   }
   for(auto &v : part) std::sort(v.begin(), v.end());
   std::vector<MineStats> pst(P);
@@ -2395,7 +2440,26 @@ int run_jobs_split(std::vector<MineJob> &jobs, const MineOptions &wave_opt, Mine
   std::vector<std::pair<int, int32_t>> where(jobs.size());
   for(int p = 0; p < P; p++)
     for(size_t k = 0; k < part[p].size(); k++) where[part[p][k]] = { p, ids[p][k] };
-  for(size_t i = 0; i < jobs.size(); i++) sch[where[i].first]->emit_deferred(where[i].second);
+  if(batch.size() == 1) {
+    // one job's parts: root subtrees merged in root-key order
+    std::vector<size_t> cur(jobs.size(), 0);
+    for(;;) {
+      int best = -1;
+      int32_t bk = 0;
+      for(size_t q = 0; q < jobs.size(); q++) {
+        const auto &rk = sch[where[q].first]->root_keys(where[q].second);
+        if(cur[q] < rk.size() && (best < 0 || rk[cur[q]] < bk)) {
+          best = (int)q;
+          bk = rk[cur[q]];
+        }
+      }
+      if(best < 0) break;
+      sch[where[best].first]->emit_root(where[best].second, cur[best]++);
+    }
+    for(size_t q = 0; q < jobs.size(); q++) sch[where[q].first]->release_patterns(where[q].second);
+  } else {
+    for(size_t i = 0; i < jobs.size(); i++) sch[where[i].first]->emit_deferred(where[i].second);
+  }
   for(int p = 0; p < P; p++) {
     add_stats(st, pst[p]);
     sch[p].reset();
@@ -2420,8 +2484,10 @@ int run_jobs(std::vector<MineJob> &jobs, const MineOptions &wave_opt, MineStats 
                                                  " is greater then the database size " +
                                                  std::to_string(j.db->host.n_graphs));
     }
+    // a batch: one scheduler per 8 jobs from 16 on; one job: split by root
+    // subtrees only when asked
     int P = wave_opt.schedulers > 0 ? wave_opt.schedulers : (jobs.size() >= 16 ? (int)(jobs.size() / 8) : 1);
-    P = std::max(1, std::min<int>({ P, kMaxSchedulers, (int)jobs.size() }));
+    P = std::max(1, std::min<int>({ P, kMaxSchedulers, jobs.size() == 1 ? kMaxSchedulers : (int)jobs.size() }));
     if(P > 1) return run_jobs_split(jobs, wave_opt, st, err, P);
     const clk::time_point t0 = clk::now();
     g_engine.pool_limit = g_pool_limit;

@@ -201,7 +201,10 @@ typedef struct gs_mine_opts {
                           side by side); 0 = one per 8 databases for batches of 16 or more, at most 4,
                           else 1.  Patterns are
                           emitted on the calling thread after all are mined, database by database in batch
-                          order.  Same patterns and supports. */
+                          order.  For one database (gs_mine_ex, gs_mine_collect) a value above 1 splits it
+                          by root subtrees (part p takes the roots whose index in the reference's order is p
+                          modulo P), the patterns merged back in the reference's order; 0 = not split.
+                          Same patterns, supports and order. */
 } gs_mine_opts;
 
 #define GS_EXTENSION_RMPATH 0

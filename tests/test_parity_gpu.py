@@ -336,6 +336,22 @@ def test_batch_split_over_schedulers_keeps_results(gs):
         assert one == pats
 
 
+def test_one_database_split_by_root_subtrees_keeps_order(gs):
+    # one database mined by 2-4 schedulers, each taking every P-th root
+    # subtree on its own thread: the same patterns in the reference's order
+    db = gs.Database.generate(2, scale=0.1)
+    s = max(2, int(0.01 * len(db)))
+    a, sa = gs.mine(db, s, label_style=gs.LABELS_SEQ)
+    for p in (2, 3, 4):
+        b, sb = gs.mine(db, s, label_style=gs.LABELS_SEQ, schedulers=p)
+        assert a == b and sa["patterns"] == sb["patterns"]
+        c, _ = gs.mine(db, s, label_style=gs.LABELS_SEQ, schedulers=p, root_part=1, root_parts=2)
+        d, _ = gs.mine(db, s, label_style=gs.LABELS_SEQ, root_part=1, root_parts=2)
+        assert c == d
+    lines, _ = _mine_lines(gs, gs.Database.load(os.path.join(GOLDEN, "cfg1_seed1.txt"), "txt"), 10, schedulers=3)
+    assert lines == read_lines(os.path.join(GOLDEN, "out_cfg1_seed1_s10.txt"))
+
+
 def test_tight_pool_reuses_fenced_blocks(gs):
     # with the device pool capped near the run's peak, blocks released on the
     # host are handed out again only after every stream has passed their last
