@@ -24,6 +24,7 @@
 #include <deque>
 #include <functional>
 #include <map>
+#include <system_error>
 #include <thread>
 #include <unordered_map>
 
@@ -2422,9 +2423,17 @@ int run_jobs_split(std::vector<MineJob> &batch, const MineOptions &wave_opt, Min
     }
   };
   std::vector<std::thread> th;
+  std::vector<int> inline_parts;  // parts whose thread could not be started run here
   for(int p = 1; p < P; p++)
-    if(!part[p].empty()) th.emplace_back(work, p);
+    if(!part[p].empty()) {
+      try {
+        th.emplace_back(work, p);
+      } catch(const std::system_error &) {
+        inline_parts.push_back(p);
+      }
+    }
   if(!part[0].empty()) work(0);
+  for(int p : inline_parts) work(p);
   for(auto &t : th) t.join();
   for(int p = 0; p < P; p++)
     if(prc[p] != ST_OK) {
