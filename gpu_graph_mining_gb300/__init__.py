@@ -59,6 +59,7 @@ class MineOpts(ctypes.Structure):
 # extension strategies (gs_mine_opts.extension)
 EXTENSION_RMPATH = 0
 EXTENSION_LISTS = 1
+EXTENSION_AUTO = 2
 
 
 class ConvertInfo(ctypes.Structure):
@@ -319,9 +320,11 @@ def code_to_string(code):
 def _extension(x):
     if x in (EXTENSION_RMPATH, "rmpath", None):
         return EXTENSION_RMPATH
+    if x in (EXTENSION_AUTO, "auto"):
+        return EXTENSION_AUTO
     if x in (EXTENSION_LISTS, "lists"):
         return EXTENSION_LISTS
-    raise ValueError("extension must be 'rmpath' or 'lists'")
+    raise ValueError("extension must be 'auto', 'rmpath' or 'lists'")
 
 
 def _opts(max_edges=0, label_style=LABELS_FULL, wave_nodes=None, threads=0, wave_rows=0, wave_words=0,
@@ -360,7 +363,8 @@ def mine(db, minsup, max_edges=0, label_style=LABELS_FULL, wave_nodes=None, thre
     Returns (patterns, stats): patterns is a list of (code, support) with code a
     tuple of 5-tuples, in the reference's traversal order (empty when
     collect=False); sink(code, support) is called per pattern if given.
-    extension="lists" selects the reference's lists (intersection) strategy.
+    extension: "rmpath" (default), "lists" (the reference's lists (intersection)
+    strategy) or "auto" (the lists for the waves whose databases do not stay in L2).
     """
     out = []
 

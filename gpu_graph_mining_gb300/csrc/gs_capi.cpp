@@ -51,7 +51,7 @@ void fill_opts(const gs_mine_opts *o, gsgb::MineOptions &m)
   m.min_check = o->min_check == 1 ? 1 : 0;
   m.launch_mode = o->launch_mode == 1 ? 1 : 0;
   if(o->count_grid > 0 && o->count_grid <= 1024) m.count_grid = o->count_grid;
-  m.extension = o->extension == GS_EXTENSION_LISTS ? 1 : 0;
+  m.extension = o->extension == GS_EXTENSION_LISTS ? 1 : o->extension == GS_EXTENSION_AUTO ? 2 : 0;
   if(o->deep_nodes > 0) m.deep_nodes = o->deep_nodes;
   m.serial = o->serial == 1 ? 1 : 0;
   if(o->schedulers > 0 && o->schedulers <= 64) m.schedulers = o->schedulers;

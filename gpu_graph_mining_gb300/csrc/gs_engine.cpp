@@ -1113,6 +1113,7 @@ struct Flight {
   int32_t W = 0, kb = 0, kmax = 1;
   bool small = true;
   bool rule_skip = false;    // the count kernel bisects past forward-rule prefixes
+  bool lists = false;        // the wave builds its children's parent-row lists (lists strategy)
   int64_t tb = 0;
   int4 *rec = nullptr;
   long long rec_cap = 0;
@@ -1840,6 +1841,9 @@ private:
     // faster) and cost more than the skipped items save beyond it
     // (configuration 5, 960 MB: 10% slower)
     f.rule_skip = adj_bytes <= rule_skip_adj_bytes();
+    // lists strategy: always (1), or (2) for waves whose databases do not stay
+    // in L2, where the joins save rescans of adjacency from DRAM
+    f.lists = wo_.extension == 1 || (wo_.extension == 2 && !f.rule_skip);
     f.tb = tb;
     // copies of the wave's counters: the warps of a large node all add into that
     // node's few counters; copies spread them over L2 slices (summed by screening)
@@ -1900,7 +1904,7 @@ private:
                               err_flag(), f.rec, f.rec_cap, f.rec ? head + kHeadRecords : nullptr,
                               wo_.count_grid, ccopies, cstride, f.join, f.rule_skip);
     int32_t *lnode = nullptr;
-    if(wo_.extension == 1) {
+    if(f.lists) {
       X.d_lnode.ensure(std::max(kb, 1));
       lnode = X.d_lnode.p;
     }
@@ -2104,7 +2108,7 @@ private:
         }
         a0 = a1;
       }
-      if(wo_.extension == 1 && f.rec && nrec >= 0 && nrec <= f.rec_cap) {
+      if(f.lists && f.rec && nrec >= 0 && nrec <= f.rec_cap) {
         list_rb.assign(W, -1);
         std::vector<char> need(W, 0);
         for(const Mat &m : mats)

@@ -127,7 +127,8 @@ struct MineOptions {
   int32_t extension = 0;      // extension strategy: 0 every right-most-path vertex's adjacency is
                               // scanned; 1 lists: forward children join their parent's per-row
                               // lists of frequent forward extensions and scan only their new
-                              // right-most vertex (the reference's gspan_cuda_lists)
+                              // right-most vertex (the reference's gspan_cuda_lists); 2 lists for
+                              // waves whose databases' adjacency does not stay in L2, else 0
   int32_t deep_nodes = 0;     // a third wave context launches while this many nodes are queued (0 = wave_nodes)
   int32_t serial = 0;         // 1: every wave context issues on the engine's stream (no kernels overlap)
   int32_t schedulers = 0;     // batches: jobs split over this many schedulers, each with its own engine and

@@ -263,7 +263,7 @@ private:
     wo_ = MineOptions();
     if(opt_.wave_nodes > 0) wo_.wave_nodes = opt_.wave_nodes;
     if(opt_.threads > 0) wo_.threads = opt_.threads;
-    wo_.extension = opt_.extension == GS_EXTENSION_LISTS ? 1 : 0;
+    wo_.extension = opt_.extension == GS_EXTENSION_LISTS ? 1 : opt_.extension == GS_EXTENSION_AUTO ? 2 : 0;
     sched_.reset(new Scheduler(wo_, opt_.pool_bytes));
     budget_ = opt_.budget_bytes;
     if(budget_ <= 0) {
@@ -470,7 +470,7 @@ gs_status gs_server_create(const gs_server_opts *opts, gs_server **out)
     gsgb::capi_set_error("unknown label style");
     return GS_ERR_USAGE;
   }
-  if(o.extension != GS_EXTENSION_RMPATH && o.extension != GS_EXTENSION_LISTS) {
+  if(o.extension != GS_EXTENSION_RMPATH && o.extension != GS_EXTENSION_LISTS && o.extension != GS_EXTENSION_AUTO) {
     gsgb::capi_set_error("unknown extension strategy");
     return GS_ERR_USAGE;
   }

@@ -180,13 +180,16 @@ typedef struct gs_mine_opts {
   int32_t launch_mode; /* a wave's device work (uploads, clears, count, selection, check, results
                           copy): 0 = replayed from a per-variant CUDA graph, 1 = launched directly */
   int32_t count_grid;  /* count-kernel grid cap in blocks per SM; 0 = built-in default (64) */
-  int32_t extension;   /* extension strategy: GS_EXTENSION_RMPATH (default) scans the adjacency of
-                          every right-most-path vertex of every embedding; GS_EXTENSION_LISTS is
-                          the reference's lists variant (gspan_cuda_lists, main_gspan_cuda_lists.cpp):
+  int32_t extension;   /* extension strategy: GS_EXTENSION_RMPATH (default) scans the adjacency of every
+                          right-most-path vertex of every embedding; GS_EXTENSION_LISTS is the
+                          reference's lists variant (gspan_cuda_lists, main_gspan_cuda_lists.cpp):
                           a forward child takes its extensions from the right-most path's older
                           vertices by joining its parent's frequent forward extensions at the same
                           parent row (extend_embeddings.cpp:206-330, intersection_fwd_fwd) and
-                          scans only its new right-most vertex.  Same patterns and supports. */
+                          scans only its new right-most vertex; GS_EXTENSION_AUTO uses the lists
+                          for the waves whose databases' adjacency is larger than three quarters of
+                          the L2 (rescans from DRAM), the plain scan otherwise.  Same patterns and
+                          supports. */
   int32_t deep_nodes;  /* a third wave may be in flight (besides two) while at least this many DFS-tree
                           nodes are queued; 0 = wave_nodes (default), 1 = always.  More waves in flight
                           hide more of the host's work per wave when a workload has many small nodes;
@@ -209,6 +212,7 @@ typedef struct gs_mine_opts {
 
 #define GS_EXTENSION_RMPATH 0
 #define GS_EXTENSION_LISTS 1
+#define GS_EXTENSION_AUTO 2
 
 typedef struct gs_mine_stats {
   int64_t patterns;
@@ -299,7 +303,8 @@ typedef struct gs_server_opts {
   int32_t wave_nodes;   /* DFS-tree nodes per launch; 0 = default */
   int32_t threads;      /* host threads for the canonicality check; 0 = all cores */
   int32_t label_style;  /* GS_LABELS_FULL or GS_LABELS_SEQ for the results */
-  int32_t extension;    /* GS_EXTENSION_RMPATH (default) or GS_EXTENSION_LISTS, as in gs_mine_opts */
+  int32_t extension;    /* GS_EXTENSION_RMPATH (default), GS_EXTENSION_LISTS or GS_EXTENSION_AUTO, as in
+                           gs_mine_opts */
   int32_t reserved;
 } gs_server_opts;
 

@@ -428,6 +428,8 @@ def test_option_structs_match_the_header(gs):
     o = gs.MineOpts()
     gs.lib().gs_mine_opts_default(ctypes.byref(o))
     assert o.extension == gs.EXTENSION_RMPATH
+    assert gs._opts().extension == gs.EXTENSION_RMPATH
+    assert gs._opts(extension="auto").extension == gs.EXTENSION_AUTO
     assert gs._opts(extension="lists").extension == gs.EXTENSION_LISTS
     assert gs._opts(extension="rmpath").extension == gs.EXTENSION_RMPATH
     with pytest.raises(ValueError):

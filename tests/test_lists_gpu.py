@@ -152,3 +152,19 @@ def test_lists_root_partition(gs):
     want, _ = gs.mine_collect(db, s)
     parts = [gs.mine_collect(db, s, root_part=r, root_parts=3, extension="lists")[0] for r in range(3)]
     assert merge_root_partitions(parts) == want
+
+
+def test_auto_extension_joins_only_where_the_database_leaves_l2(gs):
+    # auto: the lists for waves whose databases' adjacency is larger than
+    # three quarters of the L2 (configuration 5 at 0.15 scale: about 145 MB),
+    # the plain scan where it stays in L2 (configuration 2 at 0.1 scale)
+    big = gs.Database.generate(5, scale=0.15)
+    s = max(2, int(round(0.005 * len(big))))
+    a, sa = gs.mine(big, s, label_style=gs.LABELS_SEQ)
+    b, sb = gs.mine(big, s, label_style=gs.LABELS_SEQ, extension="auto")
+    assert a == b and sb["join_nodes"] > 0 and sa["join_nodes"] == 0
+    small = gs.Database.generate(2, scale=0.1)
+    s = max(2, int(0.01 * len(small)))
+    c, _ = gs.mine(small, s, label_style=gs.LABELS_SEQ)
+    d, sd = gs.mine(small, s, label_style=gs.LABELS_SEQ, extension="auto")
+    assert c == d and sd["join_nodes"] == 0
