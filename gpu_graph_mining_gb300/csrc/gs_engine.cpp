@@ -2361,7 +2361,6 @@ int run_jobs_split(std::vector<MineJob> &batch, const MineOptions &wave_opt, Min
   // parts by root subtrees (part p mines the roots whose index in the
   // reference's order is its own residue, within the job's own partition)
   std::vector<MineJob> jobs;
-  std::vector<int32_t> orig;
   if(batch.size() == 1) {
     const MineJob &j0 = batch[0];
     const int32_t RP = j0.opt.root_parts > 1 ? j0.opt.root_parts : 1, rp = RP > 1 ? j0.opt.root_part : 0;
@@ -2370,11 +2369,9 @@ int run_jobs_split(std::vector<MineJob> &batch, const MineOptions &wave_opt, Min
       j.opt.root_parts = RP * P;
       j.opt.root_part = rp + RP * p;
       jobs.push_back(j);
-      orig.push_back(0);
     }
   } else {
     jobs = batch;
-    for(size_t i = 0; i < batch.size(); i++) orig.push_back((int32_t)i);
   }
   // databases resident before the threads start (a database may appear twice)
   for(auto &j : jobs)
