@@ -465,3 +465,27 @@ def test_drop_in_shim_compiles_against_the_reference(tmp_path):
     assert "get_gspan_cuda_instance()" in nm
     for sym in ("gs_db_from_arrays_device", "gs_mine", "gs_db_free", "gs_last_error"):
         assert sym in nm, sym
+
+
+def test_bench_roofline_and_traffic_helpers():
+    # the bench line's roofline block from kernel-side counters: the count
+    # kernel on top, the others beside it, their exclusive (one-stream) times,
+    # and the committed DRAM/algorithmic ratio applied per launch
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(REPO, "bench.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    st = {"count_bytes": 2.0e11, "count_ms": 100.0, "mat_bytes": 9.0e10, "mat_ms": 20.0, "sel_bytes": 1.5e9,
+          "sel_ms": 3.0, "min_ms": 2.5, "waves": 110}
+    ser = dict(st, count_ms=90.0)
+    r = b.roofline([st, st], 6700.0, "measured", None, None, [ser])
+    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["kernel"] == "k_wave count"
+    assert abs(r["achieved"] - 2000.0) < 1e-6 and abs(r["frac"] - 2000.0 / 6700.0) < 1e-12
+    assert r["launches_per_step"] == 110
+    assert set(r["kernels"]) == set(r["kernels_one_stream"])
+    assert abs(r["kernels_one_stream"]["k_wave count"]["achieved"] - 2.0e11 / 0.09 / 1e9) < 1e-6
+    t, note = b.count_traffic("config5", 2.0e11, 100)
+    ratio = json.load(open(os.path.join(REPO, "profiles", "k_wave_count_traffic_config5.json")))
+    expect = ratio["dram_bytes_per_pass"] / ratio["algorithmic_bytes_per_pass"] * 2.0e9
+    assert abs(t - expect) < 1.0 and "k_wave_count_traffic_config5.json" in note
+    assert b.count_traffic("nonexistent", 1.0, 1) == (None, None)
