@@ -336,6 +336,26 @@ def test_batch_split_over_schedulers_keeps_results(gs):
         assert one == pats
 
 
+def test_batch_split_reports_a_scheduler_error_and_recovers(gs):
+    # a device pool too small for any wave: every scheduler of a split batch
+    # fails with GS_ERR_NOMEM, the call reports it, and the engines mine
+    # normally again once the limit is lifted
+    dbs = [gs.Database.generate(3, seed=1000 + i, scale=0.03) for i in range(16)]
+    sups = [max(2, int(0.05 * len(d))) for d in dbs]
+    want, _ = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, schedulers=2)
+    try:
+        gs.engine_reset()
+        gs.set_pool_bytes(4096)
+        with pytest.raises(gs.GSpanError) as ei:
+            gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, schedulers=2)
+        assert ei.value.status == 5  # GS_ERR_NOMEM
+    finally:
+        gs.set_pool_bytes(0)
+        gs.engine_reset()
+    got, _ = gs.mine_batch(dbs, sups, label_style=gs.LABELS_SEQ, schedulers=2)
+    assert got == want
+
+
 def test_one_database_split_by_root_subtrees_keeps_order(gs):
     # one database mined by 2-4 schedulers, each taking every P-th root
     # subtree on its own thread: the same patterns in the reference's order
